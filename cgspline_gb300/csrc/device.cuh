@@ -1,0 +1,842 @@
+// device.cuh -- device-side data layout and routines of the ray--bicubic-patch
+// path: hashed stackless BVH traversal, Bezier clipping / subdivision on the
+// projected control net, FP64 Newton polish, PBR shading.
+//
+// Reference citations are relative to the MachSilva/cgspline project root.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cgs {
+
+constexpr uint32_t EMPTY = 0xFFFFFFFFu;
+constexpr int kClipStack = 32;          // reference stack depth, src/Spline_BezierClipping.cu:577
+constexpr int kMaxClipIterations = 4096;
+constexpr int kMaxTraversalSteps = 1 << 20;
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.318309886183790671538f;
+
+// Error bits reported through Counters::errors.
+enum : uint32_t { kErrClipStack = 1u, kErrClipIterations = 2u, kErrTraversal = 4u };
+
+// ------------------------------------------------------------ data layout --
+// One BVH (a surface's patch BVH or the object-level BVH).  Node offsets in
+// the nodes / indices are relative to nodeBase / indexBase, as the
+// reference's Node::left/right/first are relative to its own arrays
+// (src/rt/BVH.h:23-39).
+struct DevBVH
+{
+    uint32_t nodeBase, indexBase, tableBase, dispBase;
+    uint32_t A, B, N, mask;  // h(k) = (A k + B + disp[k & mask]) mod N, src/rt/PerfectHashFunction.h:58-63
+};
+
+struct DevObject  // one row of Scene::ObjectArrays, src/rt/Scene.h:109-112
+{
+    float w2l[16];            // column-major world -> local
+    uint32_t surface;
+    uint32_t material;        // index into materials
+    int32_t patchMaterialBase;  // >= 0: per-patch material indices start here
+    uint32_t pad;
+};
+
+struct DevMaterial { float diffuse[3]; float specular[3]; float metalness; float roughness; };
+struct DevLight { float color[3]; float strength; float position[3]; float range; float direction[3]; float angle; };
+
+// Scene in HBM.  Nodes are 64 B (4 x float4):
+//   q0 = leftBox.lo.xyz, leftBox.hi.x   q1 = leftBox.hi.yz, rightBox.lo.xy
+//   q2 = rightBox.lo.z, rightBox.hi.xyz q3 = left, right|first (uint bits), 0, 0
+// Patches are de-indexed: 16 float4 (256 B) per patch, point (i,j) at 4j+i.
+struct DevScene
+{
+    const float4* patches;
+    const float4* nodes;
+    const uint32_t* indices;
+    const uint32_t* tables;
+    const uint32_t* disps;
+    const DevBVH* bvhs;        // [nsurfaces] patch BVHs, then the object-level BVH
+    const uint32_t* patchBase; // first global patch of each surface
+    const DevObject* objects;
+    const DevMaterial* materials;
+    const uint32_t* patchMaterial;
+    const DevLight* lights;
+    uint32_t nobjects, nlights, nsurfaces, topBVH;
+    float background[3], ambient[3];
+};
+
+struct Counters
+{
+    unsigned long long nodes, hashLookups, candidates, iterations, rays, errors;
+};
+
+struct LocalCounters
+{
+    uint32_t nodes = 0, hashLookups = 0, candidates = 0, iterations = 0;
+    uint32_t errors = 0;
+};
+
+// ------------------------------------------------------------ float math --
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float len(float3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ float3 cross(float3 a, float3 b)
+{
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 versor(float3 a)
+{
+    float l = len(a);
+    if (l != 0.0f) { float k = 1.0f / l; a = a * k; }
+    return a;
+}
+__device__ __forceinline__ float vmax3(float3 a) { return fmaxf(fmaxf(a.x, a.y), a.z); }
+__device__ __forceinline__ float3 xyz(float4 p) { return f3(p.x, p.y, p.z); }
+__device__ __forceinline__ float3 project(float4 p) { return f3(p.x / p.w, p.y / p.w, p.z / p.w); }  // src/AlignedTypes.h:63-66
+
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 operator*(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ float dot2(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ float len2(float2 a) { return sqrtf(dot2(a, a)); }
+
+// Column-major 4x4 times (x,y,z,1) / times (x,y,z,0).
+__device__ __forceinline__ float4 m4_point(const float* m, float3 p)
+{
+    return make_float4(p.x * m[0] + p.y * m[4] + p.z * m[8] + m[12], p.x * m[1] + p.y * m[5] + p.z * m[9] + m[13],
+                       p.x * m[2] + p.y * m[6] + p.z * m[10] + m[14], p.x * m[3] + p.y * m[7] + p.z * m[11] + m[15]);
+}
+__device__ __forceinline__ float3 m3_vec(const float* m, float3 v)
+{
+    return f3(v.x * m[0] + v.y * m[4] + v.z * m[8], v.x * m[1] + v.y * m[5] + v.z * m[9],
+              v.x * m[2] + v.y * m[6] + v.z * m[10]);
+}
+__device__ __forceinline__ float3 m3T_vec(const float* m, float3 v)  // mat3(M)^T * v
+{
+    return f3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+              m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+
+// ------------------------------------------------ power-basis evaluation --
+// Bernstein weights as CUBIC_BASE * [1 t t^2 t^3] (src/SplineMat.h:22-28,101-105)
+__device__ __forceinline__ float4 basis(float t)
+{
+    float t2 = t * t, t3 = t2 * t;
+    return make_float4(1.0f - 3.0f * t + 3.0f * t2 - t3, 3.0f * t - 6.0f * t2 + 3.0f * t3, 3.0f * t2 - 3.0f * t3, t3);
+}
+// CUBIC_DERIVATIVE_BASE * [1 t t^2 0] (src/SplineMat.h:38-44,107-110)
+__device__ __forceinline__ float4 dbasis(float t)
+{
+    float t2 = t * t;
+    return make_float4(-3.0f + 6.0f * t - 3.0f * t2, 3.0f - 12.0f * t + 9.0f * t2, 6.0f * t - 9.0f * t2, 3.0f * t2);
+}
+__device__ __forceinline__ float4 comb(float4 w, float4 a, float4 b, float4 c, float4 d)
+{
+    return make_float4(w.x * a.x + w.y * b.x + w.z * c.x + w.w * d.x, w.x * a.y + w.y * b.y + w.z * c.y + w.w * d.y,
+                       w.x * a.z + w.y * b.z + w.z * c.z + w.w * d.z, w.x * a.w + w.y * b.w + w.z * c.w + w.w * d.w);
+}
+// mat::interpolate (src/SplineMat.h:125-140); wu weights along u (i), wv along v (j)
+__device__ __forceinline__ float4 tensor_eval(const float4* __restrict__ P, float4 wu, float4 wv)
+{
+    float4 A0 = comb(wu, __ldg(P + 0), __ldg(P + 1), __ldg(P + 2), __ldg(P + 3));
+    float4 A1 = comb(wu, __ldg(P + 4), __ldg(P + 5), __ldg(P + 6), __ldg(P + 7));
+    float4 A2 = comb(wu, __ldg(P + 8), __ldg(P + 9), __ldg(P + 10), __ldg(P + 11));
+    float4 A3 = comb(wu, __ldg(P + 12), __ldg(P + 13), __ldg(P + 14), __ldg(P + 15));
+    return comb(wv, A0, A1, A2, A3);
+}
+// mat::normal (src/SplineMat.h:178-187), not normalized
+__device__ __forceinline__ float3 patch_normal(const float4* __restrict__ P, float u, float v)
+{
+    float4 dU = tensor_eval(P, dbasis(u), basis(v));
+    float4 dV = tensor_eval(P, basis(u), dbasis(v));
+    return cross(xyz(dU), xyz(dV));
+}
+
+// ------------------------------------------------------------- slicing --
+// mat::slice_matrix (src/SplineMat.h:64-82) applied as mat::slice
+// (src/SplineMat.h:189-206): P_j <- sum_k M[j][k] P_k, M's columns below.
+struct SliceM { float m[4][4]; };
+__device__ __forceinline__ SliceM slice_matrix(float a, float b)
+{
+    const float a2 = a * a, b2 = b * b, ia = 1.0f - a, ib = 1.0f - b, ia2 = ia * ia, ib2 = ib * ib,
+                k1 = a + 2.0f * b - 3.0f * a * b, k2 = 2.0f * a + b - 3.0f * a * b;
+    SliceM M;
+    M.m[0][0] = ia2 * ia; M.m[0][1] = 3.0f * a * ia2; M.m[0][2] = 3.0f * a2 * ia; M.m[0][3] = a2 * a;
+    M.m[1][0] = ia2 * ib; M.m[1][1] = ia * k2; M.m[1][2] = a * k1; M.m[1][3] = a2 * b;
+    M.m[2][0] = ia * ib2; M.m[2][1] = ib * k1; M.m[2][2] = b * k2; M.m[2][3] = a * b2;
+    M.m[3][0] = ib2 * ib; M.m[3][1] = 3.0f * b * ib2; M.m[3][2] = 3.0f * b2 * ib; M.m[3][3] = b2 * b;
+    return M;
+}
+template<int stride> __device__ __forceinline__ void apply_slice(float2* c, const SliceM& M)
+{
+    float2 p0 = c[0], p1 = c[stride], p2 = c[2 * stride], p3 = c[3 * stride];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+    {
+        float2 r;
+        r.x = M.m[j][0] * p0.x + M.m[j][1] * p1.x + M.m[j][2] * p2.x + M.m[j][3] * p3.x;
+        r.y = M.m[j][0] * p0.y + M.m[j][1] * p1.y + M.m[j][2] * p2.y + M.m[j][3] * p3.y;
+        c[j * stride] = r;
+    }
+}
+// mat::subpatchU / subpatchV (src/SplineMat.h:221-233)
+__device__ __forceinline__ void subpatchU(float2* p, float a, float b)
+{
+    SliceM M = slice_matrix(a, b);
+#pragma unroll
+    for (int i = 0; i < 4; i++) apply_slice<1>(p + 4 * i, M);
+}
+__device__ __forceinline__ void subpatchV(float2* p, float a, float b)
+{
+    SliceM M = slice_matrix(a, b);
+#pragma unroll
+    for (int i = 0; i < 4; i++) apply_slice<4>(p + i, M);
+}
+
+// -------------------------------------------------------- clip helpers --
+// xAxisIntersection, src/Spline_BezierClipping.cu:127-156
+__device__ __forceinline__ bool xAxisIntersection(float& lo, float& hi, float2 A, float2 B)
+{
+    const float eps = 1.1920928955078125e-07f;  // FLT_EPSILON
+    float q = A.y - B.y;
+    if (fabsf(q) > eps)
+    {
+        float t = A.y / q;
+        if (0.0f <= t && t <= 1.0f)
+        {
+            float s = (1.0f - t) * A.x + t * B.x;
+            lo = s; hi = s;
+            return true;
+        }
+    }
+    else if (fabsf(A.y) <= eps)
+    {
+        lo = fminf(A.x, B.x); hi = fmaxf(A.x, B.x);
+        return true;
+    }
+    return false;
+}
+
+// triangleOriginIntersection, src/Spline.h:709-737
+__device__ __forceinline__ bool triangleOriginIntersection(float2& coord, float2 P, float2 A, float2 B)
+{
+    float2 p = A - P, q = B - P;
+    float det = p.x * q.y - q.x * p.y;
+    if (fabsf(det) < 0x1p-80f) return false;
+    det = 1.0f / det;
+    float u = det * (q.y * -P.x + -q.x * -P.y);
+    if (u < 0.0f || u > 1.0f) return false;
+    float v = det * (-p.y * -P.x + p.x * -P.y);
+    if (v < 0.0f || u + v > 1.0f) return false;
+    coord = make_float2(u, v);
+    return true;
+}
+
+// Fat-line clip range of a sub-net (src/Spline_BezierClipping.cu:610-701):
+// distance patch against the line through the net's diagonals, column
+// extremes, convex-hull scan against the x axis, anti-sliver shrink.
+__device__ __forceinline__ void clip_range(const float2* p, int cutside, float& lower, float& upper)
+{
+    lower = 1.0f; upper = 0.0f;
+    float2 L = p[15] - p[0];
+    float2 D = p[12] - p[3];
+    L = cutside == 0 ? L + D : L - D;
+    {
+        float l = len2(L);
+        if (l != 0.0f) { float k = 1.0f / l; L = make_float2(L.x * k, L.y * k); }
+    }
+    const float2 N = make_float2(-L.y, L.x);
+    float ytop[4], ybot[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        float y0, y1, y2, y3;
+        if (cutside == 0)
+        { y0 = dot2(N, p[i]); y1 = dot2(N, p[4 + i]); y2 = dot2(N, p[8 + i]); y3 = dot2(N, p[12 + i]); }
+        else
+        { y0 = dot2(N, p[4 * i]); y1 = dot2(N, p[4 * i + 1]); y2 = dot2(N, p[4 * i + 2]); y3 = dot2(N, p[4 * i + 3]); }
+        ybot[i] = fminf(fminf(y0, y1), fminf(y2, y3));
+        ytop[i] = fmaxf(fmaxf(y0, y1), fmaxf(y2, y3));
+    }
+    const float o1 = 1.0f / 3.0f, o2 = 2.0f / 3.0f;
+    const float2 hull[7] = {make_float2(o2, ybot[2]), make_float2(1.0f, ybot[3]), make_float2(1.0f, ytop[3]),
+                            make_float2(o2, ytop[2]), make_float2(o1, ytop[1]), make_float2(0.0f, ytop[0]),
+                            make_float2(0.0f, ybot[0])};
+    float2 P1 = make_float2(0.0f, ybot[0]), P2 = make_float2(o1, ybot[1]);
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+    {
+        float2 P3 = hull[k];
+        float2 a = P2 - P1, b = P3 - P1;
+        if (a.x * b.y - a.y * b.x >= 0.0f)
+        {
+            float lo, hi;
+            if (xAxisIntersection(lo, hi, P1, P2)) { lower = fminf(lower, lo); upper = fmaxf(upper, hi); }
+            P1 = P2;
+        }
+        P2 = P3;
+    }
+    {
+        float lo, hi;
+        if (xAxisIntersection(lo, hi, P1, P2)) { lower = fminf(lower, lo); upper = fmaxf(upper, hi); }
+    }
+    lower = lower * 0x0FFp-8f;
+    upper = upper + (1.0f - upper) * 0x001p-8f;
+}
+
+// onHit of doBezierClipping (src/Spline_BezierClipping.cu:94-112): keep the
+// surface point closest to the origin and in front of it.
+struct HitSink
+{
+    const float4* P;
+    float3 o, d;
+    float dist;
+    float2 uv;
+    __device__ __forceinline__ bool operator()(float2 e)
+    {
+        float3 V = project(tensor_eval(P, basis(e.x), basis(e.y))) - o;
+        float t = len(V);
+        if (t < dist && dot(V, d) > 0.0f) { dist = t; uv = e; return true; }
+        return false;
+    }
+};
+
+// approximateIntersection, src/Spline.h:739-765
+__device__ __forceinline__ bool approximateIntersection(HitSink& sink, const float2* p, float2 pmin, float2 pmax)
+{
+    bool found = false;
+    float2 coord, psize = pmax - pmin;
+    if (triangleOriginIntersection(coord, p[0], p[3], p[12])) found |= sink(pmin + coord * psize);
+    if (triangleOriginIntersection(coord, p[15], p[12], p[3])) found |= sink(pmax - coord * psize);
+    return found;
+}
+
+// Project the 16 control points onto two planes containing the ray
+// (src/Spline_BezierClipping.cu:53-83).
+__device__ __forceinline__ void project_net(float2* net, const float4* __restrict__ P, float3 o, float3 d)
+{
+    const float3 a0 = versor(cross(d, d + f3(0.0f, 0.0f, 8.0f)));
+    const float3 a1 = versor(cross(d, a0));
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+    {
+        float3 Q = xyz(__ldg(P + i)) - o;
+        net[i] = make_float2(dot(a0, Q), dot(a1, Q));
+    }
+}
+
+// doBezierClipping2D_device (src/Spline_BezierClipping.cu:547-828) with the
+// half-precision (mid,len) stack replaced by a full-precision (min,max)
+// stack of the same depth.  Popped sub-nets are re-derived from the
+// original net (patchCopy, src/SplineMat.h:248-257), which is re-projected
+// from the patch so that it need not stay in registers.  Stack overflow and
+// the iteration cap end the search with an error bit instead of __trap().
+static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, LocalCounters& lc)
+{
+    float4 st[kClipStack];  // (min.x, min.y, max.x, max.y)
+    int sl = 0;
+    int cutsideStack = 0;
+    float2 emin = make_float2(0.0f, 0.0f), emax = make_float2(1.0f, 1.0f);
+    float2 buf[16];
+    project_net(buf, sink.P, sink.o, sink.d);
+    bool found = false;
+    for (int it = 0;; it++)
+    {
+        if (it >= kMaxClipIterations) { lc.errors |= kErrClipIterations; break; }
+        lc.iterations++;
+        const int cutside = cutsideStack & 1;
+        bool pop = true;
+        if (len2(buf[3] - buf[12]) < tol && len2(buf[15] - buf[0]) < tol)
+            found |= approximateIntersection(sink, buf, emin, emax);
+        else
+        {
+            float lower, upper;
+            clip_range(buf, cutside, lower, upper);
+            float delta = upper - lower;
+            if (delta > 0.8f)
+            {
+                float4 pushed;
+                if (cutside == 0)
+                {
+                    float hx = 0.5f * (emin.x + emax.x);
+                    pushed = make_float4(emin.x, emin.y, hx, emax.y);
+                    emin.x = hx;
+                    cutsideStack = (cutsideStack << 1) | 3;
+                    subpatchU(buf, 0.5f, 1.0f);
+                }
+                else
+                {
+                    float hy = 0.5f * (emin.y + emax.y);
+                    pushed = make_float4(emin.x, emin.y, emax.x, hy);
+                    emin.y = hy;
+                    cutsideStack = (cutsideStack << 1) & ~3;
+                    subpatchV(buf, 0.5f, 1.0f);
+                }
+                if (sl >= kClipStack) { lc.errors |= kErrClipStack; break; }
+                st[sl++] = pushed;
+                pop = false;
+            }
+            else if (delta > 0.0f)
+            {
+                if (cutside == 0)
+                {
+                    float sx = emax.x - emin.x;
+                    float u0 = emin.x + sx * lower, u1 = emax.x - sx * (1.0f - upper);
+                    subpatchU(buf, lower, upper);
+                    emin.x = u0; emax.x = u1;
+                }
+                else
+                {
+                    float sy = emax.y - emin.y;
+                    float v0 = emin.y + sy * lower, v1 = emax.y - sy * (1.0f - upper);
+                    subpatchV(buf, lower, upper);
+                    emin.y = v0; emax.y = v1;
+                }
+                cutsideStack ^= 1;
+                pop = false;
+            }
+        }
+        if (pop)
+        {
+            cutsideStack >>= 1;
+            if (--sl < 0) break;
+            float4 e = st[sl];
+            emin = make_float2(e.x, e.y); emax = make_float2(e.z, e.w);
+            project_net(buf, sink.P, sink.o, sink.d);
+            subpatchU(buf, emin.x, emax.x);
+            subpatchV(buf, emin.y, emax.y);
+        }
+    }
+    return found;
+}
+
+// Stackless 2-D subdivision (doSubdivision2D_device,
+// src/Spline_Subdivision.cu:16-109): bisect alternately along u and v, lower
+// half first, bit trails instead of a stack, re-derive the sub-net after each
+// backtrack, accept a leaf whose bounding box strictly contains the origin
+// once both diagonals are below tol (or after 31 halvings).  The sub-domain
+// follows the buffer: after k halvings su = 2^-ceil(k/2), sv = 2^-floor(k/2).
+static __device__ __noinline__ bool subdiv_patch(HitSink& sink, float tol, LocalCounters& lc)
+{
+    float2 buf[16];
+    project_net(buf, sink.P, sink.o, sink.d);
+    uint32_t trail = 0, tu = 0, tv = 0;
+    int k = 0;
+    bool reload = false, found = false;
+    for (int it = 0;; it++)
+    {
+        if (it >= 4 * kMaxClipIterations) { lc.errors |= kErrClipIterations; break; }
+        lc.iterations++;
+        const float su = ldexpf(1.0f, -((k + 1) >> 1)), sv = ldexpf(1.0f, -(k >> 1));
+        const float2 emin = make_float2(float(tu) * su, float(tv) * sv);
+        const float2 emax = make_float2(emin.x + su, emin.y + sv);
+        if (reload)
+        {
+            project_net(buf, sink.P, sink.o, sink.d);
+            subpatchU(buf, emin.x, emax.x);
+            subpatchV(buf, emin.y, emax.y);
+        }
+        float2 bmin = buf[0], bmax = buf[0];
+#pragma unroll
+        for (int i = 1; i < 16; i++)
+        {
+            bmin = make_float2(fminf(bmin.x, buf[i].x), fminf(bmin.y, buf[i].y));
+            bmax = make_float2(fmaxf(bmax.x, buf[i].x), fmaxf(bmax.y, buf[i].y));
+        }
+        if (bmin.x < 0.0f && bmin.y < 0.0f && bmax.x > 0.0f && bmax.y > 0.0f)
+        {
+            if ((len2(buf[3] - buf[12]) < tol && len2(buf[15] - buf[0]) < tol) || k >= 31)
+                found |= approximateIntersection(sink, buf, emin, emax);
+            else
+            {
+                reload = false;
+                if ((k & 1) == 0) { subpatchU(buf, 0.0f, 0.5f); tu <<= 1; }
+                else { subpatchV(buf, 0.0f, 0.5f); tv <<= 1; }
+                trail <<= 1;
+                ++k;
+                continue;
+            }
+        }
+        int ones = __clz(__brev(~trail));
+        if (ones >= k) break;
+        // levels k-1 .. k-ones are undone: even levels were u cuts
+        const int hi = k - 1, lo = k - ones;         // inclusive range of undone cut levels
+        const int evens = (hi / 2) - ((lo + 1) / 2) + 1;  // even levels in [lo, hi] were u cuts
+        tu >>= evens;
+        tv >>= (ones - evens);
+        k -= ones;
+        trail = (trail >> ones) | 1u;
+        if (((k - 1) & 1) == 0) tu |= 1u; else tv |= 1u;
+        reload = true;
+    }
+    return found;
+}
+
+// ----------------------------------------------------------- FP64 polish --
+__device__ __forceinline__ void basis_d(double t, double* w)
+{
+    double s = 1.0 - t;
+    w[0] = s * s * s; w[1] = 3.0 * t * s * s; w[2] = 3.0 * t * t * s; w[3] = t * t * t;
+}
+__device__ __forceinline__ void dbasis_d(double t, double* w)
+{
+    double s = 1.0 - t;
+    w[0] = -3.0 * s * s; w[1] = 3.0 * s * s - 6.0 * t * s; w[2] = 6.0 * t * s - 3.0 * t * t; w[3] = 3.0 * t * t;
+}
+
+// Newton polish of S(u,v) = o + t d in FP64 on the winning hit: at most 8
+// steps, stops when the update is below 1e-15; keeps the FP32 result if it
+// diverges or leaves the patch domain by more than 1e-6.
+static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P, double3 o, double3 d, double& t, double& u, double& v)
+{
+    double U = u, V = v, T = t;
+    for (int it = 0; it < 8; it++)
+    {
+        double wu[4], wv[4], du[4], dv[4];
+        basis_d(U, wu); basis_d(V, wv); dbasis_d(U, du); dbasis_d(V, dv);
+        double S[4] = {0, 0, 0, 0}, Su[4] = {0, 0, 0, 0}, Sv[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+            {
+                float4 q = __ldg(P + 4 * j + i);
+                double a = wu[i] * wv[j], b = du[i] * wv[j], c = wu[i] * dv[j];
+                S[0] += a * q.x; S[1] += a * q.y; S[2] += a * q.z; S[3] += a * q.w;
+                Su[0] += b * q.x; Su[1] += b * q.y; Su[2] += b * q.z; Su[3] += b * q.w;
+                Sv[0] += c * q.x; Sv[1] += c * q.y; Sv[2] += c * q.z; Sv[3] += c * q.w;
+            }
+        double iw = 1.0 / S[3];
+        double px = S[0] * iw, py = S[1] * iw, pz = S[2] * iw;
+        double ux = (Su[0] - Su[3] * px) * iw, uy = (Su[1] - Su[3] * py) * iw, uz = (Su[2] - Su[3] * pz) * iw;
+        double vx = (Sv[0] - Sv[3] * px) * iw, vy = (Sv[1] - Sv[3] * py) * iw, vz = (Sv[2] - Sv[3] * pz) * iw;
+        double fx = px - (o.x + T * d.x), fy = py - (o.y + T * d.y), fz = pz - (o.z + T * d.z);
+        // columns Su, Sv, -d; solve by Cramer's rule
+        double cx = -d.x, cy = -d.y, cz = -d.z;
+        double svxc_x = vy * cz - vz * cy, svxc_y = vz * cx - vx * cz, svxc_z = vx * cy - vy * cx;
+        double det = ux * svxc_x + uy * svxc_y + uz * svxc_z;
+        if (!(fabs(det) > 1e-300)) return false;
+        double mx = -fx, my = -fy, mz = -fz;
+        double dU = (mx * svxc_x + my * svxc_y + mz * svxc_z) / det;
+        double mxc_x = my * cz - mz * cy, mxc_y = mz * cx - mx * cz, mxc_z = mx * cy - my * cx;
+        double dV = (ux * mxc_x + uy * mxc_y + uz * mxc_z) / det;
+        double svxm_x = vy * mz - vz * my, svxm_y = vz * mx - vx * mz, svxm_z = vx * my - vy * mx;
+        double dT = (ux * svxm_x + uy * svxm_y + uz * svxm_z) / det;
+        U += dU; V += dV; T += dT;
+        if (!isfinite(U + V + T)) return false;
+        if (fabs(dU) + fabs(dV) < 1e-15 && fabs(dT) < 1e-15 * fabs(T)) break;
+    }
+    if (U < -1e-6 || U > 1.0 + 1e-6 || V < -1e-6 || V > 1.0 + 1e-6 || T <= 0.0) return false;
+    t = T; u = U; v = V;
+    return true;
+}
+
+// ----------------------------------------------------------- traversal --
+__device__ __forceinline__ uint32_t hash_slot(const DevScene& S, const DevBVH& b, uint32_t key)
+{
+    uint32_t disp = __ldg(S.disps + b.dispBase + (key & b.mask));
+    return (b.A * key + b.B + disp) % b.N;
+}
+
+// _node_intersect, src/rt/BVH.h:147-176
+__device__ __forceinline__ bool slab(float& tMin, float3 lo, float3 hi, float3 o, float3 inv)
+{
+    float tm = -INFINITY, tM = INFINITY;
+    {
+        float t0 = (lo.x - o.x) * inv.x, t1 = (hi.x - o.x) * inv.x;
+        bool s = signbit(inv.x);
+        float a = s ? t1 : t0, b = s ? t0 : t1;
+        if (a > tm) tm = a;
+        if (b < tM) tM = b;
+    }
+    {
+        float t0 = (lo.y - o.y) * inv.y, t1 = (hi.y - o.y) * inv.y;
+        bool s = signbit(inv.y);
+        float a = s ? t1 : t0, b = s ? t0 : t1;
+        if (a > tm) tm = a;
+        if (b < tM) tM = b;
+    }
+    {
+        float t0 = (lo.z - o.z) * inv.z, t1 = (hi.z - o.z) * inv.z;
+        bool s = signbit(inv.z);
+        float a = s ? t1 : t0, b = s ? t0 : t1;
+        if (a > tm) tm = a;
+        if (b < tM) tM = b;
+    }
+    tMin = tm;
+    return tm < tM && tM > 0.0001f;
+}
+
+// BVH::hashIntersect (src/rt/BVH.h:178-350): stackless descent that visits
+// the nearer child first and records a postponed sibling as a 1 bit; going
+// up shifts the bits out, flips to the sibling key and finds its node through
+// the perfect hash.  kAny returns at the first accepted leaf element.
+// `limit` is hit.t (closest) or ray.max (any); leaf(p) returns true on a hit
+// and may lower `limit`.
+template<bool kAny, class Leaf>
+__device__ __forceinline__ bool hash_traverse(const DevScene& S, const DevBVH& b, float3 o, float3 inv, float& limit,
+                                              Leaf&& leaf, LocalCounters& lc)
+{
+    const float4* __restrict__ nodes = S.nodes + 4ull * b.nodeBase;
+    const uint32_t* __restrict__ indices = S.indices + b.indexBase;
+    const uint32_t* __restrict__ table = S.tables + b.tableBase;
+    uint32_t node = 0, key = 1, postponed = 0;
+    bool result = false;
+    for (int step = 0;; step++)
+    {
+        if (step >= kMaxTraversalSteps) { lc.errors |= kErrTraversal; break; }
+        const float4* q = nodes + 4ull * node;
+        float4 q3 = __ldg(q + 3);
+        uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
+        if (left != EMPTY)
+        {
+            lc.nodes++;
+            float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+            float L0, R0;
+            bool iL = slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), o, inv) && L0 < limit;
+            bool iR = slab(R0, f3(q1.z, q1.w, q2.x), f3(q2.y, q2.z, q2.w), o, inv) && R0 < limit;
+            if (iL || iR) postponed <<= 1;
+            if (iL)
+            {
+                if (iR)
+                {
+                    postponed |= 1u;
+                    if (L0 < R0) { key = key << 1; node = left; }
+                    else { key = (key << 1) ^ 1u; node = right; }
+                }
+                else { key = key << 1; node = left; }
+                continue;
+            }
+            else if (iR) { key = (key << 1) ^ 1u; node = right; continue; }
+        }
+        else
+        {
+            for (uint32_t i = right;; i++)
+            {
+                uint32_t p = __ldg(indices + i);
+                if (p == EMPTY) break;
+                bool h = leaf(p);
+                if (kAny && h) return true;
+                result |= h;
+            }
+        }
+        if (!postponed) break;
+        int levels = __ffs(postponed) - 1;
+        postponed >>= levels;
+        key = (key >> levels) ^ 1u;
+        postponed ^= 1u;
+        lc.hashLookups++;
+        node = __ldg(table + hash_slot(S, b, key));
+    }
+    return kAny ? false : result;
+}
+
+struct Query { int method; int precision; float tol; };
+
+struct HitRecord { float t, u, v; int32_t patch, object; };
+
+// World -> object space ray (Context::intersect, src/rt/RayTracer.cu:305-314).
+__device__ __forceinline__ void to_local(const DevObject& ob, float3 o, float3 d, float tmax, float3& lo, float3& ld,
+                                         float& lmax, float& scale_inv)
+{
+    float4 o4 = m4_point(ob.w2l, o);
+    lo = project(o4);
+    ld = m3_vec(ob.w2l, d);
+    float s = len(ld);
+    lmax = tmax * s;
+    s = 1.0f / s;
+    ld = ld * s;
+    scale_inv = s;
+}
+
+__device__ __forceinline__ bool search_patch(HitSink& sink, const Query& q, LocalCounters& lc)
+{
+    lc.candidates++;
+    return q.method == 0 ? clip_patch(sink, q.tol, lc) : subdiv_patch(sink, q.tol, lc);
+}
+
+// Closest hit over the object-level BVH and each object's patch BVH
+// (Context::intersect, src/rt/RayTracer.cu:295-349; rt::intersect,
+// src/rt/Primitive.cu:222-248).  hit.t must hold ray.max on entry.
+__device__ __forceinline__ int scene_closest(const DevScene& S, float3 o, float3 d, float tmax, const Query& q,
+                                             HitRecord& hit, LocalCounters& lc)
+{
+    int nearest = -1;
+    float limit = tmax;
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    auto objfn = [&](uint32_t oi) -> bool {
+        const DevObject& ob = S.objects[oi];
+        float3 lo, ld; float lmax, sinv;
+        to_local(ob, o, d, tmax, lo, ld, lmax, sinv);
+        const float4* patches = S.patches + 16ull * __ldg(S.patchBase + ob.surface);
+        float lt = lmax, lu = 0.0f, lv = 0.0f;
+        uint32_t lp = 0;
+        const float3 linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
+        auto leaf = [&](uint32_t p) -> bool {
+            HitSink sink {patches + 16ull * p, lo, ld, lt, make_float2(lu, lv)};
+            if (search_patch(sink, q, lc)) { lt = sink.dist; lu = sink.uv.x; lv = sink.uv.y; lp = p; return true; }
+            return false;
+        };
+        bool b = hash_traverse<false>(S, S.bvhs[ob.surface], lo, linv, lt, leaf, lc);
+        if (b)
+        {
+            float t = lt * sinv;
+            if (t < limit)
+            {
+                hit.t = t; hit.u = lu; hit.v = lv; hit.patch = int32_t(lp); hit.object = int32_t(oi);
+                limit = t; nearest = int(oi);
+                return true;
+            }
+        }
+        return false;
+    };
+    hash_traverse<false>(S, S.bvhs[S.topBVH], o, inv, limit, objfn, lc);
+    if (nearest >= 0 && q.precision == 1)
+    {
+        // FP64 Newton polish of the winning hit in object space
+        const DevObject& ob = S.objects[nearest];
+        const float4* P = S.patches + 16ull * (__ldg(S.patchBase + ob.surface) + uint32_t(hit.patch));
+        const float* m = ob.w2l;
+        double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+        double lw = ox * m[3] + oy * m[7] + oz * m[11] + m[15];
+        double3 lo = make_double3((ox * m[0] + oy * m[4] + oz * m[8] + m[12]) / lw,
+                                  (ox * m[1] + oy * m[5] + oz * m[9] + m[13]) / lw,
+                                  (ox * m[2] + oy * m[6] + oz * m[10] + m[14]) / lw);
+        double3 ld = make_double3(dx * m[0] + dy * m[4] + dz * m[8], dx * m[1] + dy * m[5] + dz * m[9],
+                                  dx * m[2] + dy * m[6] + dz * m[10]);
+        double sc = sqrt(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z);
+        ld = make_double3(ld.x / sc, ld.y / sc, ld.z / sc);
+        double t = double(hit.t) * sc, u = hit.u, v = hit.v;
+        if (newton_polish64(P, lo, ld, t, u, v)) { hit.t = float(t / sc); hit.u = float(u); hit.v = float(v); }
+    }
+    return nearest;
+}
+
+// Any hit (Context::intersect(const Ray&), src/rt/RayTracer.cu:351-383;
+// rt::intersect(const BezierSurface&, const Ray&), src/rt/Primitive.cu:250-268).
+__device__ __forceinline__ bool scene_any(const DevScene& S, float3 o, float3 d, float tmax, const Query& q,
+                                          LocalCounters& lc)
+{
+    float limit = tmax;
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    auto objfn = [&](uint32_t oi) -> bool {
+        const DevObject& ob = S.objects[oi];
+        float3 lo, ld; float lmax, sinv;
+        to_local(ob, o, d, tmax, lo, ld, lmax, sinv);
+        const float4* patches = S.patches + 16ull * __ldg(S.patchBase + ob.surface);
+        const float3 linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
+        float llimit = lmax;
+        auto leaf = [&](uint32_t p) -> bool {
+            HitSink sink {patches + 16ull * p, lo, ld, lmax, make_float2(0.0f, 0.0f)};
+            return search_patch(sink, q, lc);
+        };
+        return hash_traverse<true>(S, S.bvhs[ob.surface], lo, linv, llimit, leaf, lc);
+    };
+    return hash_traverse<true>(S, S.bvhs[S.topBVH], o, inv, limit, objfn, lc);
+}
+
+// --------------------------------------------------------------- shading --
+// src/rt/PBR.h:21-176, src/rt/PBR.cu:198-242
+__device__ __forceinline__ bool lightVector(float& dist, float3& L, float3 P, const DevLight& l)
+{
+    if (l.angle < 0.01f) { L = -f3(l.direction[0], l.direction[1], l.direction[2]); dist = INFINITY; return true; }
+    L = f3(l.position[0], l.position[1], l.position[2]) - P;
+    dist = len(L);
+    if (dist < 1e-14f || (l.range > 0.0f && dist > l.range)) return false;
+    L = L * (1.0f / dist);
+    if (l.angle > 1.57f) return true;
+    float DL = dot(f3(l.direction[0], l.direction[1], l.direction[2]), L);
+    return DL < 0.0f && l.angle > 2.0f * acosf(DL);
+}
+__device__ __forceinline__ float3 lightColor(float dist, const DevLight& l)
+{
+    float3 c = f3(l.color[0], l.color[1], l.color[2]);
+    if (l.angle < 0.01f) return c;
+    float f;
+    if (l.range == 0.0f) { f = 1.0f / dist; f *= f; }
+    else { f = dist / l.range; f = 1.0f + f * (f - 2.0f); }
+    return c * f;
+}
+__device__ __forceinline__ float3 schlick(float3 f0, float dotLH)
+{
+    float b = 1.0f - dotLH, b2 = b * b;
+    return f0 + (f3(1.0f, 1.0f, 1.0f) - f0) * (b2 * b2 * b);
+}
+__device__ __forceinline__ float G1(float x, float k) { return x / (x * (1.0f - k) + k); }
+__device__ __forceinline__ float Gsmith(float nl, float nv, float r)
+{
+    float r1 = r + 1.0f, k = r1 * r1 * 0.125f;
+    return G1(nl, k) * G1(nv, k);
+}
+__device__ __forceinline__ float Dggx(float nh, float r)
+{
+    r = fmaxf(r, 1e-3f);
+    float a = r * r, a2 = a * a, dd = nh * nh * (a2 - 1.0f) + 1.0f;
+    return a2 / (kPi * dd * dd);
+}
+__device__ __forceinline__ float3 BRDF_specular(float hl, float hn, float nv, float nl, float r, float3 f0)
+{
+    return schlick(f0, hl) * (Gsmith(nl, nv, r) * Dggx(hn, r) / (4.0f * nl * nv));
+}
+
+__device__ __forceinline__ const DevMaterial& hit_material(const DevScene& S, const DevObject& ob, uint32_t patch)
+{
+    if (ob.patchMaterialBase >= 0) return S.materials[__ldg(S.patchMaterial + ob.patchMaterialBase + patch)];
+    return S.materials[ob.material];
+}
+
+// sRGB encode (IEC 61966-2-1) and RGBA8 packing.
+__device__ __forceinline__ uint32_t srgb8(float c)
+{
+    float x = c <= 0.0031308f ? 12.92f * c : 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+    int v = __float2int_rn(x * 255.0f);
+    return uint32_t(min(255, max(0, v)));
+}
+__device__ __forceinline__ uint32_t pack_srgb(float3 c)
+{
+    return srgb8(c.x) | (srgb8(c.y) << 8) | (srgb8(c.z) << 16) | 0xFF000000u;
+}
+
+// ---------------------------------------------------- warp-level helpers --
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated atomic increment: every active lane with `want` gets a slot.
+__device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool want)
+{
+    unsigned mask = __activemask();
+    unsigned ballot = __ballot_sync(mask, want);
+    if (!ballot) return EMPTY;
+    int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+    base = __shfl_sync(mask, base, leader);
+    return want ? base + __popc(ballot & ((1u << lane_id()) - 1u)) : EMPTY;
+}
+
+__device__ __forceinline__ void flush_counters(Counters* c, const LocalCounters& lc, uint32_t rays)
+{
+    if (!c) return;
+    unsigned mask = __activemask();
+    unsigned long long v[5] = {lc.nodes, lc.hashLookups, lc.candidates, lc.iterations, rays};
+    uint32_t err = lc.errors;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+    {
+#pragma unroll
+        for (int k = 0; k < 5; k++) v[k] += __shfl_down_sync(mask, v[k], off);
+        err |= __shfl_down_sync(mask, err, off);
+    }
+    if (lane_id() == (unsigned)(__ffs(mask) - 1))
+    {
+        atomicAdd(&c->nodes, v[0]); atomicAdd(&c->hashLookups, v[1]); atomicAdd(&c->candidates, v[2]);
+        atomicAdd(&c->iterations, v[3]); atomicAdd(&c->rays, v[4]);
+        if (err) atomicOr(&c->errors, (unsigned long long)err);
+    }
+}
+
+}  // namespace cgs

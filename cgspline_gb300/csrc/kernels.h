@@ -1,0 +1,93 @@
+// kernels.h -- host-side launchers of the CUDA kernels (one header for all
+// translation units of libcgspline_gb300.so).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device.cuh"
+
+namespace cgs {
+
+struct RaysSoA { const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax; };
+struct HitsSoA { float *t, *u, *v; int32_t *patch, *object; };
+
+// ---------------------------------------------------------- ray queries --
+// Persistent kernels: every warp takes 32 rays at a time from *next until n.
+cudaError_t launch_closest(const DevScene& S, RaysSoA rays, uint32_t n, Query q, HitsSoA hits, uint32_t* next,
+                           Counters* counters, cudaStream_t stream);
+cudaError_t launch_any(const DevScene& S, RaysSoA rays, uint32_t n, Query q, int32_t* occluded, uint32_t* next,
+                       Counters* counters, cudaStream_t stream);
+cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, RaysSoA rays, const uint32_t* patch_ids,
+                               uint32_t n, Query q, HitsSoA hits, Counters* counters, cudaStream_t stream);
+
+// --------------------------------------------------------------- render --
+struct CameraSetup
+{
+    float c2w[16];   // camera to world, column-major
+    float pos[3];
+    float tl[2];     // top-left corner of the image plane at z = -1
+    float half_dx, half_dy;
+};
+
+struct RenderParams
+{
+    CameraSetup cam;
+    uint32_t width, height, stride;
+    int depth;
+    float eps;
+    Query q;
+};
+
+// Work buffers of the wavefront schedule (device memory, sized for w*h rays).
+struct WavefrontBuffers
+{
+    // ray queues (two, ping-pong): origin, direction, attenuation, pixel
+    float* ray[2];       // 9 floats per ray, SoA: ox oy oz dx dy dz ax ay az
+    uint32_t* pixel[2];
+    uint32_t* count;     // [0..1] queue sizes, [2] shadow count, [3..7] work counters
+    HitRecord* hit;      // per ray of the current queue
+    float* shadow;       // 7 floats per shadow ray SoA: ox oy oz dx dy dz max
+    uint32_t* shadowSlot;  // (ray index * nlights + light) of each shadow ray
+    float* contrib;      // 3 floats per (ray, light) slot
+    int32_t* visible;    // per (ray, light) slot: 1 = lit, 0 = not
+    float* base;         // 3 floats per ray: ambient term, then the resolved colour factor
+    float* accum;        // 3 floats per pixel
+    uint32_t capacity;   // rays
+    uint32_t lightCapacity;
+};
+
+cudaError_t launch_render_plain(const DevScene& S, const RenderParams& p, uint32_t* framebuffer, float* linear,
+                                Counters* counters, cudaStream_t stream);
+cudaError_t launch_render_wavefront(const DevScene& S, const RenderParams& p, const WavefrontBuffers& wb,
+                                    uint32_t* framebuffer, float* linear, Counters* counters, cudaStream_t stream,
+                                    int* launches);
+
+// ---------------------------------------------------------- perfect hash --
+struct HashScratch
+{
+    uint32_t* bsize;      // [displSize]
+    uint32_t* bkeys;      // [4 * displSize]
+    uint32_t* rank;       // [displSize]
+    uint32_t* dcur;       // [displSize]
+    uint32_t* state;      // [displSize]: bit0 active, bit1 feasible
+    uint32_t* slots;      // [4 * displSize]
+    uint32_t* occ;        // [ceil(Nmax/32)]
+    unsigned long long* owner;  // [Nmax]
+    uint32_t* blockCounts;      // [2 * rankBlocks] packed class counts
+    uint32_t* misc;       // [16]: 0 error bits, 1..4 class counts, 5..8 class remaining, 9 failures
+};
+
+// Sizes of the scratch for n keys (in 4-byte words, owner in 8-byte words).
+void hash_scratch_words(uint32_t n, size_t& words32, size_t& words64);
+void hash_scratch_carve(HashScratch& s, uint32_t n, uint32_t* base32, unsigned long long* base64);
+
+// Deterministic perfect hash of keys[0..n).  A[], B[] are the 16 trials'
+// coefficients, drawn on the host.  Writes disp[displSize] and
+// table[N] (table[h(key_i)] = i); returns the trial used (0..15) in params,
+// or an error code.  Synchronises the stream once per trial.
+int hash_build_device(const uint32_t* keys, uint32_t n, const uint32_t A[16], const uint32_t B[16],
+                      uint32_t* disp, uint32_t* table, uint32_t tableCapacity, HashScratch& scratch,
+                      uint32_t params[5], cudaStream_t stream, int* launches);
+
+}  // namespace cgs

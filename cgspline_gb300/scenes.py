@@ -1,0 +1,363 @@
+"""Seeded synthetic scenes and ray sets for the ray--bicubic-patch path.
+
+Everything here uses only IEEE-exact elementwise float64 operations (+, -, *,
+/, sqrt) on numpy arrays, a splitmix64 generator and polynomial sine/cosine,
+so a given seed yields bit-identical scenes on x86-64 and aarch64 hosts and
+with any numpy version.  Normal deviates use the Irwin--Hall sum of twelve
+uniforms (mean 0, variance 1, bounded at +-6).
+
+The scene layout is the reference's: control points are ``float4`` (x, y, z,
+w) and each patch is 16 ``uint32`` indices into them, point (i, j) of a patch
+(i along u, j along v) at position 4*j + i
+(src/Spline.h:81-82, src/MainWindow.cpp:464-483).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import List, Optional
+
+import numpy as np
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+class SplitMix64:
+    """splitmix64 stream (Steele, Lea, Flood 2014), vectorised over numpy."""
+
+    def __init__(self, seed: int):
+        self.state = np.uint64(seed & 0xFFFFFFFFFFFFFFFF)
+
+    def u64(self, n: int) -> np.ndarray:
+        with np.errstate(over="ignore"):
+            k = np.arange(1, n + 1, dtype=np.uint64)
+            z = self.state + k * np.uint64(0x9E3779B97F4A7C15)
+            self.state = self.state + np.uint64(n) * np.uint64(0x9E3779B97F4A7C15)
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            return z ^ (z >> np.uint64(31))
+
+    def uniform(self, n: int, lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
+        x = (self.u64(n) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+        return lo + (hi - lo) * x
+
+    def normal(self, n: int) -> np.ndarray:
+        u = self.uniform(12 * n).reshape(n, 12)
+        s = u[:, 0]
+        for k in range(1, 12):
+            s = s + u[:, k]
+        return s - 6.0
+
+    def integers(self, n: int, hi: int) -> np.ndarray:
+        return (self.uniform(n) * hi).astype(np.int64).clip(0, hi - 1)
+
+
+_PIO2_HI = 1.5707963267341256
+_PIO2_LO = 6.077100506506192e-11
+
+
+def _sincos(x: np.ndarray):
+    """sin and cos by Cody--Waite reduction to [-pi/4, pi/4] and Taylor series."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.floor(x * (1.0 / 1.5707963267948966) + 0.5)
+    r = (x - k * _PIO2_HI) - k * _PIO2_LO
+    r2 = r * r
+    # Taylor series to degree 19 / 18 (error < 1e-18 on |r| <= pi/4)
+    s = np.zeros_like(r)
+    c = np.zeros_like(r)
+    for n in range(19, 0, -2):
+        s = s * r2 + ((-1) ** ((n - 1) // 2)) / math.factorial(n)
+    s = s * r
+    for n in range(18, -1, -2):
+        c = c * r2 + ((-1) ** (n // 2)) / math.factorial(n)
+    q = np.mod(k, 4).astype(np.int64)
+    sin = np.where(q == 0, s, np.where(q == 1, c, np.where(q == 2, -s, -c)))
+    cos = np.where(q == 0, c, np.where(q == 1, -s, np.where(q == 2, -c, s)))
+    return sin, cos
+
+
+@dataclasses.dataclass
+class Material:
+    diffuse: tuple = (0.8, 0.8, 0.8)
+    specular: tuple = (0.04, 0.04, 0.04)
+    metalness: float = 0.0
+    roughness: float = 0.5
+
+    def packed(self) -> np.ndarray:
+        return np.array([*self.diffuse, *self.specular, self.metalness, self.roughness], dtype=np.float32)
+
+
+@dataclasses.dataclass
+class Light:
+    """Point (angle > 1.57), spot, or directional (angle < 0.01) light (src/rt/Scene.h:47-77)."""
+    color: tuple = (1.0, 1.0, 1.0)
+    strength: float = 1.0
+    position: tuple = (0.0, 0.0, 0.0)
+    range: float = 0.0
+    direction: tuple = (0.0, 0.0, -1.0)
+    angle: float = math.pi
+
+    def packed(self) -> np.ndarray:
+        return np.array([*self.color, self.strength, *self.position, self.range, *self.direction, self.angle],
+                        dtype=np.float32)
+
+
+@dataclasses.dataclass
+class Surface:
+    points: np.ndarray   # (V, 4) float32
+    indices: np.ndarray  # (16 P,) uint32
+
+    @property
+    def patch_count(self) -> int:
+        return self.indices.size // 16
+
+    def patches(self) -> np.ndarray:
+        """De-indexed control nets, (P, 16, 4) float32."""
+        return self.points[self.indices.reshape(-1, 16)]
+
+
+@dataclasses.dataclass
+class Object:
+    surface: int
+    local2world: np.ndarray  # (16,) float32 column-major
+    world2local: np.ndarray  # (16,) float32 column-major
+    material: Material = dataclasses.field(default_factory=Material)
+    patch_material: Optional[np.ndarray] = None  # (P,) uint32 into materials
+    materials: Optional[List[Material]] = None
+
+
+@dataclasses.dataclass
+class Camera:
+    """Pinhole camera: rotation quaternion (x, y, z, w), position, scale and
+    vertical field of view in radians (src/rt/Scene.h:16-45)."""
+    rotation: tuple = (0.0, 0.0, 0.0, 1.0)
+    position: tuple = (0.0, 0.0, 0.0)
+    scale: tuple = (1.0, 1.0, 1.0)
+    fovy: float = math.radians(45.0)
+
+    def packed(self) -> np.ndarray:
+        return np.array([*self.rotation, *self.position, *self.scale, self.fovy], dtype=np.float32)
+
+
+@dataclasses.dataclass
+class Scene:
+    surfaces: List[Surface]
+    objects: List[Object]
+    lights: List[Light]
+    background: tuple = (0.1, 0.1, 0.1)
+    ambient: tuple = (0.1, 0.1, 0.1)
+    name: str = "scene"
+
+    @property
+    def patch_count(self) -> int:
+        return sum(self.surfaces[o.surface].patch_count for o in self.objects)
+
+
+IDENTITY16 = np.eye(4, dtype=np.float32).reshape(16)
+
+
+def look_at(eye, target, up=(0.0, 0.0, 1.0)):
+    """Quaternion (x, y, z, w) that turns the camera's -z axis towards target
+    with +y towards up."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f = f / np.sqrt(f @ f)
+    r = np.cross(f, np.asarray(up, np.float64))
+    r = r / np.sqrt(r @ r)
+    u = np.cross(r, f)
+    m = np.stack([r, u, -f], axis=1)  # columns
+    t = m[0, 0] + m[1, 1] + m[2, 2]
+    if t > 0:
+        s = np.sqrt(t + 1.0) * 2
+        w, x, y, z = 0.25 * s, (m[2, 1] - m[1, 2]) / s, (m[0, 2] - m[2, 0]) / s, (m[1, 0] - m[0, 1]) / s
+    elif m[0, 0] > m[1, 1] and m[0, 0] > m[2, 2]:
+        s = np.sqrt(1.0 + m[0, 0] - m[1, 1] - m[2, 2]) * 2
+        w, x, y, z = (m[2, 1] - m[1, 2]) / s, 0.25 * s, (m[0, 1] + m[1, 0]) / s, (m[0, 2] + m[2, 0]) / s
+    elif m[1, 1] > m[2, 2]:
+        s = np.sqrt(1.0 + m[1, 1] - m[0, 0] - m[2, 2]) * 2
+        w, x, y, z = (m[0, 2] - m[2, 0]) / s, (m[0, 1] + m[1, 0]) / s, 0.25 * s, (m[1, 2] + m[2, 1]) / s
+    else:
+        s = np.sqrt(1.0 + m[2, 2] - m[0, 0] - m[1, 1]) * 2
+        w, x, y, z = (m[1, 0] - m[0, 1]) / s, (m[0, 2] + m[2, 0]) / s, (m[1, 2] + m[2, 1]) / s, 0.25 * s
+    return tuple(float(np.float32(v)) for v in (x, y, z, w))
+
+
+# ----------------------------------------------------------------- C1 ----
+def heightfield(seed: int = 1, sigma: float = 0.25, n: int = 4) -> Surface:
+    """n x n bicubic patches tiling [0,n]^2 over a shared (3n+1)^2 control grid.
+    Control points on patch boundaries have z = 0 (shared edges stay C0);
+    the 4 interior points of every patch get z ~ sigma * N(0,1)."""
+    g = 3 * n + 1
+    rng = SplitMix64(seed)
+    i = np.arange(g)
+    X, Y = np.meshgrid(i / 3.0, i / 3.0, indexing="xy")  # [row j][col i]
+    interior = (np.arange(g)[None, :] % 3 != 0) & (np.arange(g)[:, None] % 3 != 0)
+    Z = np.zeros((g, g))
+    Z[interior] = sigma * rng.normal(int(interior.sum()))
+    pts = np.stack([X, Y, Z, np.ones_like(X)], axis=-1).reshape(-1, 4).astype(np.float32)
+    idx = []
+    for pj in range(n):
+        for pi in range(n):
+            for j in range(4):
+                for ii in range(4):
+                    idx.append((3 * pj + j) * g + (3 * pi + ii))
+    return Surface(pts, np.asarray(idx, dtype=np.uint32))
+
+
+def scene_c1(seed: int = 1) -> Scene:
+    s = heightfield(seed)
+    ob = Object(0, IDENTITY16.copy(), IDENTITY16.copy(), Material((0.8, 0.8, 0.8), (0.04, 0.04, 0.04), 0.0, 1.0))
+    sun = Light((1.0, 1.0, 1.0), 1.0, (0.0, 0.0, 0.0), 0.0, tuple(np.float32([0.3, 0.2, -0.93])), 0.0)
+    return Scene([s], [ob], [sun], name="heightfield4x4")
+
+
+def camera_c1() -> Camera:
+    return Camera((0.0, 0.0, 0.0, 1.0), (2.0, 2.0, 6.0), (1, 1, 1), float(np.float32(math.radians(40.0))))
+
+
+# ----------------------------------------------------------------- C2 ----
+def torus_surface(R: float = 4.0, r: float = 1.0, nu: int = 128, nv: int = 128, sigma: float = 0.05,
+                  seed: int = 2) -> Surface:
+    """Torus about the z axis as an nu x nv periodic grid of bicubic Bezier
+    patches over a (3 nu) x (3 nv) periodic control grid.  Corners and
+    tangents are sampled from the exact torus (Hermite -> Bezier, twist
+    vectors from the mixed derivative); then the four interior control points
+    of every patch move along the tube's radial direction by sigma * N(0,1)."""
+    gu, gv = 3 * nu, 3 * nv
+    ht, hp = 2 * math.pi / nu, 2 * math.pi / nv
+    a = np.arange(nu + 1) * ht
+    b = np.arange(nv + 1) * hp
+    st, ct = _sincos(a)
+    sp, cp = _sincos(b)
+    ST, CT = st[:, None], ct[:, None]
+    SP, CP = sp[None, :], cp[None, :]
+    shape = (nu + 1, nv + 1)
+    rad = np.broadcast_to(R + r * CP, shape)
+    ST, CT = np.broadcast_to(ST, shape), np.broadcast_to(CT, shape)
+    SP, CP = np.broadcast_to(SP, shape), np.broadcast_to(CP, shape)
+    S = np.stack([rad * CT, rad * ST, r * SP], -1)
+    St = np.stack([-rad * ST, rad * CT, np.zeros(shape)], -1)
+    Sp = np.stack([-r * SP * CT, -r * SP * ST, r * CP], -1)
+    Stp = np.stack([r * SP * ST, -r * SP * CT, np.zeros(shape)], -1)
+    k1, k2, k12 = ht / 3.0, hp / 3.0, ht * hp / 9.0
+    grid = np.zeros((gu, gv, 3))
+    for iu in range(3):
+        for jv in range(3):
+            # control point (3a+iu, 3b+jv) hangs off corner (a+cu, b+cv)
+            cu, su = (0, 1.0) if iu < 2 else (1, -1.0)
+            cv, sv = (0, 1.0) if jv < 2 else (1, -1.0)
+            A = slice(cu, cu + nu)
+            B = slice(cv, cv + nv)
+            P = S[A, B].copy()
+            if iu != 0:
+                P = P + (su * k1) * St[A, B]
+            if jv != 0:
+                P = P + (sv * k2) * Sp[A, B]
+            if iu != 0 and jv != 0:
+                P = P + (su * sv * k12) * Stp[A, B]
+            grid[iu::3, jv::3] = P
+    # radial displacement of interior points
+    rng = SplitMix64(seed)
+    th = np.arange(gu) * (2 * math.pi / gu)
+    ph = np.arange(gv) * (2 * math.pi / gv)
+    sth, cth = _sincos(th)
+    sph, cph = _sincos(ph)
+    nrm = np.stack([cph[None, :] * cth[:, None], cph[None, :] * sth[:, None],
+                    np.broadcast_to(sph[None, :], (gu, gv))], -1)
+    inter = ((np.arange(gu) % 3 != 0)[:, None]) & ((np.arange(gv) % 3 != 0)[None, :])
+    nint = int(inter.sum())
+    disp = np.zeros((gu, gv))
+    disp[inter] = sigma * rng.normal(nint)
+    grid = grid + disp[..., None] * nrm
+    pts = np.concatenate([grid.reshape(-1, 3), np.ones((gu * gv, 1))], axis=1).astype(np.float32)
+    # grid index (iu, jv) -> iu * gv + jv ; patch p = b * nu + a ; point(i,j) -> [4j+i]
+    A, B = np.meshgrid(np.arange(nu), np.arange(nv), indexing="xy")  # [b][a]
+    A = A.reshape(-1)
+    B = B.reshape(-1)
+    idx = np.zeros((nu * nv, 16), dtype=np.int64)
+    for j in range(4):
+        for i in range(4):
+            idx[:, 4 * j + i] = ((3 * A + i) % gu) * gv + ((3 * B + j) % gv)
+    return Surface(pts, idx.reshape(-1).astype(np.uint32))
+
+
+def scene_c2(seed: int = 2, nu: int = 128, nv: int = 128) -> Scene:
+    s = torus_surface(nu=nu, nv=nv, seed=seed)
+    rng = SplitMix64(seed + 1000)
+    P = s.patch_count
+    rough = rng.uniform(P, 0.1, 0.9)
+    metal = (rng.uniform(P) < 0.5).astype(np.float64)
+    mats = [Material((0.75, 0.55, 0.35), (0.95, 0.93, 0.88), float(np.float32(m)), float(np.float32(r)))
+            for m, r in zip(metal, rough)]
+    ob = Object(0, IDENTITY16.copy(), IDENTITY16.copy(), mats[0], np.arange(P, dtype=np.uint32), mats)
+    lights = [Light((60.0, 60.0, 60.0), 1.0, (6.0, -6.0, 8.0), 0.0, (0.0, 0.0, -1.0), math.pi),
+              Light((30.0, 26.0, 22.0), 1.0, (-8.0, 3.0, 5.0), 0.0, (0.0, 0.0, -1.0), math.pi)]
+    return Scene([s], [ob], lights, name=f"torus{nu}x{nv}")
+
+
+def camera_c2() -> Camera:
+    eye = (2.0, -5.0, 8.0)
+    return Camera(look_at(eye, (0.0, 0.0, -0.5)), eye, (1, 1, 1), float(np.float32(math.radians(55.0))))
+
+
+# ---------------------------------------------------------- evaluation ---
+def bernstein(t: np.ndarray):
+    t = np.asarray(t, np.float64)
+    s = 1.0 - t
+    return np.stack([s * s * s, 3 * t * s * s, 3 * t * t * s, t * t * t], -1)
+
+
+def dbernstein(t: np.ndarray):
+    t = np.asarray(t, np.float64)
+    s = 1.0 - t
+    return np.stack([-3 * s * s, 3 * s * s - 6 * t * s, 6 * t * s - 3 * t * t, 3 * t * t], -1)
+
+
+def eval_patches(nets: np.ndarray, u: np.ndarray, v: np.ndarray):
+    """Point, dS/du, dS/dv of non-rational nets (n, 16, 4) at (u, v), float64."""
+    P = nets[..., :3].astype(np.float64).reshape(-1, 4, 4, 3)  # [n][j][i]
+    Bu, Bv, dBu, dBv = bernstein(u), bernstein(v), dbernstein(u), dbernstein(v)
+    S = np.einsum("nj,ni,njic->nc", Bv, Bu, P)
+    Su = np.einsum("nj,ni,njic->nc", Bv, dBu, P)
+    Sv = np.einsum("nj,ni,njic->nc", dBv, Bu, P)
+    return S, Su, Sv
+
+
+# ----------------------------------------------------------------- C3 ----
+def grazing_rays(surface: Surface, n: int, seed: int = 3, max_deg: float = 0.5, t0=(1.0, 10.0)) -> np.ndarray:
+    """Rays that graze the surface: pick a patch and (u,v) uniformly, take a
+    tangent direction at S(u,v), tilt it out of the tangent plane by an angle
+    ~ U(-max_deg, max_deg) degrees and start the ray t0 ~ U(1,10) before S.
+    Returns SoA (7, n) float32: ox oy oz dx dy dz tmax (= inf)."""
+    rng = SplitMix64(seed)
+    nets = surface.patches()
+    p = rng.integers(n, surface.patch_count)
+    u = rng.uniform(n)
+    v = rng.uniform(n)
+    S, Su, Sv = eval_patches(nets[p], u, v)
+    N = np.cross(Su, Sv)
+    N = N / np.sqrt((N * N).sum(-1, keepdims=True))
+    T1 = Su / np.sqrt((Su * Su).sum(-1, keepdims=True))
+    T2 = np.cross(N, T1)
+    phi = rng.uniform(n, 0.0, 2 * math.pi)
+    sphi, cphi = _sincos(phi)
+    T = cphi[:, None] * T1 + sphi[:, None] * T2
+    th = rng.uniform(n, -max_deg, max_deg) * (math.pi / 180.0)
+    sth, cth = _sincos(th)
+    d = cth[:, None] * T + sth[:, None] * N
+    d = d / np.sqrt((d * d).sum(-1, keepdims=True))
+    t = rng.uniform(n, *t0)
+    o = S - t[:, None] * d
+    rays = np.empty((7, n), dtype=np.float32)
+    rays[0:3] = o.T
+    rays[3:6] = d.T
+    rays[6] = np.inf
+    return rays
+
+
+def random_subset(n_total: int, fraction: float, seed: int) -> np.ndarray:
+    """Sorted seeded subset of range(n_total) of size round(fraction*n_total)."""
+    rng = SplitMix64(seed)
+    k = max(1, int(round(fraction * n_total)))
+    keys = rng.u64(n_total)
+    return np.sort(np.argsort(keys, kind="stable")[:k])

@@ -1,0 +1,215 @@
+/*
+ * cgspline.h -- C ABI of libcgspline_gb300.so, a GB300 (sm_103a) implementation
+ * of the ray--bicubic-patch path of MachSilva/cgspline.
+ *
+ * All entry points return an int status (CGS_OK == 0); nothing aborts, traps
+ * or throws across this boundary.  Pointers documented as "device" are CUDA
+ * device pointers on the scene's device; "host" pointers are ordinary host
+ * memory.  Streams are cudaStream_t passed as void* (NULL = legacy default
+ * stream).  Reference paths below are relative to the reference project root.
+ */
+#ifndef CGSPLINE_GB300_H
+#define CGSPLINE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- status -- */
+enum cgs_status {
+    CGS_OK = 0,
+    CGS_ERR_INVALID_ARGUMENT = 1,
+    CGS_ERR_CUDA = 2,              /* a CUDA runtime call failed (the reference aborts: src/rt/CUDAUtility.cpp:8-22) */
+    CGS_ERR_OUT_OF_MEMORY = 3,
+    CGS_ERR_NOT_BUILT = 4,         /* scene used before cgs_scene_build */
+    CGS_ERR_HASH_BUCKET_OVERFLOW = 5, /* > 4 keys share a displacement bucket (reference: __trap, src/rt/PerfectHashFunction.cu:44-46) */
+    CGS_ERR_HASH_FAILED = 6,       /* no perfect hash in 16 trials (reference: src/rt/BVH.cpp:26-28 throws) */
+    CGS_ERR_EMPTY_LEAF = 7,        /* BVH leaf without elements (reference: src/rt/BVH.cpp:85-87 throws) */
+    CGS_ERR_BUSY = 8,              /* a render is still in flight (reference: src/rt/RayTracer.cu:110-116 warns and returns) */
+    CGS_ERR_DEVICE_LIMIT = 9,      /* a kernel hit a bounded loop or stack limit (reference: __trap, src/Spline_BezierClipping.cu:736-737) */
+    CGS_ERR_ADMISSION = 10,        /* serving: request does not fit the HBM budget */
+    CGS_ERR_NOT_FOUND = 11
+};
+
+const char* cgs_status_string(int status);
+int cgs_version(void);
+
+/* ----------------------------------------------------------- options -- */
+enum cgs_method { CGS_METHOD_CLIP = 0, CGS_METHOD_SUBDIV = 1 };
+/* FP32: the reference's arithmetic.  FP32_POLISH64: FP32 search, then an FP64
+ * Newton polish of (u,v,t) of the winning hit.  FP64: the whole search in FP64. */
+enum cgs_precision { CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP64 = 2 };
+/* PLAIN: one thread per pixel runs the whole bounce chain (the reference's
+ * launch shape, src/rt/RayTracer.cu:171-178).  WAVEFRONT: persistent,
+ * stage-separated kernels over compacted ray queues. */
+enum cgs_schedule { CGS_SCHED_PLAIN = 0, CGS_SCHED_WAVEFRONT = 1 };
+
+/* src/rt/Scene.h:79-95 */
+typedef struct cgs_material {
+    float diffuse[3];
+    float specular[3];   /* f0 */
+    float metalness;
+    float roughness;
+} cgs_material;
+
+/* src/rt/Scene.h:47-77: angle < 0.01 directional, > 1.57 point, else spot */
+typedef struct cgs_light {
+    float color[3];
+    float strength;
+    float position[3];
+    float range;         /* 0 = infinite (inverse-square falloff) */
+    float direction[3];
+    float angle;
+} cgs_light;
+
+/* src/rt/Scene.h:16-45: camera looks down its local -z with +y up */
+typedef struct cgs_camera {
+    float rotation[4];   /* quaternion x, y, z, w */
+    float position[3];
+    float scale[3];
+    float fovy;          /* radians */
+} cgs_camera;
+
+/* src/rt/RayTracer.h:26-34 plus this build's choices */
+typedef struct cgs_render_options {
+    int recursion_depth; /* mirror bounces after the primary hit (reference GPU default 6) */
+    float eps;           /* shadow / bounce ray offset (reference 1e-4) */
+    int flip_y;
+    int method;          /* enum cgs_method */
+    int precision;       /* enum cgs_precision */
+    float tol;           /* search tolerance on the projected net (reference 2^-12) */
+    int schedule;        /* enum cgs_schedule */
+} cgs_render_options;
+
+/* Rays as structure of arrays; direction must be unit length. */
+typedef struct cgs_rays {
+    const float* ox; const float* oy; const float* oz;
+    const float* dx; const float* dy; const float* dz;
+    const float* tmax;   /* ray.max (src/rt/Intersection.h:16-24) */
+} cgs_rays;
+
+/* Closest-hit results (src/rt/Intersection.h:28-34); patch = object = -1 on a miss.
+ * For any-hit queries only patch is written (0 = occluded, -1 = free). */
+typedef struct cgs_hits {
+    float* t; float* u; float* v;
+    int32_t* patch;
+    int32_t* object;
+} cgs_hits;
+
+typedef struct cgs_counters {
+    uint64_t rays;            /* rays traced by the last call (all kinds) */
+    uint64_t primary_rays, bounce_rays, shadow_rays;
+    uint64_t nodes;           /* inner BVH nodes visited */
+    uint64_t hash_lookups;    /* stackless backtracks through the perfect hash */
+    uint64_t candidates;      /* (ray, patch) pairs searched */
+    uint64_t iterations;      /* clip / subdivision iterations */
+    uint64_t device_errors;   /* bounded-loop or stack-limit exits */
+    uint64_t kernel_launches;
+} cgs_counters;
+
+/* -------------------------------------------------------------- scene -- */
+typedef struct cgs_scene cgs_scene;
+
+int cgs_scene_create(cgs_scene** out, int device);
+int cgs_scene_destroy(cgs_scene* scene);
+
+/* A BezierSurface (src/rt/Primitive.h:90-116): points are xyzw float4, each
+ * patch is 16 uint32 indices, point (i,j) at 4*j+i. */
+int cgs_scene_add_surface(cgs_scene* scene, const float* points_xyzw, uint32_t npoints,
+                          const uint32_t* indices, uint32_t nindices, uint32_t* surface_id);
+
+/* One row of the Scene object arrays (src/rt/Scene.h:99-112).  Matrices are
+ * column-major.  patch_material (nullable, one entry per patch) indexes
+ * materials[] and overrides `material` per patch. */
+int cgs_scene_add_object(cgs_scene* scene, uint32_t surface, const float local2world[16],
+                         const float world2local[16], const cgs_material* material,
+                         const uint32_t* patch_material, const cgs_material* materials,
+                         uint32_t nmaterials, uint32_t* object_id);
+
+int cgs_scene_set_lights(cgs_scene* scene, const cgs_light* lights, uint32_t n);
+int cgs_scene_set_environment(cgs_scene* scene, const float background[3], const float ambient[3]);
+
+/* BVH::build for every surface (BezierSurface::buildBVH, src/rt/Primitive.cu:199-220)
+ * and the object level (Scene::buildBVH, src/rt/Scene.cu:218-232): host median
+ * split, one element per leaf (src/rt/BVH.cpp:9-124). */
+int cgs_bvh_build(cgs_scene* scene);
+
+/* BVH::buildHashTable for every BVH (src/rt/BVH.cpp:24-38) with the GPU
+ * perfect-hash build (PerfectHashFunction::build, src/rt/PerfectHashFunction.cu:229-503),
+ * made deterministic. */
+int cgs_hash_build(cgs_scene* scene, void* stream);
+
+/* cgs_bvh_build + device upload + cgs_hash_build (MainWindow::convertScene's
+ * acceleration steps, src/MainWindow.cpp:479-491). */
+int cgs_scene_build(cgs_scene* scene, void* stream);
+
+/* Device bytes held by a built scene. */
+int cgs_scene_footprint(const cgs_scene* scene, uint64_t* bytes);
+
+/* which = surface id, or -1 for the object-level BVH.
+ * sizes = nodes, indices, table size, displacement size, keys. */
+int cgs_bvh_sizes(const cgs_scene* scene, int32_t which, uint32_t sizes[5]);
+/* nodes: 14 uint32 per node = leftBox lo,hi; rightBox lo,hi (float bits); left; right|first
+ * (src/rt/BVH.h:23-39).  params = A, B, N (table size), mask.  Tables are read
+ * back from the device. */
+int cgs_bvh_export(const cgs_scene* scene, int32_t which, uint32_t* nodes, uint32_t* keys,
+                   uint32_t* indices, uint32_t* table, uint32_t* disp, uint32_t params[4]);
+
+/* ------------------------------------------------------------ queries -- */
+/* Closest hit (BVH::hashIntersect + rt::intersect, src/rt/BVH.h:178-266,
+ * src/rt/Primitive.cu:222-248, Context::intersect src/rt/RayTracer.cu:295-349)
+ * or any hit (src/rt/BVH.h:268-350, src/rt/Primitive.cu:250-268) for n rays.
+ * rays and hits are device pointers.  Asynchronous on `stream`. */
+int cgs_intersect(cgs_scene* scene, const cgs_rays* rays, uint32_t n, int method, int precision,
+                  float tol, int any_hit, const cgs_hits* hits, void* stream);
+
+/* Same with host rays / hits: copies in, runs, copies out, synchronises. */
+int cgs_intersect_host(cgs_scene* scene, const cgs_rays* rays, uint32_t n, int method, int precision,
+                       float tol, int any_hit, const cgs_hits* hits, void* stream);
+
+/* spline::doBezierClipping / doSubdivision on explicit (ray, patch) pairs
+ * (src/Spline.h:488-508): ray k against patch patch_ids[k] of `surface`.
+ * hits->t is hit.distance (in: current best, out: closer hit if found);
+ * hits->patch is set to 1 when a closer hit was found, else 0.  Device pointers. */
+int cgs_patch_intersect(cgs_scene* scene, uint32_t surface, const cgs_rays* rays,
+                        const uint32_t* patch_ids, uint32_t n, int method, float tol,
+                        const cgs_hits* hits, void* stream);
+
+/* ------------------------------------------------------------- render -- */
+/* RayTracer::render (src/rt/RayTracer.cu:107-180): width x height pixels,
+ * one primary ray each, PBR shading with shadow rays and
+ * options->recursion_depth mirror bounces.  framebuffer: device RGBA8 sRGB,
+ * row stride `stride` pixels (>= width).  linear_rgb: optional device float
+ * (height, width, 3) clamped to [0,1].  Asynchronous; returns CGS_ERR_BUSY if
+ * the scene's previous render has not finished. */
+int cgs_render(cgs_scene* scene, const cgs_camera* camera, uint32_t width, uint32_t height,
+               const cgs_render_options* options, uint32_t* framebuffer, uint32_t stride,
+               float* linear_rgb, void* stream);
+
+/* Same with host framebuffer / linear_rgb (either may be NULL); synchronises. */
+int cgs_render_host(cgs_scene* scene, const cgs_camera* camera, uint32_t width, uint32_t height,
+                    const cgs_render_options* options, uint32_t* framebuffer, float* linear_rgb,
+                    void* stream);
+
+/* RayTracer::running (src/rt/RayTracer.h:45-48): 1 while a render is in flight. */
+int cgs_render_running(cgs_scene* scene);
+
+/* Counters of the scene's last query or render (synchronises the stream it ran on). */
+int cgs_scene_counters(cgs_scene* scene, cgs_counters* out);
+
+/* ------------------------------------------------------ perfect hash -- */
+/* PerfectHashFunction::build on n device keys (src/rt/PerfectHashFunction.cu:229-503).
+ * Outputs (device): disp[displ_capacity], table[table_capacity] with
+ * table[h(keys[i])] = i; params (host) = A, B, N, mask, trials.
+ * displacement size = bit_floor(max(2, (n-1)>>1)); table_capacity must be at
+ * least n + 15*max(4, 0.05n).  Synchronises `stream`. */
+int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t displ_capacity,
+                           uint32_t* table, uint32_t table_capacity, uint32_t params[5], void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CGSPLINE_GB300_H */

@@ -1,0 +1,214 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle on the same seeded inputs.
+
+Bars: BVH topology and perfect-hash tables bit-exact; hit/miss and patch id
+identical (a different patch id is allowed only when both hits lie within
+1e-5 of a shared patch edge and their t agree to 1e-6 relative -- a tie);
+t within 1e-5 relative, (u,v) within 1e-3 of the oracle's FP32 reference
+semantics; after the FP64 polish t within 1e-5 relative of the FP64 oracle.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from cgspline_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    return torch
+
+
+@pytest.fixture(scope="module")
+def rt():
+    from cgspline_gb300 import rt
+    return rt
+
+
+@pytest.fixture(scope="module")
+def c1_gpu(rt, c1_scene):
+    return rt.GpuScene(c1_scene)
+
+
+@pytest.fixture(scope="module")
+def c2_small():
+    return S.scene_c2(nu=32, nv=32)
+
+
+@pytest.fixture(scope="module")
+def c2_small_gpu(rt, c2_small):
+    return rt.GpuScene(c2_small)
+
+
+@pytest.fixture(scope="module")
+def c2_small_oracle(oracle_mod, c2_small):
+    return oracle_mod.OracleScene(c2_small)
+
+
+def edge_tie(u, v, tol=1e-5):
+    return (np.minimum.reduce([u, 1 - u, v, 1 - v]) < tol)
+
+
+def compare_hits(g, o, t_rtol=1e-5, uv_atol=1e-3):
+    gp, op = np.asarray(g["patch"]), np.asarray(o["patch"])
+    assert np.array_equal(gp >= 0, op >= 0), f"hit/miss disagreements: {int(((gp >= 0) != (op >= 0)).sum())}"
+    hit = op >= 0
+    diff = hit & (gp != op)
+    if diff.any():
+        ties = edge_tie(np.asarray(g["u"])[diff], np.asarray(g["v"])[diff]) & \
+            edge_tie(np.asarray(o["u"])[diff], np.asarray(o["v"])[diff])
+        rel = np.abs(np.asarray(g["t"])[diff] - np.asarray(o["t"])[diff]) / np.asarray(o["t"])[diff]
+        assert ties.all() and (rel < 1e-6).all(), f"{int(diff.sum())} patch-id disagreements"
+    same = hit & (gp == op)
+    rel = np.abs(np.asarray(g["t"])[same] - np.asarray(o["t"])[same]) / np.asarray(o["t"])[same]
+    assert rel.max(initial=0) < t_rtol, rel.max()
+    du = np.abs(np.asarray(g["u"])[same] - np.asarray(o["u"])[same])
+    dv = np.abs(np.asarray(g["v"])[same] - np.asarray(o["v"])[same])
+    assert max(du.max(initial=0), dv.max(initial=0)) < uv_atol
+    return int(hit.sum()), int(diff.sum())
+
+
+def to_host(d):
+    return {k: v.cpu().numpy() for k, v in d.items()}
+
+
+def test_bvh_and_hash_bit_exact(c1_gpu, c1_oracle):
+    for which in (0, -1):
+        g, o = c1_gpu.bvh(which), c1_oracle.bvh(which)
+        for k in ("nodes", "keys", "indices", "table", "disp"):
+            assert np.array_equal(g[k], o[k]), (which, k)
+        assert (g["A"], g["B"], g["N"], g["mask"]) == (o["A"], o["B"], o["N"], o["mask"])
+
+
+def test_bvh_and_hash_bit_exact_torus(c2_small_gpu, c2_small_oracle):
+    g, o = c2_small_gpu.bvh(0), c2_small_oracle.bvh(0)
+    for k in ("nodes", "keys", "indices", "table", "disp"):
+        assert np.array_equal(g[k], o[k]), k
+    assert (g["A"], g["B"], g["N"]) == (o["A"], o["B"], o["N"])
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 1000, 32767, 65537, 1 << 20])
+def test_perfect_hash_matches_oracle(rt, oracle_mod, n):
+    keys = np.arange(1, n + 1, dtype=np.uint32)
+    o = oracle_mod.hash_build(keys)
+    h = rt.PerfectHashFunction()
+    assert h.build(keys) == 0
+    assert (h.A, h.B, h.N, h.mask) == (o["A"], o["B"], o["N"], o["mask"])
+    assert np.array_equal(h.disp, o["disp"]) and np.array_equal(h.table, o["table"])
+
+
+def test_c1_closest_hits(c1_gpu, c1_oracle, oracle_mod, torch):
+    rays = oracle_mod.camera_rays(S.camera_c1(), 256, 256)
+    o = c1_oracle.intersect(rays)
+    g = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda()))
+    nhit, nties = compare_hits(g, o)
+    assert nhit > 40000
+    assert c1_gpu.counters()["device_errors"] == 0
+
+
+def test_c1_golden_on_gpu(c1_gpu, torch):
+    import os
+    gdn = np.load(os.path.join(os.path.dirname(__file__), "golden", "c1_golden.npz"))
+    g = to_host(c1_gpu.intersect(torch.from_numpy(gdn["rays"]).cuda()))
+    compare_hits(g, dict(t=gdn["t"], u=gdn["u"], v=gdn["v"], patch=gdn["patch"]))
+
+
+def test_c1_host_entry_point_matches_device(c1_gpu, oracle_mod, torch):
+    rays = oracle_mod.camera_rays(S.camera_c1(), 64, 64)
+    a = c1_gpu.intersect(rays)  # numpy -> cgs_intersect_host (copies inside)
+    b = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda()))
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_torus_closest_and_any(c2_small_gpu, c2_small_oracle, oracle_mod, torch):
+    rays = oracle_mod.camera_rays(S.camera_c2(), 240, 135)
+    o = c2_small_oracle.intersect(rays)
+    g = to_host(c2_small_gpu.intersect(torch.from_numpy(rays).cuda()))
+    # FP32 (u,v) near silhouettes is ill-conditioned; compare t loosely here and tightly after the polish
+    compare_hits(g, o, t_rtol=2e-3, uv_atol=5e-2)
+    oa = c2_small_oracle.intersect(rays, any_hit=True)
+    ga = to_host(c2_small_gpu.intersect(torch.from_numpy(rays).cuda(), any_hit=True))
+    assert np.array_equal(ga["patch"] >= 0, oa["patch"] >= 0)
+
+
+def test_torus_polish_vs_fp64(rt, c2_small_gpu, c2_small_oracle, oracle_mod, torch):
+    rays = oracle_mod.camera_rays(S.camera_c2(), 240, 135)
+    o64 = c2_small_oracle.intersect(rays, precision=oracle_mod.FP64)
+    g = to_host(c2_small_gpu.intersect(torch.from_numpy(rays).cuda(), precision=rt.FP32_POLISH64))
+    gp, op = g["patch"], o64["patch"]
+    assert np.array_equal(gp >= 0, op >= 0)
+    both = (gp >= 0) & (gp == op)
+    rel = np.abs(g["t"][both] - o64["t"][both]) / o64["t"][both]
+    assert rel.max() <= 1e-5, rel.max()
+
+
+def test_subdivision_agrees_with_clipping(rt, c1_gpu, c1_oracle, oracle_mod, torch):
+    rays = oracle_mod.camera_rays(S.camera_c1(), 128, 128)
+    o = c1_oracle.intersect(rays, method=oracle_mod.SUBDIV)
+    g = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda(), method=rt.SUBDIV))
+    compare_hits(g, o, t_rtol=1e-5, uv_atol=2e-3)
+
+
+def test_patch_pairs_entry_point(rt, c1_gpu, c1_scene, oracle_mod, torch):
+    rays = oracle_mod.camera_rays(S.camera_c1(), 32, 32)
+    n = rays.shape[1]
+    pids = np.arange(n, dtype=np.int32) % 16
+    found, t, u, v = rt.do_bezier_clipping(c1_gpu, 0, torch.from_numpy(rays).cuda(), torch.from_numpy(pids).cuda())
+    found, t = found.cpu().numpy(), t.cpu().numpy()
+    s = c1_scene.surfaces[0]
+    for k in range(0, n, 7):
+        hit, to, uv, _ = oracle_mod.patch_intersect(s.points, s.indices[16 * pids[k]:16 * pids[k] + 16], rays[:, k],
+                                                    method=oracle_mod.CLIP_DEVICE)
+        assert bool(found[k]) == hit
+        if hit:
+            assert abs(t[k] - to) / to < 1e-5
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_render_c1_matches_oracle(rt, c1_gpu, c1_oracle, schedule):
+    cam = S.camera_c1()
+    w = h = 128
+    ro = c1_oracle.render(cam, w, h, depth=0)
+    tracer = rt.RayTracer(rt.Options(recursion_depth=0, schedule=schedule))
+    fb, lin = tracer.render_host(cam, c1_gpu, w, h)
+    err = np.abs(lin - ro["rgb"])
+    assert np.sqrt((err ** 2).mean()) < 1e-4
+    assert err.max() < 1e-2
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_render_torus_pbr_matches_oracle(rt, c2_small_gpu, c2_small_oracle, schedule):
+    cam = S.camera_c2()
+    w, h = 192, 108
+    ro = c2_small_oracle.render(cam, w, h, depth=1)
+    tracer = rt.RayTracer(rt.Options(recursion_depth=1, schedule=schedule))
+    fb, lin = tracer.render_host(cam, c2_small_gpu, w, h)
+    err = np.abs(lin - ro["rgb"])
+    rmse = float(np.sqrt((err ** 2).mean()))
+    # bounce rays start from FP32 hit points: a few silhouette pixels may differ
+    assert rmse < 5e-3, rmse
+    assert (err.max(axis=-1) > 0.05).mean() < 2e-3
+    c = c2_small_gpu.counters()
+    assert c["device_errors"] == 0 and c["rays"] >= w * h
+
+
+def test_schedules_agree(rt, c2_small_gpu):
+    cam = S.camera_c2()
+    a = rt.RayTracer(rt.Options(recursion_depth=1, schedule=rt.PLAIN)).render_host(cam, c2_small_gpu, 160, 90)[1]
+    b = rt.RayTracer(rt.Options(recursion_depth=1, schedule=rt.WAVEFRONT)).render_host(cam, c2_small_gpu, 160, 90)[1]
+    assert np.abs(a - b).max() < 1e-5
+
+
+def test_device_frame_and_busy_flag(rt, c1_gpu, torch):
+    frame = rt.Frame(100, 60, alignment=32)
+    assert frame.stride == 128
+    tracer = rt.RayTracer(rt.Options(recursion_depth=0))
+    tracer.render(frame, S.camera_c1(), c1_gpu)
+    torch.cuda.synchronize()
+    assert not tracer.running()
+    img = frame.rgba()
+    assert img.shape == (60, 100, 4) and (img[..., 3] == 255).all()

@@ -1,0 +1,194 @@
+"""CPU tests of the oracle (the checker): known-answer patches, BVH and hash
+invariants of the reference (src/rt/BVH.cpp:9-124, src/rt/PerfectHashFunction.cu:486-503),
+agreement between its FP32 variants and its FP64 truth, and determinism."""
+import math
+
+import numpy as np
+import pytest
+
+from cgspline_gb300 import scenes as S
+
+
+def grid_patch(P00, P10, P01, P11):
+    """Degree-elevated bilinear patch: control point (i,j) = bilinear(i/3, j/3)."""
+    P00, P10, P01, P11 = (np.asarray(p, np.float64) for p in (P00, P10, P01, P11))
+    pts = []
+    for j in range(4):
+        for i in range(4):
+            u, v = i / 3.0, j / 3.0
+            p = (1 - u) * (1 - v) * P00 + u * (1 - v) * P10 + (1 - u) * v * P01 + u * v * P11
+            pts.append([*p, 1.0])
+    return np.asarray(pts, np.float32)
+
+
+def ray7(o, d):
+    d = np.asarray(d, np.float64)
+    d = d / np.linalg.norm(d)
+    return np.asarray([*o, *d, np.inf], np.float32)
+
+
+def test_planar_patch_known_answer(oracle_mod):
+    # plane through (0,0,0) spanned by U=(1,0.2,0.1), V=(0.1,1,0.3): S(u,v) = uU + vV
+    U, V = np.array([1.0, 0.2, 0.1]), np.array([0.1, 1.0, 0.3])
+    pts = grid_patch([0, 0, 0], U, V, U + V)
+    idx = np.arange(16, dtype=np.uint32)
+    rng = S.SplitMix64(11)
+    for _ in range(50):
+        u, v = rng.uniform(2, 0.05, 0.95)
+        target = u * U + v * V
+        o = target + np.array([0.3, -0.2, 2.0]) * rng.uniform(1, 1.0, 3.0)[0]
+        r = ray7(o, target - o)
+        t_true = np.linalg.norm(target - o)
+        for method in (oracle_mod.CLIP_HOST, oracle_mod.CLIP_DEVICE, oracle_mod.SUBDIV):
+            hit, t, uv, _ = oracle_mod.patch_intersect(pts, idx, r, method=method)
+            assert hit
+            assert abs(t - t_true) / t_true < 1e-5
+            assert abs(uv[0] - u) < 1e-4 and abs(uv[1] - v) < 1e-4
+
+
+def test_bilinear_patch_known_answer(oracle_mod):
+    # hyperbolic paraboloid z = (x - 0.5)(y - 0.5) over the unit square (a twisted bilinear patch)
+    P00, P10, P01, P11 = [0, 0, 0.25], [1, 0, -0.25], [0, 1, -0.25], [1, 1, 0.25]
+    pts = grid_patch(P00, P10, P01, P11)
+    idx = np.arange(16, dtype=np.uint32)
+    rng = S.SplitMix64(12)
+    for _ in range(50):
+        u, v = rng.uniform(2, 0.05, 0.95)
+        target = np.array([u, v, (u - 0.5) * (v - 0.5)])
+        o = target + np.array([0.1, 0.2, 3.0])
+        r = ray7(o, target - o)
+        t_true = np.linalg.norm(target - o)
+        hit, t, uv, _ = oracle_mod.patch_intersect(pts, idx, r)
+        assert hit
+        assert abs(t - t_true) / t_true < 1e-5
+        assert abs(uv[0] - u) < 2e-4 and abs(uv[1] - v) < 2e-4
+
+
+def test_miss_and_behind(oracle_mod):
+    pts = grid_patch([0, 0, 0], [1, 0, 0.1], [0, 1, 0.1], [1, 1, 0.2])
+    idx = np.arange(16, dtype=np.uint32)
+    # pointing away from the patch: the root is behind the origin (V.d <= 0 is rejected)
+    hit, t, _, _ = oracle_mod.patch_intersect(pts, idx, ray7([0.5, 0.5, 2.0], [0, 0, 1]))
+    assert not hit and math.isinf(t)
+    # passing beside the patch
+    hit, _, _, _ = oracle_mod.patch_intersect(pts, idx, ray7([3.0, 3.0, 2.0], [0, 0, -1]))
+    assert not hit
+    # a closer current hit.distance culls the root (onHit keeps t < hit.distance)
+    hit, _, _, _ = oracle_mod.patch_intersect(pts, idx, ray7([0.5, 0.5, 2.0], [0.01, 0.02, -1]), t=0.5)
+    assert not hit
+
+
+def test_bvh_invariants(c1_oracle):
+    b = c1_oracle.bvh(0)
+    nodes, keys, ind = b["nodes"], b["keys"], b["indices"]
+    P = 16
+    assert nodes.shape[0] == 2 * P - 1 and keys.size == 2 * P - 1
+    EMPTY = 0xFFFFFFFF
+    leaves = 0
+    seen = set()
+    for i, nd in enumerate(nodes):
+        left, right = int(nd[12]), int(nd[13])
+        if left == EMPTY:
+            leaves += 1
+            assert ind[right] != EMPTY and ind[right + 1] == EMPTY  # one element per leaf
+            seen.add(int(ind[right]))
+        else:
+            # pre-order layout: the left child follows its parent; heap keys
+            assert left == i + 1
+            assert keys[left] == 2 * keys[i] and keys[right] == 2 * keys[i] + 1
+            box = nd[:12].view(np.float32)
+            for child, off in ((left, 0), (right, 6)):
+                cb = nodes[child][:12].view(np.float32)
+                lo, hi = cb[0:3], cb[3:6]
+                if nodes[child][12] != EMPTY:
+                    lo = np.minimum(lo, cb[6:9]); hi = np.maximum(hi, cb[9:12])
+                assert np.array_equal(box[off:off + 3], lo) and np.array_equal(box[off + 3:off + 6], hi)
+    assert leaves == P and seen == set(range(P))
+    assert keys[0] == 1
+
+
+def test_perfect_hash_injective_and_deterministic(oracle_mod, c1_oracle):
+    b = c1_oracle.bvh(0)
+    keys = b["keys"]
+    h = oracle_mod.hash_build(keys)
+    assert h["status"] == 0
+    assert h["A"] == b["A"] and h["B"] == b["B"] and h["N"] == b["N"]
+    assert np.array_equal(h["table"], b["table"]) and np.array_equal(h["disp"], b["disp"])
+    slots = ((h["A"] * keys.astype(np.uint64) + h["B"] + h["disp"][keys & h["mask"]]) & 0xFFFFFFFF) % h["N"]
+    assert len(set(slots.tolist())) == keys.size
+    assert np.array_equal(h["table"][slots], np.arange(keys.size))
+    h2 = oracle_mod.hash_build(keys)
+    assert all(np.array_equal(h[k], h2[k]) for k in ("disp", "table"))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 1023, 4097, 65535, 200001])
+def test_perfect_hash_sizes(oracle_mod, n):
+    # heap keys of a complete-ish binary tree, as the BVH produces
+    keys = np.arange(1, n + 1, dtype=np.uint32)
+    h = oracle_mod.hash_build(keys)
+    assert h["status"] == 0
+    dsz = 1 << (max(2, (n - 1) >> 1).bit_length() - 1)
+    assert h["disp"].size == dsz
+    slots = ((h["A"] * keys.astype(np.uint64) + h["B"] + h["disp"][keys & h["mask"]]) & 0xFFFFFFFF) % h["N"]
+    assert np.unique(slots).size == n
+
+
+def test_hash_bucket_overflow_reported(oracle_mod):
+    # 5 keys in one displacement bucket: the reference traps; the oracle reports status 1
+    keys = np.array([8, 16, 24, 32, 40, 1, 2, 3, 4, 5, 6, 7], np.uint32)
+    assert oracle_mod.hash_build(keys)["status"] == 1
+
+
+def test_c1_variants_agree_with_fp64(oracle_mod, c1_oracle):
+    rays = oracle_mod.camera_rays(S.camera_c1(), 128, 128)
+    r = c1_oracle.intersect(rays)
+    r64 = c1_oracle.intersect(rays, precision=oracle_mod.FP64)
+    rd = c1_oracle.intersect(rays, method=oracle_mod.CLIP_DEVICE)
+    hit = r["patch"] >= 0
+    assert np.array_equal(hit, r64["patch"] >= 0)
+    assert np.array_equal(r["patch"], r64["patch"])
+    assert np.array_equal(r["patch"], rd["patch"])
+    rel = np.abs(r["t"][hit] - r64["t"][hit]) / r64["t"][hit]
+    assert rel.max() < 1e-5
+    assert np.abs(rd["t"][hit] - r["t"][hit]).max() / r["t"][hit].min() < 1e-5
+
+
+def test_c1_golden(c1_oracle, oracle_mod):
+    """The restatement against committed vectors (tests/golden/make_golden.py)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "c1_golden.npz"))
+    sc = S.scene_c1()
+    assert np.array_equal(sc.surfaces[0].points, g["points"])
+    assert np.array_equal(sc.surfaces[0].indices, g["indices"])
+    b = c1_oracle.bvh(0)
+    for k in ("nodes", "keys", "indices", "table", "disp"):
+        assert np.array_equal(b[k], g["bvh_" + k]), k
+    rays = g["rays"]
+    r = c1_oracle.intersect(rays)
+    assert np.array_equal(r["patch"], g["patch"])
+    hit = g["patch"] >= 0
+    np.testing.assert_allclose(r["t"][hit], g["t"][hit], rtol=2e-6)
+    np.testing.assert_allclose(r["u"][hit], g["u"][hit], atol=2e-5)
+    np.testing.assert_allclose(r["v"][hit], g["v"][hit], atol=2e-5)
+
+
+def test_render_c1_small(c1_oracle, oracle_mod):
+    out = c1_oracle.render(S.camera_c1(), 64, 64, depth=0)
+    assert out["primary"] == 64 * 64
+    rgb = out["rgb"]
+    assert np.isfinite(rgb).all() and 0.0 <= rgb.min() and rgb.max() <= 1.0
+    # background pixels equal the background colour exactly; hits are lit
+    assert (rgb.reshape(-1, 3) > 0.15).any()
+
+
+def test_scene_generators_deterministic():
+    a, b = S.torus_surface(nu=16, nv=16, seed=5), S.torus_surface(nu=16, nv=16, seed=5)
+    assert np.array_equal(a.points, b.points) and np.array_equal(a.indices, b.indices)
+    c = S.torus_surface(nu=16, nv=16, seed=6)
+    assert not np.array_equal(a.points, c.points)
+    # C0 across patch edges: neighbouring patches share their boundary points exactly
+    nets = a.patches()
+    nu = 16
+    for p in range(nu * nu):
+        q = (p // nu) * nu + (p % nu + 1) % nu  # next patch along u
+        np.testing.assert_array_equal(nets[p].reshape(4, 4, 4)[:, 3], nets[q].reshape(4, 4, 4)[:, 0])
