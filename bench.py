@@ -203,11 +203,14 @@ def main():
     stream = torch.cuda.current_stream()
 
     def step():
+        # a scene refuses a new render while its previous one is in flight
+        # (src/rt/RayTracer.cu:110-116), so frames are issued one at a time;
+        # the events below time each frame on the device.
         tracer.render(frame, cam, g, stream)
 
     for _ in range(max(3, args.warmup)):
         step()
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
     counters = g.counters()
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -221,6 +224,7 @@ def main():
             starts[k].record(stream)
             step()
             ends[k].record(stream)
+            ends[k].synchronize()
         torch.cuda.synchronize()
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = float(sum(ms))
@@ -268,7 +272,7 @@ def main():
             plain = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=prec, schedule=rt.PLAIN))
             for _ in range(2):
                 plain.render(frame, cam, g, stream)
-            torch.cuda.synchronize()
+                torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             pm = 0.0
             for k in range(3):

@@ -5,7 +5,7 @@ this package is the host-side mirror of the reference's call surface
 (rt.py), the seeded synthetic scenes (scenes.py) and the build recipe
 (build.py).
 """
-from . import scenes  # noqa: F401
+from . import rt, scenes  # noqa: F401
 
 __all__ = ["scenes", "rt", "build_library"]
 
@@ -13,10 +13,3 @@ __all__ = ["scenes", "rt", "build_library"]
 def build_library(force: bool = False, verbose: bool = False) -> str:
     from . import build
     return build.build(force=force, verbose=verbose)
-
-
-def __getattr__(name):
-    if name == "rt":
-        from . import rt
-        return rt
-    raise AttributeError(name)
