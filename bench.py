@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--precision", default="polish64", choices=["fp32", "polish64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--quick", action="store_true", help="no plain-path comparison, no FP64 check")
+    ap.add_argument("--size", default=None, help="WxH of a smaller frame (profiling cases); default 1920x1080")
     return ap.parse_args()
 
 
@@ -175,6 +176,9 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
+    global W, H
+    if args.size:
+        W, H = (int(x) for x in args.size.lower().split("x"))
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -29,7 +29,21 @@ struct DevBVH
 {
     uint32_t nodeBase, indexBase, tableBase, dispBase;
     uint32_t A, B, N, mask;  // h(k) = (A k + B + disp[k & mask]) mod N, src/rt/PerfectHashFunction.h:58-63
+    unsigned long long Nmagic;  // ceil(2^64 / N): x mod N by multiplication (fastmod_u32)
 };
+
+// x mod N for 32-bit x and N >= 1 with M = ceil(2^64 / N) (Lemire, Kaser,
+// Kurz, "Faster remainder by direct computation", 2019): the low 64 bits of
+// M*x, times N, keep the remainder in their high 64 bits.
+__host__ __device__ __forceinline__ unsigned long long fastmod_magic(uint32_t N)
+{
+    return ~0ull / N + 1ull;
+}
+__device__ __forceinline__ uint32_t fastmod(uint32_t x, uint32_t N, unsigned long long M)
+{
+    unsigned long long low = M * x;
+    return uint32_t(__umul64hi(low, N));
+}
 
 struct DevObject  // one row of Scene::ObjectArrays, src/rt/Scene.h:109-112
 {
@@ -336,83 +350,103 @@ __device__ __forceinline__ void project_net(float2* net, const float4* __restric
 // original net (patchCopy, src/SplineMat.h:248-257), which is re-projected
 // from the patch so that it need not stay in registers.  Stack overflow and
 // the iteration cap end the search with an error bit instead of __trap().
-static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, LocalCounters& lc)
+//
+// The search is resumable: clip_begin sets up the state, each clip_step runs
+// one iteration of the reference loop and returns false when the search is
+// over, so a persistent kernel can interleave candidates lane by lane.
+struct ClipState
 {
-    float4 st[kClipStack];  // (min.x, min.y, max.x, max.y)
-    int sl = 0;
-    int cutsideStack = 0;
-    float2 emin = make_float2(0.0f, 0.0f), emax = make_float2(1.0f, 1.0f);
     float2 buf[16];
-    project_net(buf, sink.P, sink.o, sink.d);
-    bool found = false;
-    for (int it = 0;; it++)
+    float2 emin, emax;
+    int cutsideStack, sl, it;
+    bool found;
+};
+
+__device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink)
+{
+    project_net(c.buf, sink.P, sink.o, sink.d);
+    c.emin = make_float2(0.0f, 0.0f);
+    c.emax = make_float2(1.0f, 1.0f);
+    c.cutsideStack = 0;
+    c.sl = 0;
+    c.it = 0;
+    c.found = false;
+}
+
+__device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, float tol, LocalCounters& lc)
+{
+    if (c.it++ >= kMaxClipIterations) { lc.errors |= kErrClipIterations; return false; }
+    lc.iterations++;
+    const int cutside = c.cutsideStack & 1;
+    if (len2(c.buf[3] - c.buf[12]) < tol && len2(c.buf[15] - c.buf[0]) < tol)
+        c.found |= approximateIntersection(sink, c.buf, c.emin, c.emax);
+    else
     {
-        if (it >= kMaxClipIterations) { lc.errors |= kErrClipIterations; break; }
-        lc.iterations++;
-        const int cutside = cutsideStack & 1;
-        bool pop = true;
-        if (len2(buf[3] - buf[12]) < tol && len2(buf[15] - buf[0]) < tol)
-            found |= approximateIntersection(sink, buf, emin, emax);
-        else
+        float lower, upper;
+        clip_range(c.buf, cutside, lower, upper);
+        float delta = upper - lower;
+        if (delta > 0.8f)
         {
-            float lower, upper;
-            clip_range(buf, cutside, lower, upper);
-            float delta = upper - lower;
-            if (delta > 0.8f)
+            float4 pushed;
+            if (cutside == 0)
             {
-                float4 pushed;
-                if (cutside == 0)
-                {
-                    float hx = 0.5f * (emin.x + emax.x);
-                    pushed = make_float4(emin.x, emin.y, hx, emax.y);
-                    emin.x = hx;
-                    cutsideStack = (cutsideStack << 1) | 3;
-                    subpatchU(buf, 0.5f, 1.0f);
-                }
-                else
-                {
-                    float hy = 0.5f * (emin.y + emax.y);
-                    pushed = make_float4(emin.x, emin.y, emax.x, hy);
-                    emin.y = hy;
-                    cutsideStack = (cutsideStack << 1) & ~3;
-                    subpatchV(buf, 0.5f, 1.0f);
-                }
-                if (sl >= kClipStack) { lc.errors |= kErrClipStack; break; }
-                st[sl++] = pushed;
-                pop = false;
+                float hx = 0.5f * (c.emin.x + c.emax.x);
+                pushed = make_float4(c.emin.x, c.emin.y, hx, c.emax.y);
+                c.emin.x = hx;
+                c.cutsideStack = (c.cutsideStack << 1) | 3;
+                subpatchU(c.buf, 0.5f, 1.0f);
             }
-            else if (delta > 0.0f)
+            else
             {
-                if (cutside == 0)
-                {
-                    float sx = emax.x - emin.x;
-                    float u0 = emin.x + sx * lower, u1 = emax.x - sx * (1.0f - upper);
-                    subpatchU(buf, lower, upper);
-                    emin.x = u0; emax.x = u1;
-                }
-                else
-                {
-                    float sy = emax.y - emin.y;
-                    float v0 = emin.y + sy * lower, v1 = emax.y - sy * (1.0f - upper);
-                    subpatchV(buf, lower, upper);
-                    emin.y = v0; emax.y = v1;
-                }
-                cutsideStack ^= 1;
-                pop = false;
+                float hy = 0.5f * (c.emin.y + c.emax.y);
+                pushed = make_float4(c.emin.x, c.emin.y, c.emax.x, hy);
+                c.emin.y = hy;
+                c.cutsideStack = (c.cutsideStack << 1) & ~3;
+                subpatchV(c.buf, 0.5f, 1.0f);
             }
+            if (c.sl >= kClipStack) { lc.errors |= kErrClipStack; return false; }
+            st[c.sl++] = pushed;
+            return true;
         }
-        if (pop)
+        else if (delta > 0.0f)
         {
-            cutsideStack >>= 1;
-            if (--sl < 0) break;
-            float4 e = st[sl];
-            emin = make_float2(e.x, e.y); emax = make_float2(e.z, e.w);
-            project_net(buf, sink.P, sink.o, sink.d);
-            subpatchU(buf, emin.x, emax.x);
-            subpatchV(buf, emin.y, emax.y);
+            if (cutside == 0)
+            {
+                float sx = c.emax.x - c.emin.x;
+                float u0 = c.emin.x + sx * lower, u1 = c.emax.x - sx * (1.0f - upper);
+                subpatchU(c.buf, lower, upper);
+                c.emin.x = u0; c.emax.x = u1;
+            }
+            else
+            {
+                float sy = c.emax.y - c.emin.y;
+                float v0 = c.emin.y + sy * lower, v1 = c.emax.y - sy * (1.0f - upper);
+                subpatchV(c.buf, lower, upper);
+                c.emin.y = v0; c.emax.y = v1;
+            }
+            c.cutsideStack ^= 1;
+            return true;
         }
     }
-    return found;
+    // pop
+    c.cutsideStack >>= 1;
+    if (--c.sl < 0) return false;
+    float4 e = st[c.sl];
+    c.emin = make_float2(e.x, e.y);
+    c.emax = make_float2(e.z, e.w);
+    project_net(c.buf, sink.P, sink.o, sink.d);
+    subpatchU(c.buf, c.emin.x, c.emax.x);
+    subpatchV(c.buf, c.emin.y, c.emax.y);
+    return true;
+}
+
+static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, LocalCounters& lc)
+{
+    float4 st[kClipStack];
+    ClipState c;
+    clip_begin(c, sink);
+    while (clip_step(c, st, sink, tol, lc)) {}
+    return c.found;
 }
 
 // Stackless 2-D subdivision (doSubdivision2D_device,
@@ -540,7 +574,7 @@ static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P
 __device__ __forceinline__ uint32_t hash_slot(const DevScene& S, const DevBVH& b, uint32_t key)
 {
     uint32_t disp = __ldg(S.disps + b.dispBase + (key & b.mask));
-    return (b.A * key + b.B + disp) % b.N;
+    return fastmod(b.A * key + b.B + disp, b.N, b.Nmagic);
 }
 
 // _node_intersect, src/rt/BVH.h:147-176
@@ -591,12 +625,11 @@ __device__ __forceinline__ bool hash_traverse(const DevScene& S, const DevBVH& b
     {
         if (step >= kMaxTraversalSteps) { lc.errors |= kErrTraversal; break; }
         const float4* q = nodes + 4ull * node;
-        float4 q3 = __ldg(q + 3);
+        const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
         uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
         if (left != EMPTY)
         {
             lc.nodes++;
-            float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
             float L0, R0;
             bool iL = slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), o, inv) && L0 < limit;
             bool iR = slab(R0, f3(q1.z, q1.w, q2.x), f3(q2.y, q2.z, q2.w), o, inv) && R0 < limit;
@@ -660,6 +693,25 @@ __device__ __forceinline__ bool search_patch(HitSink& sink, const Query& q, Loca
     return q.method == 0 ? clip_patch(sink, q.tol, lc) : subdiv_patch(sink, q.tol, lc);
 }
 
+// FP64 Newton polish of a world-space hit, done in the object's space.
+__device__ __forceinline__ void polish_hit(const DevScene& S, float3 o, float3 d, HitRecord& hit)
+{
+    const DevObject& ob = S.objects[hit.object];
+    const float4* P = S.patches + 16ull * (__ldg(S.patchBase + ob.surface) + uint32_t(hit.patch));
+    const float* m = ob.w2l;
+    double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+    double lw = ox * m[3] + oy * m[7] + oz * m[11] + m[15];
+    double3 lo = make_double3((ox * m[0] + oy * m[4] + oz * m[8] + m[12]) / lw,
+                              (ox * m[1] + oy * m[5] + oz * m[9] + m[13]) / lw,
+                              (ox * m[2] + oy * m[6] + oz * m[10] + m[14]) / lw);
+    double3 ld = make_double3(dx * m[0] + dy * m[4] + dz * m[8], dx * m[1] + dy * m[5] + dz * m[9],
+                              dx * m[2] + dy * m[6] + dz * m[10]);
+    double sc = sqrt(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z);
+    ld = make_double3(ld.x / sc, ld.y / sc, ld.z / sc);
+    double t = double(hit.t) * sc, u = hit.u, v = hit.v;
+    if (newton_polish64(P, lo, ld, t, u, v)) { hit.t = float(t / sc); hit.u = float(u); hit.v = float(v); }
+}
+
 // Closest hit over the object-level BVH and each object's patch BVH
 // (Context::intersect, src/rt/RayTracer.cu:295-349; rt::intersect,
 // src/rt/Primitive.cu:222-248).  hit.t must hold ray.max on entry.
@@ -696,24 +748,7 @@ __device__ __forceinline__ int scene_closest(const DevScene& S, float3 o, float3
         return false;
     };
     hash_traverse<false>(S, S.bvhs[S.topBVH], o, inv, limit, objfn, lc);
-    if (nearest >= 0 && q.precision == 1)
-    {
-        // FP64 Newton polish of the winning hit in object space
-        const DevObject& ob = S.objects[nearest];
-        const float4* P = S.patches + 16ull * (__ldg(S.patchBase + ob.surface) + uint32_t(hit.patch));
-        const float* m = ob.w2l;
-        double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
-        double lw = ox * m[3] + oy * m[7] + oz * m[11] + m[15];
-        double3 lo = make_double3((ox * m[0] + oy * m[4] + oz * m[8] + m[12]) / lw,
-                                  (ox * m[1] + oy * m[5] + oz * m[9] + m[13]) / lw,
-                                  (ox * m[2] + oy * m[6] + oz * m[10] + m[14]) / lw);
-        double3 ld = make_double3(dx * m[0] + dy * m[4] + dz * m[8], dx * m[1] + dy * m[5] + dz * m[9],
-                                  dx * m[2] + dy * m[6] + dz * m[10]);
-        double sc = sqrt(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z);
-        ld = make_double3(ld.x / sc, ld.y / sc, ld.z / sc);
-        double t = double(hit.t) * sc, u = hit.u, v = hit.v;
-        if (newton_polish64(P, lo, ld, t, u, v)) { hit.t = float(t / sc); hit.u = float(u); hit.v = float(v); }
-    }
+    if (nearest >= 0 && q.precision == 1) polish_hit(S, o, d, hit);
     return nearest;
 }
 
@@ -803,7 +838,12 @@ __device__ __forceinline__ uint32_t pack_srgb(float3 c)
 }
 
 // ---------------------------------------------------- warp-level helpers --
-__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lane_id()
+{
+    unsigned id;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(id));
+    return id;
+}
 
 // Warp-aggregated atomic increment: every active lane with `want` gets a slot.
 __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool want)

@@ -1,0 +1,537 @@
+// k_engine.cu -- the query engine: closest / any hit over the two-level
+// hashed stackless BVH with Bezier clipping.
+//
+// A query runs a few passes of two persistent kernels:
+//
+// k_collect walks the reference's traversal (BVH::hashIntersect,
+// src/rt/BVH.h:178-350, nested through the object level as in
+// Context::intersect, src/rt/RayTracer.cu:295-383) -- same stackless key /
+// postponed-bit state, same perfect-hash backtracking, same nearer-child-first
+// order -- and appends what it meets to the ray's chunk: each patch of a
+// leaf with the entry distance of the leaf's box, and markers where it enters
+// or leaves an object.  It culls with the ray's best t as known at the start
+// of the pass (the ray's extent in the first pass).  When the chunk is full
+// the ray parks: its key, postponed bits and node are saved and the next
+// pass resumes it.
+//
+// k_resolve replays the reference's leaf callbacks over the chunk in order: a
+// patch whose leaf box starts at or beyond the object's current best t is
+// skipped (the reference's `L0 < hit.t` test), any other runs the
+// Bezier-clipping search with the current best as hit.distance
+// (doBezierClipping, src/Spline_BezierClipping.cu:46-114) and keeps a
+// strictly closer hit; leaving an object keeps its hit if it beats the world
+// best.  A subtree the reference culls lies behind its box entry, at or
+// beyond the best t of that moment, so none of its patches can give a
+// strictly closer hit; collecting it anyway changes nothing except for hits
+// within the search tolerance of the current best (near-ties).  Any-hit
+// queries stop at the first patch that reports a hit.
+//
+// Both kernels refill lanes one ray (k_collect) or one clip iteration
+// (k_resolve) at a time, so heavy-tailed per-ray work does not idle the other
+// lanes of a warp, and take rays in id order so a warp's rays stay coherent.
+// Rays still unfinished after kPasses passes are completed by k_rest, the
+// inline version of the same search.
+#include <algorithm>
+
+#include "kernels.h"
+
+namespace cgs {
+
+namespace {
+
+constexpr int kCollectThreads = 256;
+constexpr int kResolveThreads = 128;
+constexpr uint32_t kChunk = 16;   // list entries per ray and pass
+constexpr int kPasses = 4;
+
+// list entry word 0: a patch index, or one of these markers (word 1 = object)
+constexpr uint32_t kLeave = 0xFFFFFFFFu, kEnter = 0xFFFFFFFEu, kCont = 0xFFFFFFFDu;
+// ray status
+enum : uint32_t { kPending = 0, kTraversed = 1, kFinished = 2 };
+
+struct Eng  // per-ray engine state, SoA over the query's capacity
+{
+    uint32_t *status, *count;
+    uint2* list;  // [cap * kChunk]
+    uint32_t *node, *key, *post, *leaf, *tnode, *tkey, *tpost, *tleaf, *jumped;
+    int32_t *obj, *lpatch;
+    float *leafEntry, *limit, *lt, *lu, *lv;
+    uint32_t* ctl;  // per pass: collect fetch, resolve fetch
+};
+
+constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 16;
+
+Eng carve(uint32_t* base, uint32_t cap)
+{
+    Eng e;
+    uint32_t* p = base;
+    auto take = [&](size_t words) { uint32_t* r = p; p += words; return r; };
+    e.status = take(cap); e.count = take(cap);
+    e.list = reinterpret_cast<uint2*>(take(2ull * cap * kChunk));
+    e.node = take(cap); e.key = take(cap); e.post = take(cap); e.leaf = take(cap); e.tnode = take(cap);
+    e.tkey = take(cap); e.tpost = take(cap); e.tleaf = take(cap); e.jumped = take(cap);
+    e.obj = reinterpret_cast<int32_t*>(take(cap)); e.lpatch = reinterpret_cast<int32_t*>(take(cap));
+    e.leafEntry = reinterpret_cast<float*>(take(cap)); e.limit = reinterpret_cast<float*>(take(cap));
+    e.lt = reinterpret_cast<float*>(take(cap)); e.lu = reinterpret_cast<float*>(take(cap));
+    e.lv = reinterpret_cast<float*>(take(cap));
+    e.ctl = take(4 * (kPasses + 1));
+    return e;
+}
+
+// Warp-wide refill: every lane in `need` gets the next index from *fetch.
+__device__ __forceinline__ uint32_t warp_fetch(uint32_t* fetch, bool need)
+{
+    unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+    if (!m) return EMPTY;
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    unsigned lt = (1u << lane_id()) - 1u;
+    return need ? base + __popc(m & lt) : EMPTY;
+}
+
+__device__ __forceinline__ void load_ray(const RaysSoA& r, uint32_t i, float3& o, float3& d, float& tmax)
+{
+    o = f3(r.ox[i], r.oy[i], r.oz[i]);
+    d = f3(r.dx[i], r.dy[i], r.dz[i]);
+    tmax = r.tmax ? r.tmax[i] : INFINITY;
+}
+
+// ------------------------------------------------------------ collect --
+template<bool kAny>
+__global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, RaysSoA rays, uint32_t n0,
+                                                                const uint32_t* nDev, Eng E, int pass, Counters* cnt)
+{
+    const uint32_t n = nDev ? *nDev : n0;
+    LocalCounters lc;
+    bool active = false, exhausted = false, jumped = false;
+    uint32_t rid = 0, ncand = 0;
+    float3 o = f3(0, 0, 0), inv = f3(0, 0, 0), lo = f3(0, 0, 0), linv = f3(0, 0, 0);
+    float tmax = 0, lmax = 0, limit = 0, lt = 0;
+    uint32_t node = 0, key = 1, post = 0, leaf = EMPTY, tnode = 0, tkey = 1, tpost = 0, tleaf = EMPTY;
+    float leafEntry = -INFINITY;
+    int32_t obj = -1;
+    const DevBVH topB = S.bvhs[S.topBVH];
+    DevBVH B = topB;
+    uint32_t nrays = 0;
+    uint2* list = nullptr;
+    for (;;)
+    {
+        const bool need = !active && !exhausted;
+        const uint32_t idx = warp_fetch(E.ctl + 4 * pass, need);
+        if (need)
+        {
+            if (idx >= n)
+                exhausted = true;
+            else if (pass == 0 || E.status[idx] == kPending)
+            {
+                rid = idx;
+                active = true;
+                float3 d;
+                load_ray(rays, rid, o, d, tmax);
+                inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+                list = E.list + size_t(rid) * kChunk;
+                ncand = 0;
+                if (pass == 0)
+                {
+                    node = 0; key = 1; post = 0; leaf = EMPTY; obj = -1; jumped = false;
+                    leafEntry = -INFINITY; limit = tmax;
+                    B = topB;
+                    nrays++;
+                }
+                else
+                {
+                    node = E.node[rid]; key = E.key[rid]; post = E.post[rid]; leaf = E.leaf[rid];
+                    jumped = E.jumped[rid] != 0; leafEntry = E.leafEntry[rid]; obj = E.obj[rid];
+                    limit = kAny ? tmax : E.limit[rid];
+                    B = topB;
+                    if (obj >= 0)
+                    {
+                        tnode = E.tnode[rid]; tkey = E.tkey[rid]; tpost = E.tpost[rid]; tleaf = E.tleaf[rid];
+                        const DevObject& O = S.objects[obj];
+                        float3 ld; float sinv;
+                        to_local(O, o, d, tmax, lo, ld, lmax, sinv);
+                        linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
+                        lt = kAny ? lmax : E.lt[rid];
+                        B = S.bvhs[O.surface];
+                        list[ncand++] = make_uint2(kCont, uint32_t(obj));
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active || !exhausted) == 0) break;
+        if (!active) continue;
+
+        if (ncand >= kChunk)
+        {
+            // chunk full: park before this step
+            E.node[rid] = node; E.key[rid] = key; E.post[rid] = post; E.leaf[rid] = leaf;
+            E.jumped[rid] = jumped; E.leafEntry[rid] = leafEntry; E.obj[rid] = obj;
+            E.tnode[rid] = tnode; E.tkey[rid] = tkey; E.tpost[rid] = tpost; E.tleaf[rid] = tleaf;
+            E.count[rid] = ncand;
+            E.status[rid] = kPending;
+            active = false;
+            continue;
+        }
+
+        bool ascend = false, done = false;
+        if (leaf != EMPTY)
+        {
+            const uint32_t e = __ldg(S.indices + B.indexBase + leaf);
+            if (e != EMPTY)
+            {
+                leaf++;
+                if (obj < 0)
+                {
+                    // descend into object e (Context::intersect's callback)
+                    tnode = node; tkey = key; tpost = post; tleaf = leaf;
+                    obj = int32_t(e);
+                    const DevObject& O = S.objects[e];
+                    const float3 d = f3(rays.dx[rid], rays.dy[rid], rays.dz[rid]);
+                    float3 ld; float sinv;
+                    to_local(O, o, d, tmax, lo, ld, lmax, sinv);
+                    linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
+                    lt = lmax;
+                    B = S.bvhs[O.surface];
+                    node = 0; key = 1; post = 0; leaf = EMPTY; jumped = false;
+                    leafEntry = -INFINITY;
+                    list[ncand++] = make_uint2(kEnter, e);
+                }
+                else
+                    list[ncand++] = make_uint2(e, __float_as_uint(leafEntry));
+            }
+            else
+            {
+                leaf = EMPTY;
+                ascend = true;
+            }
+        }
+        else
+        {
+            const float4* q = S.nodes + 4ull * (B.nodeBase + node);
+            // one round trip for the whole 64-byte node
+            const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+            const uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
+            const bool top = obj < 0;
+            const float3 ro = top ? o : lo, ri = top ? inv : linv;
+            if (left == EMPTY)
+            {
+                leaf = right;
+                if (jumped)
+                {
+                    // reached through the hash: its entry is the slab test of its own box
+                    float L0;
+                    slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), ro, ri);
+                    leafEntry = L0;
+                }
+                jumped = false;
+            }
+            else
+            {
+                lc.nodes++;
+                jumped = false;
+                const float lim = top ? limit : lt;
+                float L0, R0;
+                const bool iL = slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), ro, ri) && L0 < lim;
+                const bool iR = slab(R0, f3(q1.z, q1.w, q2.x), f3(q2.y, q2.z, q2.w), ro, ri) && R0 < lim;
+                if (iL || iR) post <<= 1;
+                if (iL && iR)
+                {
+                    post |= 1u;
+                    if (L0 < R0) { key = key << 1; node = left; leafEntry = L0; }
+                    else { key = (key << 1) ^ 1u; node = right; leafEntry = R0; }
+                }
+                else if (iL) { key = key << 1; node = left; leafEntry = L0; }
+                else if (iR) { key = (key << 1) ^ 1u; node = right; leafEntry = R0; }
+                else ascend = true;
+            }
+        }
+        if (ascend)
+        {
+            if (post == 0)
+            {
+                if (obj < 0)
+                    done = true;
+                else
+                {
+                    list[ncand++] = make_uint2(kLeave, uint32_t(obj));
+                    obj = -1;
+                    B = topB;
+                    node = tnode; key = tkey; post = tpost; leaf = tleaf;
+                    leafEntry = -INFINITY;
+                }
+            }
+            else
+            {
+                const int levels = __ffs(post) - 1;
+                post >>= levels;
+                key = (key >> levels) ^ 1u;
+                post ^= 1u;
+                lc.hashLookups++;
+                node = __ldg(S.tables + B.tableBase + hash_slot(S, B, key));
+                jumped = true;
+            }
+        }
+        if (done)
+        {
+            E.count[rid] = ncand;
+            E.status[rid] = kTraversed;
+            active = false;
+        }
+    }
+    flush_counters(cnt, lc, nrays);
+}
+
+// ------------------------------------------------------------ resolve --
+template<bool kAny>
+__global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA rays, uint32_t n0,
+                                                             const uint32_t* nDev, Eng E, int pass, Query q,
+                                                             HitsSoA hits, int32_t* occluded, Counters* cnt)
+{
+    const uint32_t n = nDev ? *nDev : n0;
+    LocalCounters lc;
+    float4 stack[kClipStack];
+    ClipState c;
+    HitSink sink {nullptr, f3(0, 0, 0), f3(0, 0, 1), 0.0f, make_float2(0, 0)};
+    bool active = false, exhausted = false, clipping = false;
+    uint32_t rid = 0, k = 0, count = 0, patch = 0;
+    int32_t obj = -1, lpatch = -1;
+    float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
+    float tmax = 0, lmax = 0, sinv = 1, lt = 0, lu = 0, lv = 0, limit = 0;
+    const uint2* list = nullptr;
+    for (;;)
+    {
+        const bool need = !active && !exhausted;
+        const uint32_t idx = warp_fetch(E.ctl + 4 * pass + 1, need);
+        if (need)
+        {
+            if (idx >= n)
+                exhausted = true;
+            else
+            {
+                const uint32_t st = E.status[idx];
+                count = E.count[idx];
+                if (count > 0 && st != kFinished)
+                {
+                    rid = idx;
+                    active = true;
+                    k = 0;
+                    obj = -1;
+                    clipping = false;
+                    load_ray(rays, rid, o, d, tmax);
+                    limit = kAny ? tmax : (pass == 0 ? tmax : E.limit[rid]);
+                    list = E.list + size_t(rid) * kChunk;
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active || !exhausted) == 0) break;
+        if (!active) continue;
+
+        bool finished = false;
+        if (clipping)
+        {
+            bool found = false, more = false;
+            if (q.method == 0) { more = clip_step(c, stack, sink, q.tol, lc); found = c.found; }
+            else found = subdiv_patch(sink, q.tol, lc);
+            if (!more)
+            {
+                clipping = false;
+                if (kAny)
+                {
+                    if (found) { occluded[rid] = 0; E.status[rid] = kFinished; finished = true; }
+                }
+                else if (found)
+                {
+                    lt = sink.dist; lu = sink.uv.x; lv = sink.uv.y; lpatch = int32_t(patch);
+                }
+            }
+        }
+        else if (k < count)
+        {
+            const uint2 e = list[k++];
+            if (e.x == kEnter || e.x == kCont)
+            {
+                obj = int32_t(e.y);
+                float3 ld;
+                to_local(S.objects[obj], o, d, tmax, sink.o, ld, lmax, sinv);
+                sink.d = ld;
+                if (e.x == kEnter || kAny) { lt = lmax; lpatch = -1; lu = 0.0f; lv = 0.0f; }
+                else { lt = E.lt[rid]; lu = E.lu[rid]; lv = E.lv[rid]; lpatch = E.lpatch[rid]; }
+            }
+            else if (e.x == kLeave)
+            {
+                if (!kAny && lpatch >= 0)
+                {
+                    const float t = lt * sinv;
+                    if (t < limit)
+                    {
+                        limit = t;
+                        hits.t[rid] = t; hits.u[rid] = lu; hits.v[rid] = lv;
+                        hits.patch[rid] = lpatch; hits.object[rid] = obj;
+                    }
+                }
+                obj = -1;
+            }
+            else
+            {
+                patch = e.x;
+                const float entry = __uint_as_float(e.y);
+                if (entry < (kAny ? lmax : lt))
+                {
+                    const uint32_t surface = S.objects[obj].surface;
+                    sink.P = S.patches + 16ull * (__ldg(S.patchBase + surface) + patch);
+                    sink.dist = kAny ? lmax : lt;
+                    sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
+                    lc.candidates++;
+                    if (q.method == 0) clip_begin(c, sink);
+                    clipping = true;
+                }
+            }
+        }
+        else
+        {
+            // end of this pass's chunk: keep what the next pass needs
+            if (!kAny)
+            {
+                E.limit[rid] = limit;
+                if (obj >= 0) { E.lt[rid] = lt; E.lu[rid] = lu; E.lv[rid] = lv; E.lpatch[rid] = lpatch; }
+            }
+            finished = true;
+        }
+        if (finished)
+        {
+            active = false;
+            E.count[rid] = 0;
+        }
+    }
+    flush_counters(cnt, lc, 0);
+}
+
+// Rays unfinished after the last pass: the inline search from the start.
+template<bool kAny>
+__global__ void __launch_bounds__(128) k_rest(DevScene S, RaysSoA rays, uint32_t n0, const uint32_t* nDev, Eng E,
+                                              Query q, HitsSoA hits, int32_t* occluded, Counters* cnt)
+{
+    const uint32_t n = nDev ? *nDev : n0;
+    LocalCounters lc;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    for (uint32_t rid = tid; rid < n; rid += nt)
+    {
+        if (E.status[rid] != kPending) continue;
+        float3 o, d; float tmax;
+        load_ray(rays, rid, o, d, tmax);
+        Query q32 = q;
+        q32.precision = 0;  // the polish kernel runs afterwards
+        if (kAny)
+            occluded[rid] = scene_any(S, o, d, tmax, q32, lc) ? 0 : -1;
+        else
+        {
+            HitRecord h {tmax, 0.0f, 0.0f, -1, -1};
+            int ob = scene_closest(S, o, d, tmax, q32, h, lc);
+            hits.t[rid] = ob >= 0 ? h.t : tmax; hits.u[rid] = h.u; hits.v[rid] = h.v;
+            hits.patch[rid] = ob >= 0 ? h.patch : -1; hits.object[rid] = ob;
+        }
+    }
+    flush_counters(cnt, lc, 0);
+}
+
+__global__ void k_init(RaysSoA rays, uint32_t n0, const uint32_t* nDev, HitsSoA hits, int32_t* occluded, Eng E)
+{
+    const uint32_t n = nDev ? *nDev : n0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        E.count[i] = 0;
+        if (occluded) { occluded[i] = -1; continue; }
+        hits.t[i] = rays.tmax ? rays.tmax[i] : INFINITY;
+        hits.u[i] = 0.0f; hits.v[i] = 0.0f; hits.patch[i] = -1; hits.object[i] = -1;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_polish(DevScene S, RaysSoA rays, uint32_t n0, const uint32_t* nDev,
+                                                HitsSoA hits)
+{
+    const uint32_t n = nDev ? *nDev : n0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const int32_t ob = hits.object[i];
+        if (ob < 0) continue;
+        HitRecord h {hits.t[i], hits.u[i], hits.v[i], hits.patch[i], ob};
+        polish_hit(S, f3(rays.ox[i], rays.oy[i], rays.oz[i]), f3(rays.dx[i], rays.dy[i], rays.dz[i]), h);
+        hits.t[i] = h.t; hits.u[i] = h.u; hits.v[i] = h.v;
+    }
+}
+
+int sms()
+{
+    static int v = 0;
+    if (!v)
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    }
+    return v;
+}
+
+int resident(const void* fn, int threads)
+{
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
+    return sms() * (per > 0 ? per : 1);
+}
+
+template<bool kAny>
+void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, HitsSoA hits,
+            int32_t* occluded, Eng E, Counters* cnt, cudaStream_t stream, int& nl)
+{
+    static int gCol = 0, gRes = 0;
+    if (!gCol)
+    {
+        gCol = resident((const void*)k_collect<kAny>, kCollectThreads);
+        gRes = resident((const void*)k_resolve<kAny>, kResolveThreads);
+    }
+    const uint32_t warps = (n + 31) / 32;
+    const int gc = int(std::min<uint32_t>(uint32_t(gCol), warps / (kCollectThreads / 32) + 1));
+    const int gr = int(std::min<uint32_t>(uint32_t(gRes), warps / (kResolveThreads / 32) + 1));
+    for (int p = 0; p < kPasses; p++)
+    {
+        k_collect<kAny><<<gc, kCollectThreads, 0, stream>>>(S, rays, n, nDev, E, p, cnt);
+        k_resolve<kAny><<<gr, kResolveThreads, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
+        nl += 2;
+    }
+    k_rest<kAny><<<sms() * 4, 128, 0, stream>>>(S, rays, n, nDev, E, q, hits, occluded, cnt);
+    nl++;
+}
+
+}  // namespace
+
+size_t engine_words(uint32_t capacity, int)
+{
+    return size_t(capacity) * kWordsPerRay + 4 * (kPasses + 1) + 64;
+}
+
+cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, bool any,
+                      HitsSoA hits, int32_t* occluded, uint32_t* scratch, uint32_t capacity, int, Counters* cnt,
+                      cudaStream_t stream, int* launches)
+{
+    if (nDev) n = capacity;  // grid sizing only; kernels read *nDev
+    if (n == 0) return cudaSuccess;
+    if (n > capacity) return cudaErrorInvalidValue;
+    Eng E = carve(scratch, capacity);
+    cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kPasses + 1), stream);
+    const int flat = sms() * 4;
+    k_init<<<flat, 256, 0, stream>>>(rays, n, nDev, hits, any ? occluded : nullptr, E);
+    int nl = 1;
+    if (any) launch<true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    else launch<false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    if (!any && q.precision == 1)
+    {
+        k_polish<<<flat * 2, 128, 0, stream>>>(S, rays, n, nDev, hits);
+        nl++;
+    }
+    if (launches) *launches += nl;
+    return cudaGetLastError();
+}
+
+}  // namespace cgs

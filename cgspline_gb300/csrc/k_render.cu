@@ -165,35 +165,8 @@ __global__ void k_wf_camera(RenderParams p, Q q, float* accum, uint32_t* count)
     if (blockIdx.x == 0 && threadIdx.x == 0) { count[0] = n; count[1] = 0; count[2] = 0; }
 }
 
-// closest hit over queue `cur`
-__global__ void __launch_bounds__(kWfThreads) k_wf_closest(DevScene S, Q q, const uint32_t* count, uint32_t* next,
-                                                           Query qq, HitRecord* hits, Counters* cnt)
-{
-    const uint32_t n = *count;
-    LocalCounters lc;
-    uint32_t nrays = 0;
-    for (;;)
-    {
-        uint32_t base = 0;
-        if (lane_id() == 0) base = atomicAdd(next, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t k = base + lane_id();
-        if (k < n)
-        {
-            float3 o, d;
-            q.get(k, o, d);
-            HitRecord h {INFINITY, 0.0f, 0.0f, -1, -1};
-            scene_closest(S, o, d, INFINITY, qq, h, lc);
-            hits[k] = h;
-            nrays++;
-        }
-    }
-    flush_counters(cnt, lc, nrays);
-}
-
 __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, RenderParams p, Q q, Q qn, const uint32_t* count,
-                                                         uint32_t* nextCount, uint32_t* shadowCount, const HitRecord* hits,
+                                                         uint32_t* nextCount, uint32_t* shadowCount, HitsSoA hits,
                                                          float* shadow, uint32_t* shadowSlot, uint32_t shadowCap,
                                                          float* contrib, int32_t* visible, float* base, float* accum,
                                                          int depthLeft)
@@ -207,7 +180,11 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, RenderParam
         HitRecord h {INFINITY, 0.0f, 0.0f, -1, -1};
         float3 o = f3(0, 0, 0), d = f3(0, 0, 1), att = f3(0, 0, 0);
         uint32_t pixel = 0;
-        if (live) { h = hits[k]; q.get(k, o, d); att = q.att(k); pixel = q.px[k]; }
+        if (live)
+        {
+            h = HitRecord {hits.t[k], hits.u[k], hits.v[k], hits.patch[k], hits.object[k]};
+            q.get(k, o, d); att = q.att(k); pixel = q.px[k];
+        }
         const bool isHit = live && h.object >= 0;
         if (live && !isHit)
         {
@@ -248,41 +225,21 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, RenderParam
     }
 }
 
-__global__ void __launch_bounds__(kWfThreads) k_wf_shadow(DevScene S, const float* __restrict__ shadow,
-                                                          const uint32_t* __restrict__ shadowSlot, uint32_t cap,
-                                                          const uint32_t* count, uint32_t* next, Query qq,
-                                                          int32_t* visible, Counters* cnt)
+__global__ void k_wf_visibility(const int32_t* occluded, const uint32_t* shadowSlot, const uint32_t* count, uint32_t cap,
+                                int32_t* visible)
 {
     const uint32_t n = min(*count, cap);
-    LocalCounters lc;
-    uint32_t nrays = 0;
-    for (;;)
-    {
-        uint32_t b = 0;
-        if (lane_id() == 0) b = atomicAdd(next, 32u);
-        b = __shfl_sync(0xFFFFFFFFu, b, 0);
-        if (b >= n) break;
-        const uint32_t k = b + lane_id();
-        if (k < n)
-        {
-            float3 o = f3(shadow[k], shadow[cap + k], shadow[2ull * cap + k]);
-            float3 d = f3(shadow[3ull * cap + k], shadow[4ull * cap + k], shadow[5ull * cap + k]);
-            float tmax = shadow[6ull * cap + k];
-            bool occ = scene_any(S, o, d, tmax, qq, lc);
-            visible[shadowSlot[k]] = occ ? 0 : 1;
-            nrays++;
-        }
-    }
-    flush_counters(cnt, lc, nrays);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        if (occluded[k] < 0) visible[shadowSlot[k]] = 1;
 }
 
-__global__ void k_wf_resolve(DevScene S, Q q, const uint32_t* count, const HitRecord* hits, const float* contrib,
+__global__ void k_wf_resolve(DevScene S, Q q, const uint32_t* count, HitsSoA hits, const float* contrib,
                              const int32_t* visible, const float* base, float* accum)
 {
     const uint32_t n = *count, nl = S.nlights;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
     {
-        if (hits[k].object < 0) continue;
+        if (hits.object[k] < 0) continue;
         float3 c = f3(base[3ull * k], base[3ull * k + 1], base[3ull * k + 2]);
         for (uint32_t l = 0; l < nl; l++)
         {
@@ -337,41 +294,43 @@ cudaError_t launch_render_wavefront(const DevScene& S, const RenderParams& p, co
                                     uint32_t* framebuffer, float* linear, Counters* counters, cudaStream_t stream,
                                     int* launches)
 {
-    static int gClosest = 0, gShadow = 0, gShade = 0;
-    if (!gClosest)
-    {
-        gClosest = blocks_for((const void*)k_wf_closest, kWfThreads);
-        gShadow = blocks_for((const void*)k_wf_shadow, kWfThreads);
-        gShade = blocks_for((const void*)k_wf_shade, kWfThreads);
-    }
+    static int gShade = 0;
+    if (!gShade) gShade = blocks_for((const void*)k_wf_shade, kWfThreads);
     const int gFlat = sm_count() * 8;
     int nl = 0;
-    const uint32_t n = p.width * p.height;
-    Q q[2] = {{wb.ray[0], wb.pixel[0], wb.capacity}, {wb.ray[1], wb.pixel[1], wb.capacity}};
+    const uint32_t cap = wb.capacity;
+    const uint32_t scap = wb.capacity * (wb.lightCapacity ? wb.lightCapacity : 1);
+    Q q[2] = {{wb.ray[0], wb.pixel[0], cap}, {wb.ray[1], wb.pixel[1], cap}};
     k_wf_camera<<<gFlat, 256, 0, stream>>>(p, q[0], wb.accum, wb.count);
     nl++;
-    uint32_t* work = wb.count + 3;  // 3: closest, 4: shadow
+    Query qa = p.q;
+    qa.precision = 0;
+    const float* sh = wb.shadow;
+    RaysSoA shadowRays {sh, sh + scap, sh + 2ull * scap, sh + 3ull * scap, sh + 4ull * scap, sh + 5ull * scap,
+                        sh + 6ull * scap};
     for (int level = 0, cur = 0; level <= p.depth; level++, cur ^= 1)
     {
-        cudaMemsetAsync(work, 0, 2 * sizeof(uint32_t), stream);
         cudaMemsetAsync(wb.count + (cur ^ 1), 0, sizeof(uint32_t), stream);
         cudaMemsetAsync(wb.count + 2, 0, sizeof(uint32_t), stream);
-        k_wf_closest<<<gClosest, kWfThreads, 0, stream>>>(S, q[cur], wb.count + cur, work, p.q, wb.hit, counters);
+        const float* r = wb.ray[cur];
+        RaysSoA rays {r, r + cap, r + 2ull * cap, r + 3ull * cap, r + 4ull * cap, r + 5ull * cap, nullptr};
+        cudaError_t e = run_query(S, rays, 0, wb.count + cur, p.q, false, wb.hit, nullptr, wb.engine, wb.engineCapacity,
+                                  kEnginePasses, counters, stream, &nl);
+        if (e != cudaSuccess) return e;
         k_wf_shade<<<gShade, kWfThreads, 0, stream>>>(S, p, q[cur], q[cur ^ 1], wb.count + cur, wb.count + (cur ^ 1),
-                                                      wb.count + 2, wb.hit, wb.shadow, wb.shadowSlot,
-                                                      wb.capacity * (wb.lightCapacity ? wb.lightCapacity : 1),
-                                                      wb.contrib, wb.visible, wb.base, wb.accum, p.depth - level);
-        k_wf_shadow<<<gShadow, kWfThreads, 0, stream>>>(S, wb.shadow, wb.shadowSlot,
-                                                        wb.capacity * (wb.lightCapacity ? wb.lightCapacity : 1),
-                                                        wb.count + 2, work + 1, p.q, wb.visible, counters);
+                                                      wb.count + 2, wb.hit, wb.shadow, wb.shadowSlot, scap, wb.contrib,
+                                                      wb.visible, wb.base, wb.accum, p.depth - level);
+        e = run_query(S, shadowRays, 0, wb.count + 2, qa, true, HitsSoA {}, wb.occluded, wb.engine, wb.engineCapacity,
+                      kEnginePasses, counters, stream, &nl);
+        if (e != cudaSuccess) return e;
+        k_wf_visibility<<<gFlat, 256, 0, stream>>>(wb.occluded, wb.shadowSlot, wb.count + 2, scap, wb.visible);
         k_wf_resolve<<<gFlat, 256, 0, stream>>>(S, q[cur], wb.count + cur, wb.hit, wb.contrib, wb.visible, wb.base,
                                                wb.accum);
-        nl += 4;
+        nl += 3;
     }
     k_wf_finish<<<gFlat, 256, 0, stream>>>(p, wb.accum, framebuffer, linear);
     nl++;
     if (launches) *launches += nl;
-    (void)n;
     return cudaGetLastError();
 }
 

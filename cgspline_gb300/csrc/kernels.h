@@ -21,6 +21,16 @@ cudaError_t launch_any(const DevScene& S, RaysSoA rays, uint32_t n, Query q, int
 cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, RaysSoA rays, const uint32_t* patch_ids,
                                uint32_t n, Query q, HitsSoA hits, Counters* counters, cudaStream_t stream);
 
+// ---------------------------------------------------------- query engine --
+// Closest / any hit of n rays (n from the host, or *nDev when nDev != null;
+// capacity bounds both) by alternating traversal and clip passes
+// (k_engine.cu).  scratch holds engine_words(capacity, passes) words.
+size_t engine_words(uint32_t capacity, int passes);
+cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, bool any,
+                      HitsSoA hits, int32_t* occluded, uint32_t* scratch, uint32_t capacity, int passes,
+                      Counters* counters, cudaStream_t stream, int* launches);
+constexpr int kEnginePasses = 12;
+
 // --------------------------------------------------------------- render --
 struct CameraSetup
 {
@@ -46,7 +56,10 @@ struct WavefrontBuffers
     float* ray[2];       // 9 floats per ray, SoA: ox oy oz dx dy dz ax ay az
     uint32_t* pixel[2];
     uint32_t* count;     // [0..1] queue sizes, [2] shadow count, [3..7] work counters
-    HitRecord* hit;      // per ray of the current queue
+    HitsSoA hit;         // per ray of the current queue
+    int32_t* occluded;   // per shadow ray
+    uint32_t* engine;    // query-engine scratch
+    uint32_t engineCapacity;
     float* shadow;       // 7 floats per shadow ray SoA: ox oy oz dx dy dz max
     uint32_t* shadowSlot;  // (ray index * nlights + light) of each shadow ray
     float* contrib;      // 3 floats per (ray, light) slot

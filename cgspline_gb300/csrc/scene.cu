@@ -191,10 +191,11 @@ struct cgs_scene
 
     // wavefront buffers
     WavefrontBuffers wb {};
-    DBuf<float> wfRay0, wfRay1, wfShadow, wfContrib, wfBase, wfAccum;
+    DBuf<float> wfRay0, wfRay1, wfShadow, wfContrib, wfBase, wfAccum, wfHitF;
     DBuf<uint32_t> wfPix0, wfPix1, wfCount, wfShadowSlot;
-    DBuf<HitRecord> wfHit;
-    DBuf<int32_t> wfVisible;
+    DBuf<int32_t> wfVisible, wfHitI, wfOccluded;
+    DBuf<uint32_t> engine;
+    uint32_t engineCapacity = 0;
     DBuf<uint32_t> fbStage;
     DBuf<float> linStage;
 
@@ -222,10 +223,12 @@ struct cgs_scene
         for (auto* b : {&indices, &tables, &disps, &patchBase, &patchMaterial, &keys, &scratch32, &work, &wfPix0,
                         &wfPix1, &wfCount, &wfShadowSlot, &fbStage})
             b->release();
-        for (auto* b : {&rayStage, &hitF, &wfRay0, &wfRay1, &wfShadow, &wfContrib, &wfBase, &wfAccum, &linStage})
+        for (auto* b : {&rayStage, &hitF, &wfRay0, &wfRay1, &wfShadow, &wfContrib, &wfBase, &wfAccum, &linStage,
+                        &wfHitF})
             b->release();
         bvhs.release(); dobjects.release(); materials.release(); dlights.release(); scratch64.release();
-        counters.release(); hitI.release(); wfHit.release(); wfVisible.release();
+        counters.release(); hitI.release(); wfHitF.release(); wfHitI.release(); wfOccluded.release();
+        wfVisible.release(); engine.release();
         if (finished) cudaEventDestroy(finished);
     }
 };
@@ -347,6 +350,7 @@ int upload(cgs_scene* sc)
         dispCursor += displ_size(n);
         d.mask = displ_size(n) - 1;
         d.N = n; d.A = 31; d.B = 19;
+        d.Nmagic = fastmod_magic(std::max<uint32_t>(n, 1));
     }
     for (const Surface& s : sc->surfaces)
     {
@@ -432,6 +436,7 @@ int hash_all(cgs_scene* sc, cudaStream_t stream)
         if (r < 0) return CGS_ERR_CUDA;
         if (r) return CGS_ERR_HASH_FAILED;
         d.A = params[0]; d.B = params[1]; d.N = params[2]; d.mask = params[3];
+        d.Nmagic = fastmod_magic(d.N);
     }
     CGS_TRY(cudaMemcpyAsync(sc->bvhs.p, sc->hbvh.data(), nb * sizeof(DevBVH), cudaMemcpyHostToDevice, stream));
     CGS_TRY(cudaStreamSynchronize(stream));
@@ -466,17 +471,31 @@ void camera_setup(const cgs_camera& c, uint32_t w, uint32_t h, int flip, CameraS
     if (flip) { s.tl[1] = -s.tl[1]; s.half_dy = -s.half_dy; }
 }
 
+int ensure_engine(cgs_scene* sc, uint32_t capacity)
+{
+    if (sc->engineCapacity >= capacity) return CGS_OK;
+    CGS_TRY(sc->engine.reserve(engine_words(capacity, kEnginePasses)));
+    sc->engineCapacity = capacity;
+    return CGS_OK;
+}
+
 int ensure_wavefront(cgs_scene* sc, uint32_t nrays)
 {
     uint32_t nl = std::max<uint32_t>(1, uint32_t(sc->lights.size()));
-    if (sc->wb.capacity >= nrays && sc->wb.lightCapacity >= nl) return CGS_OK;
+    if (sc->wb.capacity >= nrays && sc->wb.lightCapacity >= nl && sc->wb.engine == sc->engine.p) return CGS_OK;
     size_t cap = nrays, sc_ = size_t(nrays) * nl;
     CGS_TRY(sc->wfRay0.reserve(9 * cap));
     CGS_TRY(sc->wfRay1.reserve(9 * cap));
     CGS_TRY(sc->wfPix0.reserve(cap));
     CGS_TRY(sc->wfPix1.reserve(cap));
     CGS_TRY(sc->wfCount.reserve(8));
-    CGS_TRY(sc->wfHit.reserve(cap));
+    CGS_TRY(sc->wfHitF.reserve(3 * cap));
+    CGS_TRY(sc->wfHitI.reserve(2 * cap));
+    CGS_TRY(sc->wfOccluded.reserve(sc_));
+    {
+        int r = ensure_engine(sc, uint32_t(std::max<size_t>(cap, sc_)));
+        if (r) return r;
+    }
     CGS_TRY(sc->wfShadow.reserve(7 * sc_));
     CGS_TRY(sc->wfShadowSlot.reserve(sc_));
     CGS_TRY(sc->wfContrib.reserve(3 * sc_));
@@ -486,7 +505,11 @@ int ensure_wavefront(cgs_scene* sc, uint32_t nrays)
     WavefrontBuffers& wb = sc->wb;
     wb.ray[0] = sc->wfRay0.p; wb.ray[1] = sc->wfRay1.p;
     wb.pixel[0] = sc->wfPix0.p; wb.pixel[1] = sc->wfPix1.p;
-    wb.count = sc->wfCount.p; wb.hit = sc->wfHit.p; wb.shadow = sc->wfShadow.p; wb.shadowSlot = sc->wfShadowSlot.p;
+    wb.count = sc->wfCount.p; wb.shadow = sc->wfShadow.p; wb.shadowSlot = sc->wfShadowSlot.p;
+    wb.hit = HitsSoA {sc->wfHitF.p, sc->wfHitF.p + cap, sc->wfHitF.p + 2 * cap, sc->wfHitI.p, sc->wfHitI.p + cap};
+    wb.occluded = sc->wfOccluded.p;
+    wb.engine = sc->engine.p;
+    wb.engineCapacity = sc->engineCapacity;
     wb.contrib = sc->wfContrib.p; wb.visible = sc->wfVisible.p; wb.base = sc->wfBase.p; wb.accum = sc->wfAccum.p;
     wb.capacity = nrays;
     wb.lightCapacity = nl;
@@ -723,13 +746,13 @@ int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, in
     Query q {method, precision, tol};
     s->launches = 0;
     s->primaryRays = n; s->bounceRays = 0; s->shadowRays = 0;
-    cudaError_t e;
-    if (any_hit)
-        e = launch_any(s->dev(), r, n, q, hits->patch, s->work.p, s->counters.p, st);
-    else
-        e = launch_closest(s->dev(), r, n, q, HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object},
-                           s->work.p, s->counters.p, st);
-    s->launches = 1;
+    {
+        int er = ensure_engine(s, n);
+        if (er) return er;
+    }
+    cudaError_t e = run_query(s->dev(), r, n, nullptr, q, any_hit != 0,
+                              HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, hits->patch,
+                              s->engine.p, s->engineCapacity, kEnginePasses, s->counters.p, st, &s->launches);
     s->lastStream = st;
     return cuda_status(e);
 }

@@ -61,6 +61,7 @@ def lib():
                                  P, P, P, C.c_int, P]
         L.ora_render_rows.argtypes = [P, fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_float,
                                       C.c_int, C.c_float, P, P, P, C.c_int, P]
+        L.ora_intersect_stats.argtypes = [P, fp, C.c_uint64, C.c_int, C.c_float, C.c_int, u32, C.c_int]
         L.ora_camera_rays.argtypes = [fp, C.c_uint32, C.c_uint32, fp]
         L.ora_patch_intersect.argtypes = [fp, u32, fp, C.c_float, C.c_int, P, P, P]
         L.ora_patch_eval.argtypes = [fp, C.c_float, C.c_float, fp, fp]
@@ -145,6 +146,14 @@ class OracleScene:
             out["counters"] = dict(zip(["nodes", "leaves", "hash_lookups", "candidates", "clip_iterations",
                                         "pushes", "max_depth", "overflow"], [int(x) for x in cnt]))
         return out
+
+    def intersect_stats(self, rays, method=CLIP_HOST, tol=2.0 ** -12, any_hit=False, nthreads=None):
+        """Per-ray work: dict of (n,) arrays nodes, hash_lookups, candidates, iterations."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[1]
+        out = np.zeros((4, n), np.uint32)
+        lib().ora_intersect_stats(self.h, rays, n, method, tol, int(any_hit), out, nthreads or os.cpu_count() or 1)
+        return dict(nodes=out[0], hash_lookups=out[1], candidates=out[2], iterations=out[3])
 
     def render(self, camera, w, h, depth=1, eps=1e-4, method=CLIP_HOST, tol=2.0 ** -12, nthreads=None,
                want_rgb=True, want_packed=True):

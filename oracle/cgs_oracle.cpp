@@ -1557,6 +1557,25 @@ int ora_intersect(void* s_, const float* rays, uint64_t n, int method, int preci
     return 0;
 }
 
+// Per-ray work of a query (diagnostics): out (4, n) u32 = inner nodes,
+// hash lookups, candidates, search iterations.
+int ora_intersect_stats(void* s_, const float* rays, uint64_t n, int method, float tol, int any_hit, uint32_t* out,
+                        int nthreads)
+{
+    auto* s = static_cast<Scene*>(s_);
+    if (!s->built) return -1;
+    QueryOpts q; q.method = method; q.tol = tol;
+    parallel_for(n, nthreads, [&](uint64_t i, int) {
+        Ray<float> r; unpack_ray(rays, n, i, r);
+        Counters c;
+        if (any_hit) scene_occluded(*s, r, q, &c);
+        else { Hit hit; hit.t = r.max; scene_intersect(*s, hit, r, q, &c); }
+        out[i] = uint32_t(c.ts.nodes); out[n + i] = uint32_t(c.ts.hashLookups);
+        out[2 * n + i] = uint32_t(c.candidates); out[3 * n + i] = uint32_t(c.cs.iterations);
+    });
+    return 0;
+}
+
 // camera11 = rotation quaternion (x,y,z,w), position[3], scale[3], fovy
 // Renders w x h pixels (one primary ray each, non Monte-Carlo shading) with
 // 32x32 tiles handed to nthreads workers (src/rt/CPURayTracer.cpp:55-197).

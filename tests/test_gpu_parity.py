@@ -212,3 +212,20 @@ def test_device_frame_and_busy_flag(rt, c1_gpu, torch):
     assert not tracer.running()
     img = frame.rgba()
     assert img.shape == (60, 100, 4) and (img[..., 3] == 255).all()
+
+
+def test_long_runs_of_misses_do_not_end_the_query(c1_gpu, c1_oracle, oracle_mod, torch):
+    # 64K rays that miss (pointing up, away from the heightfield) before the hitting ones:
+    # persistent warps must keep fetching through them
+    hit_rays = oracle_mod.camera_rays(S.camera_c1(), 128, 128)
+    miss = hit_rays.copy()
+    miss = np.repeat(miss, 4, axis=1)
+    miss[5] = -miss[5]
+    rays = np.ascontiguousarray(np.concatenate([miss, hit_rays], axis=1))
+    o = c1_oracle.intersect(rays)
+    g = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda()))
+    assert (o["patch"][: miss.shape[1]] < 0).all()
+    compare_hits(g, o)
+    ga = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda(), any_hit=True))
+    oa = c1_oracle.intersect(rays, any_hit=True)
+    assert np.array_equal(ga["patch"] >= 0, oa["patch"] >= 0)
