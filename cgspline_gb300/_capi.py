@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libcgspline_gb300.so")
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "scene not built",
     5: "perfect hash bucket overflow", 6: "perfect hash failed", 7: "empty BVH leaf", 8: "render still in flight",
-    9: "device stack/iteration limit", 10: "admission refused", 11: "not found",
+    9: "device stack/iteration limit", 10: "admission refused", 11: "not found", 12: "exceeds fixed capacity",
 }
 
 
@@ -86,6 +86,7 @@ SIGNATURES = [
     ("cgs_render_running", C.c_int, [P]),
     ("cgs_scene_counters", C.c_int, [P, C.POINTER(Counters)]),
     ("cgs_perfect_hash_build", C.c_int, [P, U32, P, U32, P, U32, P, P]),
+    ("cgs_perfect_hash_build_noalloc", C.c_int, [P, U32, P, U32, P, U32, P, P]),
 ]
 
 

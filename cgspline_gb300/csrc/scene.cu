@@ -539,6 +539,7 @@ const char* cgs_status_string(int s)
     case CGS_ERR_DEVICE_LIMIT: return "a kernel hit a stack or iteration limit";
     case CGS_ERR_ADMISSION: return "request exceeds the device-memory budget";
     case CGS_ERR_NOT_FOUND: return "not found";
+    case CGS_ERR_CAPACITY: return "input exceeds the fixed capacity of this entry point";
     default: return "unknown status";
     }
 }

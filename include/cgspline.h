@@ -30,7 +30,8 @@ enum cgs_status {
     CGS_ERR_BUSY = 8,              /* a render is still in flight (reference: src/rt/RayTracer.cu:110-116 warns and returns) */
     CGS_ERR_DEVICE_LIMIT = 9,      /* a kernel hit a bounded loop or stack limit (reference: __trap, src/Spline_BezierClipping.cu:736-737) */
     CGS_ERR_ADMISSION = 10,        /* serving: request does not fit the HBM budget */
-    CGS_ERR_NOT_FOUND = 11
+    CGS_ERR_NOT_FOUND = 11,
+    CGS_ERR_CAPACITY = 12          /* input larger than a fixed-capacity entry point accepts */
 };
 
 const char* cgs_status_string(int status);
@@ -207,6 +208,24 @@ int cgs_scene_counters(cgs_scene* scene, cgs_counters* out);
  * least n + 15*max(4, 0.05n).  Synchronises `stream`. */
 int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t displ_capacity,
                            uint32_t* table, uint32_t table_capacity, uint32_t params[5], void* stream);
+
+/* cgs_perfect_hash_build without any device allocation.  This entry point
+ * has no counterpart in the reference.  It exists for callers that cannot
+ * allocate device memory when they need a table (for example while a stream
+ * is being captured into a CUDA graph, inside an allocator callback, or in a
+ * service that must not grow the device heap after start-up).  Its working
+ * memory is a fixed array inside the library (about 6.9 MB, held on every
+ * GPU that loads the library until the process exits), so n is limited to
+ * CGS_NOALLOC_MAX_KEYS; larger inputs return CGS_ERR_CAPACITY.  The caller
+ * still provides keys, disp and table (device) and params (host), exactly as
+ * for cgs_perfect_hash_build, and gets the same results.  The first call on
+ * a device resolves the array's address for that device; make it before any
+ * stream capture.  All calls on a device share the array: each call clears
+ * the parts that must start from zero, but calls that overlap on the GPU race
+ * and must be serialised by the caller.  Synchronises `stream`. */
+#define CGS_NOALLOC_MAX_KEYS 262144u
+int cgs_perfect_hash_build_noalloc(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t displ_capacity,
+                                   uint32_t* table, uint32_t table_capacity, uint32_t params[5], void* stream);
 
 #ifdef __cplusplus
 }
