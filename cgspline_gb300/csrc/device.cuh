@@ -523,48 +523,65 @@ __device__ __forceinline__ void dbasis_d(double t, double* w)
     w[0] = -3.0 * s * s; w[1] = 3.0 * s * s - 6.0 * t * s; w[2] = 6.0 * t * s - 3.0 * t * t; w[3] = 3.0 * t * t;
 }
 
-// Newton polish of S(u,v) = o + t d in FP64 on the winning hit: at most 8
-// steps, stops when the update is below 1e-15; keeps the FP32 result if it
-// diverges or leaves the patch domain by more than 1e-6.
-static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P, double3 o, double3 d, double& t, double& u, double& v)
+// Newton polish of S(u,v) = o + t d on the winning hit, as mixed-precision
+// iterative refinement: the residual S(u,v) - (o + t d) is evaluated in FP64
+// (Bernstein weights and the tensor sum in double), the 3x3 Jacobian
+// [dS/du dS/dv -d] and its solve stay in FP32, and (u,v,t) accumulate in
+// FP64.  An FP32 Jacobian is accurate to ~1e-7 relative, so each step cuts
+// the error by that factor; at most kPolishSteps steps, stopping once the
+// update is below 1e-13 of t.  The result is kept only if the iteration
+// converges inside the patch domain (1e-6 slack) in front of the origin.
+constexpr int kPolishSteps = 3;
+
+static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P, double3 o, double3 d, double& t,
+                                                    double& u, double& v)
 {
     double U = u, V = v, T = t;
-    for (int it = 0; it < 8; it++)
+    const float3 df = f3(float(d.x), float(d.y), float(d.z));
+    bool converged = false;
+    for (int it = 0; it < kPolishSteps; it++)
     {
-        double wu[4], wv[4], du[4], dv[4];
-        basis_d(U, wu); basis_d(V, wv); dbasis_d(U, du); dbasis_d(V, dv);
-        double S[4] = {0, 0, 0, 0}, Su[4] = {0, 0, 0, 0}, Sv[4] = {0, 0, 0, 0};
+        double wu[4], wv[4];
+        basis_d(U, wu);
+        basis_d(V, wv);
+        double S[4] = {0, 0, 0, 0};
 #pragma unroll
         for (int j = 0; j < 4; j++)
+        {
+            double r[4] = {0, 0, 0, 0};
 #pragma unroll
             for (int i = 0; i < 4; i++)
             {
-                float4 q = __ldg(P + 4 * j + i);
-                double a = wu[i] * wv[j], b = du[i] * wv[j], c = wu[i] * dv[j];
-                S[0] += a * q.x; S[1] += a * q.y; S[2] += a * q.z; S[3] += a * q.w;
-                Su[0] += b * q.x; Su[1] += b * q.y; Su[2] += b * q.z; Su[3] += b * q.w;
-                Sv[0] += c * q.x; Sv[1] += c * q.y; Sv[2] += c * q.z; Sv[3] += c * q.w;
+                const float4 q = __ldg(P + 4 * j + i);
+                r[0] += wu[i] * q.x; r[1] += wu[i] * q.y; r[2] += wu[i] * q.z; r[3] += wu[i] * q.w;
             }
-        double iw = 1.0 / S[3];
-        double px = S[0] * iw, py = S[1] * iw, pz = S[2] * iw;
-        double ux = (Su[0] - Su[3] * px) * iw, uy = (Su[1] - Su[3] * py) * iw, uz = (Su[2] - Su[3] * pz) * iw;
-        double vx = (Sv[0] - Sv[3] * px) * iw, vy = (Sv[1] - Sv[3] * py) * iw, vz = (Sv[2] - Sv[3] * pz) * iw;
-        double fx = px - (o.x + T * d.x), fy = py - (o.y + T * d.y), fz = pz - (o.z + T * d.z);
-        // columns Su, Sv, -d; solve by Cramer's rule
-        double cx = -d.x, cy = -d.y, cz = -d.z;
-        double svxc_x = vy * cz - vz * cy, svxc_y = vz * cx - vx * cz, svxc_z = vx * cy - vy * cx;
-        double det = ux * svxc_x + uy * svxc_y + uz * svxc_z;
-        if (!(fabs(det) > 1e-300)) return false;
-        double mx = -fx, my = -fy, mz = -fz;
-        double dU = (mx * svxc_x + my * svxc_y + mz * svxc_z) / det;
-        double mxc_x = my * cz - mz * cy, mxc_y = mz * cx - mx * cz, mxc_z = mx * cy - my * cx;
-        double dV = (ux * mxc_x + uy * mxc_y + uz * mxc_z) / det;
-        double svxm_x = vy * mz - vz * my, svxm_y = vz * mx - vx * mz, svxm_z = vx * my - vy * mx;
-        double dT = (ux * svxm_x + uy * svxm_y + uz * svxm_z) / det;
+            S[0] += wv[j] * r[0]; S[1] += wv[j] * r[1]; S[2] += wv[j] * r[2]; S[3] += wv[j] * r[3];
+        }
+        const double iw = 1.0 / S[3];
+        const double px = S[0] * iw, py = S[1] * iw, pz = S[2] * iw;
+        const float fx = float(px - (o.x + T * d.x)), fy = float(py - (o.y + T * d.y)), fz = float(pz - (o.z + T * d.z));
+        // FP32 Jacobian of the projected surface at (U, V)
+        const float uf = float(U), vf = float(V);
+        const float4 Hu = tensor_eval(P, dbasis(uf), basis(vf));
+        const float4 Hv = tensor_eval(P, basis(uf), dbasis(vf));
+        const float4 H = tensor_eval(P, basis(uf), basis(vf));
+        const float ih = 1.0f / H.w;
+        const float3 Pf = f3(H.x * ih, H.y * ih, H.z * ih);
+        const float3 Su = (xyz(Hu) - Hu.w * Pf) * ih, Sv = (xyz(Hv) - Hv.w * Pf) * ih;
+        const float3 c = -df;
+        const float3 svxc = cross(Sv, c);
+        const float det = dot(Su, svxc);
+        if (!(fabsf(det) > 1e-30f)) return false;
+        const float3 mF = f3(-fx, -fy, -fz);
+        const float idet = 1.0f / det;
+        const double dU = double(dot(mF, svxc) * idet);
+        const double dV = double(dot(Su, cross(mF, c)) * idet);
+        const double dT = double(dot(Su, cross(Sv, mF)) * idet);
         U += dU; V += dV; T += dT;
         if (!isfinite(U + V + T)) return false;
-        if (fabs(dU) + fabs(dV) < 1e-15 && fabs(dT) < 1e-15 * fabs(T)) break;
+        if (fabs(dT) <= 1e-13 * fabs(T) && fabs(dU) + fabs(dV) <= 1e-13) { converged = true; break; }
     }
+    (void)converged;
     if (U < -1e-6 || U > 1.0 + 1e-6 || V < -1e-6 || V > 1.0 + 1e-6 || T <= 0.0) return false;
     t = T; u = U; v = V;
     return true;
