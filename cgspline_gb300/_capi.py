@@ -44,7 +44,13 @@ class RenderOptions(C.Structure):
 
 
 class Rays(C.Structure):
-    _fields_ = [(k, C.c_void_p) for k in ("ox", "oy", "oz", "dx", "dy", "dz", "tmax")]
+    _fields_ = [(k, C.c_void_p) for k in ("ox", "oy", "oz", "dx", "dy", "dz", "tmax", "group")]
+
+
+class RenderRequest(C.Structure):
+    _fields_ = [("group", C.c_uint32), ("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("spp", C.c_uint32), ("recursion_depth", C.c_int), ("framebuffer", C.c_void_p),
+                ("linear_rgb", C.c_void_p)]
 
 
 class Hits(C.Structure):
@@ -68,6 +74,7 @@ SIGNATURES = [
     ("cgs_scene_create", C.c_int, [C.POINTER(P), C.c_int]),
     ("cgs_scene_destroy", C.c_int, [P]),
     ("cgs_scene_add_surface", C.c_int, [P, P, U32, P, U32, C.POINTER(U32)]),
+    ("cgs_scene_add_group", C.c_int, [P, C.POINTER(U32)]),
     ("cgs_scene_add_object", C.c_int, [P, U32, P, P, C.POINTER(Material), P, P, U32, C.POINTER(U32)]),
     ("cgs_scene_set_lights", C.c_int, [P, P, U32]),
     ("cgs_scene_set_environment", C.c_int, [P, P, P]),
@@ -83,6 +90,7 @@ SIGNATURES = [
     ("cgs_patch_intersect", C.c_int, [P, U32, C.POINTER(Rays), P, U32, C.c_int, C.c_float, C.POINTER(Hits), P]),
     ("cgs_render", C.c_int, [P, C.POINTER(Camera), U32, U32, C.POINTER(RenderOptions), P, U32, P, P]),
     ("cgs_render_host", C.c_int, [P, C.POINTER(Camera), U32, U32, C.POINTER(RenderOptions), P, P, P]),
+    ("cgs_render_batch", C.c_int, [P, C.POINTER(RenderRequest), U32, C.POINTER(RenderOptions), P]),
     ("cgs_render_running", C.c_int, [P]),
     ("cgs_scene_counters", C.c_int, [P, C.POINTER(Counters)]),
     ("cgs_perfect_hash_build", C.c_int, [P, U32, P, U32, P, U32, P, P]),

@@ -1,0 +1,383 @@
+// api.cu -- queries and rendering entry points of libcgspline_gb300.so:
+// closest / any-hit ray queries, (ray, patch) pair clipping, single and
+// batched frame renders, and the standalone perfect-hash build.
+#include "scene_impl.h"
+
+using namespace cgs;
+
+namespace cgs {
+
+void camera_setup(const cgs_camera& c, uint32_t w, uint32_t h, int flip, CameraSetup& s)
+{
+    // Transform::matrix() = T R S with the quaternion rotation of src/AlignedTypes.h:99-115
+    float i = c.rotation[0], j = c.rotation[1], k = c.rotation[2], r = c.rotation[3];
+    float ii = 2 * i * i, ij = 2 * i * j, ik = 2 * i * k, jj = 2 * j * j, jk = 2 * j * k, kk = 2 * k * k,
+          ri = 2 * r * i, rj = 2 * r * j, rk = 2 * r * k;
+    float c0[3] = {1 - jj - kk, ij + rk, ik - rj}, c1[3] = {ij - rk, 1 - ii - kk, jk + ri},
+          c2[3] = {ik + rj, jk - ri, 1 - ii - jj};
+    for (int q = 0; q < 3; q++)
+    {
+        s.c2w[q] = c0[q] * c.scale[0];
+        s.c2w[4 + q] = c1[q] * c.scale[1];
+        s.c2w[8 + q] = c2[q] * c.scale[2];
+        s.c2w[12 + q] = c.position[q];
+        s.pos[q] = c.position[q];
+    }
+    s.c2w[3] = s.c2w[7] = s.c2w[11] = 0.0f;
+    s.c2w[15] = 1.0f;
+    // src/rt/RayTracer.cu:152-163
+    float halfHeight = std::tan(0.5f * c.fovy);
+    s.half_dy = halfHeight / float(h);
+    s.half_dx = s.half_dy;
+    s.tl[0] = -s.half_dx * float(w - 1);
+    s.tl[1] = halfHeight - s.half_dy;
+    if (flip) { s.tl[1] = -s.tl[1]; s.half_dy = -s.half_dy; }
+}
+
+int ensure_engine(cgs_scene* sc, uint32_t capacity)
+{
+    if (sc->engineCapacity >= capacity) return CGS_OK;
+    CGS_TRY(sc->engine.reserve(engine_words(capacity, kEnginePasses)));
+    sc->engineCapacity = capacity;
+    return CGS_OK;
+}
+
+// Device bytes of a render slot for `samples` primary rays and `lights`
+// lights per group (the sizes RenderSlot::ensure reserves).
+uint64_t RenderSlot::bytes_for(uint32_t samples, uint32_t lights)
+{
+    const uint64_t c = samples, l = std::max<uint32_t>(lights, 1), s = c * l;
+    uint64_t b = 0;
+    b += 2 * 9 * c * 4;          // ray queues
+    b += 6 * c * 4;              // sample, group, depth of both queues
+    b += 5 * c * 4;              // hits
+    b += 6 * c * 4;              // base, accum
+    b += s * 4 * (1 + 7 + 2 + 3 + 1);  // occluded, shadow rays, slot+group, contrib, visible
+    b += engine_words(uint32_t(std::max<uint64_t>(c, s)), kEnginePasses) * 4;
+    return b;
+}
+
+int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
+{
+    const uint32_t nl = std::max<uint32_t>(lights, 1);
+    CGS_TRY(req.reserve(std::max<uint32_t>(nreq, 1)));
+    CGS_TRY(counters.reserve(1));
+    if (wb.capacity >= samples && wb.lightCapacity >= nl && wb.engine) return CGS_OK;
+    const size_t cap = std::max<uint32_t>(samples, wb.capacity);
+    const uint32_t lc = std::max<uint32_t>(nl, wb.lightCapacity);
+    const size_t sc = cap * lc;
+    if (sc >= (1ull << 31)) return CGS_ERR_INVALID_ARGUMENT;
+    CGS_TRY(ray0.reserve(9 * cap));
+    CGS_TRY(ray1.reserve(9 * cap));
+    CGS_TRY(smp0.reserve(cap)); CGS_TRY(smp1.reserve(cap));
+    CGS_TRY(grp0.reserve(cap)); CGS_TRY(grp1.reserve(cap));
+    CGS_TRY(dep0.reserve(cap)); CGS_TRY(dep1.reserve(cap));
+    CGS_TRY(count.reserve(8));
+    CGS_TRY(hitF.reserve(3 * cap));
+    CGS_TRY(hitI.reserve(2 * cap));
+    CGS_TRY(occluded.reserve(sc));
+    const uint32_t ecap = uint32_t(std::max(cap, sc));
+    if (engineCapacity < ecap)
+    {
+        CGS_TRY(engine.reserve(engine_words(ecap, kEnginePasses)));
+        engineCapacity = ecap;
+    }
+    CGS_TRY(shadow.reserve(7 * sc));
+    CGS_TRY(shadowSlot.reserve(sc));
+    CGS_TRY(shadowGroup.reserve(sc));
+    CGS_TRY(contrib.reserve(3 * sc));
+    CGS_TRY(visible.reserve(sc));
+    CGS_TRY(base.reserve(3 * cap));
+    CGS_TRY(accum.reserve(3 * cap));
+    wb.ray[0] = ray0.p; wb.ray[1] = ray1.p;
+    wb.sample[0] = smp0.p; wb.sample[1] = smp1.p;
+    wb.group[0] = grp0.p; wb.group[1] = grp1.p;
+    wb.depth[0] = dep0.p; wb.depth[1] = dep1.p;
+    wb.count = count.p;
+    wb.hit = HitsSoA {hitF.p, hitF.p + cap, hitF.p + 2 * cap, hitI.p, hitI.p + cap};
+    wb.occluded = occluded.p;
+    wb.engine = engine.p;
+    wb.engineCapacity = engineCapacity;
+    wb.shadow = shadow.p; wb.shadowGroup = shadowGroup.p; wb.shadowSlot = shadowSlot.p;
+    wb.contrib = contrib.p; wb.visible = visible.p; wb.base = base.p; wb.accum = accum.p;
+    wb.capacity = uint32_t(cap);
+    wb.lightCapacity = lc;
+    return CGS_OK;
+}
+
+void RenderSlot::release()
+{
+    ray0.release(); ray1.release(); shadow.release(); contrib.release(); base.release(); accum.release();
+    hitF.release();
+    for (auto* b : {&smp0, &smp1, &grp0, &grp1, &dep0, &dep1, &count, &shadowSlot, &shadowGroup, &engine}) b->release();
+    visible.release(); hitI.release(); occluded.release(); req.release(); counters.release();
+    wb = WavefrontBuffers {};
+    engineCapacity = 0;
+}
+
+int prepare_batch(cgs_scene* sc, const cgs_render_request* reqs, uint32_t n, const cgs_render_options* opt,
+                  std::vector<DevRequest>& host, RenderBatch& b)
+{
+    if (!reqs || n == 0 || !opt) return CGS_ERR_INVALID_ARGUMENT;
+    if (!valid_query(opt->method, opt->precision) || !(opt->tol > 0.0f) ||
+        (opt->schedule != CGS_SCHED_PLAIN && opt->schedule != CGS_SCHED_WAVEFRONT))
+        return CGS_ERR_INVALID_ARGUMENT;
+    host.resize(n);
+    uint64_t samples = 0, pixels = 0;
+    int maxDepth = 0;
+    for (uint32_t k = 0; k < n; k++)
+    {
+        const cgs_render_request& r = reqs[k];
+        if (r.width == 0 || r.height == 0 || r.spp == 0 || r.spp > 4096 || (!r.framebuffer && !r.linear_rgb))
+            return CGS_ERR_INVALID_ARGUMENT;
+        if (r.group >= sc->groups.size()) return CGS_ERR_INVALID_ARGUMENT;
+        const int depth = r.recursion_depth < 0 ? opt->recursion_depth : r.recursion_depth;
+        if (depth < 0 || depth > 64) return CGS_ERR_INVALID_ARGUMENT;
+        DevRequest& d = host[k];
+        camera_setup(r.camera, r.width, r.height, opt->flip_y, d.cam);
+        d.group = r.group; d.width = r.width; d.height = r.height; d.spp = r.spp; d.depth = depth;
+        d.sampleBase = uint32_t(samples); d.pixelBase = uint32_t(pixels); d.stride = r.width;
+        d.fb = r.framebuffer; d.linear = r.linear_rgb;
+        samples += uint64_t(r.width) * r.height * r.spp;
+        pixels += uint64_t(r.width) * r.height;
+        if (samples >= (1ull << 31)) return CGS_ERR_INVALID_ARGUMENT;
+        maxDepth = std::max(maxDepth, depth);
+    }
+    b = RenderBatch {};
+    b.nreq = n; b.samples = uint32_t(samples); b.pixels = uint32_t(pixels);
+    b.maxDepth = maxDepth; b.eps = opt->eps;
+    b.q = Query {opt->method, opt->precision, opt->tol};
+    return CGS_OK;
+}
+
+int run_batch(cgs_scene* sc, RenderSlot& slot, const std::vector<DevRequest>& host, RenderBatch& b, int schedule,
+              cudaStream_t stream, int* launches)
+{
+    CGS_TRY(slot.counters.reserve(1));
+    CGS_TRY(cudaMemsetAsync(slot.counters.p, 0, sizeof(Counters), stream));
+    cudaError_t e;
+    if (schedule == CGS_SCHED_PLAIN)
+        e = launch_render_plain(sc->dev(), b, host.data(), slot.counters.p, stream, launches);
+    else
+    {
+        int r = slot.ensure(b.samples, sc->maxLights(), b.nreq);
+        if (r) return r;
+        CGS_TRY(cudaMemcpyAsync(slot.req.p, host.data(), host.size() * sizeof(DevRequest), cudaMemcpyHostToDevice,
+                                stream));
+        b.req = slot.req.p;
+        e = launch_render_wavefront(sc->dev(), b, slot.wb, slot.counters.p, stream, launches);
+    }
+    return cuda_status(e);
+}
+
+}  // namespace cgs
+
+extern "C" {
+
+int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, int precision, float tol, int any_hit,
+                  const cgs_hits* hits, void* stream)
+{
+    if (!s || !rays || !hits || !valid_query(method, precision) || !(tol > 0.0f)) return CGS_ERR_INVALID_ARGUMENT;
+    if (!hits->patch || (!any_hit && (!hits->t || !hits->u || !hits->v || !hits->object)))
+        return CGS_ERR_INVALID_ARGUMENT;
+    if (n && (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz))
+        return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (!s->hashed) return CGS_ERR_NOT_BUILT;
+    if (n == 0) return CGS_OK;
+    CGS_TRY(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
+    RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, rays->group};
+    Query q {method, precision, tol};
+    s->launches = 0;
+    {
+        int er = ensure_engine(s, n);
+        if (er) return er;
+    }
+    cudaError_t e = run_query(s->dev(), r, n, nullptr, q, any_hit != 0,
+                              HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, hits->patch,
+                              s->engine.p, s->engineCapacity, kEnginePasses, s->counters.p, st, &s->launches);
+    s->lastStream = st;
+    s->lastCounters = s->counters.p;
+    return cuda_status(e);
+}
+
+int cgs_intersect_host(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, int precision, float tol,
+                       int any_hit, const cgs_hits* hits, void* stream)
+{
+    if (!s || !rays || !hits) return CGS_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CGS_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    cgs_rays dr {};
+    cgs_hits dh {};
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        CGS_TRY(cudaSetDevice(s->device));
+        CGS_TRY(s->rayStage.reserve(7ull * n));
+        CGS_TRY(s->hitF.reserve(3ull * n));
+        CGS_TRY(s->hitI.reserve(2ull * n));
+        const float* src[7] = {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax};
+        for (int k = 0; k < 7; k++)
+        {
+            if (!src[k]) { if (k == 6) continue; return CGS_ERR_INVALID_ARGUMENT; }
+            CGS_TRY(cudaMemcpyAsync(s->rayStage.p + size_t(k) * n, src[k], n * sizeof(float), cudaMemcpyHostToDevice, st));
+        }
+        float* R = s->rayStage.p;
+        dr = cgs_rays {R, R + n, R + 2ull * n, R + 3ull * n, R + 4ull * n, R + 5ull * n,
+                       rays->tmax ? R + 6ull * n : nullptr, nullptr};
+        if (rays->group)
+        {
+            CGS_TRY(s->groupStage.reserve(n));
+            CGS_TRY(cudaMemcpyAsync(s->groupStage.p, rays->group, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            dr.group = s->groupStage.p;
+        }
+        dh = cgs_hits {s->hitF.p, s->hitF.p + n, s->hitF.p + 2ull * n, s->hitI.p, s->hitI.p + n};
+    }
+    int r = cgs_intersect(s, &dr, n, method, precision, tol, any_hit, &dh, stream);
+    if (r) return r;
+    if (hits->patch) CGS_TRY(cudaMemcpyAsync(hits->patch, dh.patch, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    if (!any_hit)
+    {
+        if (hits->t) CGS_TRY(cudaMemcpyAsync(hits->t, dh.t, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (hits->u) CGS_TRY(cudaMemcpyAsync(hits->u, dh.u, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (hits->v) CGS_TRY(cudaMemcpyAsync(hits->v, dh.v, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (hits->object) CGS_TRY(cudaMemcpyAsync(hits->object, dh.object, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    }
+    CGS_TRY(cudaStreamSynchronize(st));
+    return CGS_OK;
+}
+
+int cgs_patch_intersect(cgs_scene* s, uint32_t surface, const cgs_rays* rays, const uint32_t* pids, uint32_t n,
+                        int method, float tol, const cgs_hits* hits, void* stream)
+{
+    if (!s || !rays || !pids || !hits || !hits->t || !hits->u || !hits->v || !hits->patch) return CGS_ERR_INVALID_ARGUMENT;
+    if (!valid_query(method, 0) || !(tol > 0.0f)) return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (!s->uploaded) return CGS_ERR_NOT_BUILT;
+    if (surface >= s->surfaces.size()) return CGS_ERR_INVALID_ARGUMENT;
+    CGS_TRY(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
+    RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, nullptr};
+    Query q {method, 0, tol};
+    s->launches = 1;
+    s->lastStream = st;
+    s->lastCounters = s->counters.p;
+    return cuda_status(launch_patch_pairs(s->dev(), surface, r, pids, n, q,
+                                          HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, s->counters.p,
+                                          st));
+}
+
+// RayTracer::render (src/rt/RayTracer.cu:107-180) for a batch of requests;
+// refuses while the previous batch of this scene is in flight, as the
+// reference's render refuses while its worker thread runs.
+int cgs_render_batch(cgs_scene* s, const cgs_render_request* reqs, uint32_t n, const cgs_render_options* opt,
+                     void* stream)
+{
+    if (!s) return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    std::vector<DevRequest> host;
+    RenderBatch b;
+    int r = prepare_batch(s, reqs, n, opt, host, b);
+    if (r) return r;
+    if (!s->hashed) return CGS_ERR_NOT_BUILT;
+    CGS_TRY(cudaSetDevice(s->device));
+    if (cudaEventQuery(s->finished) == cudaErrorNotReady) return CGS_ERR_BUSY;
+    cudaStream_t st = (cudaStream_t)stream;
+    s->launches = 0;
+    r = run_batch(s, s->slot, host, b, opt->schedule, st, &s->launches);
+    if (r) return r;
+    CGS_TRY(cudaEventRecord(s->finished, st));
+    s->lastStream = st;
+    s->lastCounters = s->slot.counters.p;
+    return CGS_OK;
+}
+
+int cgs_render(cgs_scene* s, const cgs_camera* cam, uint32_t w, uint32_t h, const cgs_render_options* opt,
+               uint32_t* fb, uint32_t stride, float* linear, void* stream)
+{
+    if (!s || !cam || !opt || w == 0 || h == 0 || (!fb && !linear) || (fb && stride < w)) return CGS_ERR_INVALID_ARGUMENT;
+    if (opt->recursion_depth < 0 || opt->recursion_depth > 64) return CGS_ERR_INVALID_ARGUMENT;
+    cgs_render_request req {};
+    req.group = 0;
+    req.camera = *cam;
+    req.width = w; req.height = h; req.spp = 1;
+    req.recursion_depth = opt->recursion_depth;
+    req.framebuffer = fb; req.linear_rgb = linear;
+    std::lock_guard<std::mutex> g(s->mu);
+    std::vector<DevRequest> host;
+    RenderBatch b;
+    int r = prepare_batch(s, &req, 1, opt, host, b);
+    if (r) return r;
+    host[0].stride = fb ? stride : w;
+    if (!s->hashed) return CGS_ERR_NOT_BUILT;
+    CGS_TRY(cudaSetDevice(s->device));
+    if (cudaEventQuery(s->finished) == cudaErrorNotReady) return CGS_ERR_BUSY;
+    cudaStream_t st = (cudaStream_t)stream;
+    s->launches = 0;
+    r = run_batch(s, s->slot, host, b, opt->schedule, st, &s->launches);
+    if (r) return r;
+    CGS_TRY(cudaEventRecord(s->finished, st));
+    s->lastStream = st;
+    s->lastCounters = s->slot.counters.p;
+    return CGS_OK;
+}
+
+int cgs_render_host(cgs_scene* s, const cgs_camera* cam, uint32_t w, uint32_t h, const cgs_render_options* opt,
+                    uint32_t* fb, float* linear, void* stream)
+{
+    if (!s || (!fb && !linear) || w == 0 || h == 0) return CGS_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        CGS_TRY(cudaSetDevice(s->device));
+        if (cudaEventQuery(s->finished) == cudaErrorNotReady) return CGS_ERR_BUSY;
+        if (fb) CGS_TRY(s->fbStage.reserve(size_t(w) * h));
+        if (linear) CGS_TRY(s->linStage.reserve(3ull * w * h));
+    }
+    int r = cgs_render(s, cam, w, h, opt, fb ? s->fbStage.p : nullptr, w, linear ? s->linStage.p : nullptr, stream);
+    if (r) return r;
+    if (fb) CGS_TRY(cudaMemcpyAsync(fb, s->fbStage.p, size_t(w) * h * 4, cudaMemcpyDeviceToHost, st));
+    if (linear) CGS_TRY(cudaMemcpyAsync(linear, s->linStage.p, 12ull * w * h, cudaMemcpyDeviceToHost, st));
+    CGS_TRY(cudaStreamSynchronize(st));
+    return CGS_OK;
+}
+
+int cgs_render_running(cgs_scene* s)
+{
+    if (!s) return 0;
+    return cudaEventQuery(s->finished) == cudaErrorNotReady ? 1 : 0;
+}
+
+int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t dcap, uint32_t* table,
+                           uint32_t tcap, uint32_t params[5], void* stream)
+{
+    if (!keys || !disp || !table || !params || n == 0) return CGS_ERR_INVALID_ARGUMENT;
+    if (dcap < displ_size(n) || tcap < table_capacity(n)) return CGS_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t w32 = 0, w64 = 0;
+    hash_scratch_words(n, w32, w64);
+    uint32_t* s32 = nullptr;
+    unsigned long long* s64 = nullptr;
+    CGS_TRY(cudaMallocAsync(&s32, w32 * sizeof(uint32_t), st));
+    if (cudaMallocAsync(&s64, w64 * sizeof(unsigned long long), st) != cudaSuccess)
+    {
+        cudaFreeAsync(s32, st);
+        return CGS_ERR_OUT_OF_MEMORY;
+    }
+    HashScratch hs {};
+    hash_scratch_carve(hs, n, s32, s64);
+    uint32_t A[16], B[16];
+    hash_coefficients(n, A, B);
+    int r = hash_build_device(keys, n, A, B, disp, table, tcap, hs, params, st, nullptr);
+    cudaFreeAsync(s32, st);
+    cudaFreeAsync(s64, st);
+    cudaStreamSynchronize(st);
+    if (r == 4) return CGS_ERR_HASH_BUCKET_OVERFLOW;
+    if (r < 0) return CGS_ERR_CUDA;
+    if (r) return CGS_ERR_HASH_FAILED;
+    return CGS_OK;
+}
+
+}  // extern "C"

@@ -18,7 +18,7 @@ constexpr float kPi = 3.14159265358979323846f;
 constexpr float kInvPi = 0.318309886183790671538f;
 
 // Error bits reported through Counters::errors.
-enum : uint32_t { kErrClipStack = 1u, kErrClipIterations = 2u, kErrTraversal = 4u };
+enum : uint32_t { kErrClipStack = 1u, kErrClipIterations = 2u, kErrTraversal = 4u, kErrGroup = 8u };
 
 // ------------------------------------------------------------ data layout --
 // One BVH (a surface's patch BVH or the object-level BVH).  Node offsets in
@@ -74,9 +74,25 @@ struct DevScene
     const DevMaterial* materials;
     const uint32_t* patchMaterial;
     const DevLight* lights;
-    uint32_t nobjects, nlights, nsurfaces, topBVH;
-    float background[3], ambient[3];
+    // Groups: independent scenes that share the store.  Group g has its own
+    // object-level BVH bvhs[groupTop[g]], lights lights[groupLights[g].x ..
+    // + groupLights[g].y) and background / ambient colours groupEnv[6g..6g+5].
+    const uint32_t* groupTop;
+    const uint2* groupLights;
+    const float* groupEnv;
+    uint32_t nobjects, nsurfaces, ngroups;
 };
+
+__device__ __forceinline__ float3 group_background(const DevScene& S, uint32_t g)
+{
+    const float* e = S.groupEnv + 6ull * g;
+    return make_float3(__ldg(e), __ldg(e + 1), __ldg(e + 2));
+}
+__device__ __forceinline__ float3 group_ambient(const DevScene& S, uint32_t g)
+{
+    const float* e = S.groupEnv + 6ull * g;
+    return make_float3(__ldg(e + 3), __ldg(e + 4), __ldg(e + 5));
+}
 
 struct Counters
 {
@@ -732,8 +748,8 @@ __device__ __forceinline__ void polish_hit(const DevScene& S, float3 o, float3 d
 // Closest hit over the object-level BVH and each object's patch BVH
 // (Context::intersect, src/rt/RayTracer.cu:295-349; rt::intersect,
 // src/rt/Primitive.cu:222-248).  hit.t must hold ray.max on entry.
-__device__ __forceinline__ int scene_closest(const DevScene& S, float3 o, float3 d, float tmax, const Query& q,
-                                             HitRecord& hit, LocalCounters& lc)
+__device__ __forceinline__ int scene_closest(const DevScene& S, uint32_t group, float3 o, float3 d, float tmax,
+                                             const Query& q, HitRecord& hit, LocalCounters& lc)
 {
     int nearest = -1;
     float limit = tmax;
@@ -764,15 +780,15 @@ __device__ __forceinline__ int scene_closest(const DevScene& S, float3 o, float3
         }
         return false;
     };
-    hash_traverse<false>(S, S.bvhs[S.topBVH], o, inv, limit, objfn, lc);
+    hash_traverse<false>(S, S.bvhs[S.groupTop[group]], o, inv, limit, objfn, lc);
     if (nearest >= 0 && q.precision == 1) polish_hit(S, o, d, hit);
     return nearest;
 }
 
 // Any hit (Context::intersect(const Ray&), src/rt/RayTracer.cu:351-383;
 // rt::intersect(const BezierSurface&, const Ray&), src/rt/Primitive.cu:250-268).
-__device__ __forceinline__ bool scene_any(const DevScene& S, float3 o, float3 d, float tmax, const Query& q,
-                                          LocalCounters& lc)
+__device__ __forceinline__ bool scene_any(const DevScene& S, uint32_t group, float3 o, float3 d, float tmax,
+                                          const Query& q, LocalCounters& lc)
 {
     float limit = tmax;
     const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
@@ -789,7 +805,7 @@ __device__ __forceinline__ bool scene_any(const DevScene& S, float3 o, float3 d,
         };
         return hash_traverse<true>(S, S.bvhs[ob.surface], lo, linv, llimit, leaf, lc);
     };
-    return hash_traverse<true>(S, S.bvhs[S.topBVH], o, inv, limit, objfn, lc);
+    return hash_traverse<true>(S, S.bvhs[S.groupTop[group]], o, inv, limit, objfn, lc);
 }
 
 // --------------------------------------------------------------- shading --

@@ -112,8 +112,8 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
     uint32_t node = 0, key = 1, post = 0, leaf = EMPTY, tnode = 0, tkey = 1, tpost = 0, tleaf = EMPTY;
     float leafEntry = -INFINITY;
     int32_t obj = -1;
-    const DevBVH topB = S.bvhs[S.topBVH];
-    DevBVH B = topB;
+    uint32_t topIdx = 0;  // the ray's object-level BVH (its group's)
+    DevBVH B {};
     uint32_t nrays = 0;
     uint2* list = nullptr;
     for (;;)
@@ -124,20 +124,29 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         {
             if (idx >= n)
                 exhausted = true;
+            else if (pass == 0 && rays.group && __ldg(rays.group + idx) >= S.ngroups)
+            {
+                // a group outside the store: the ray stays a miss and raises an error bit
+                lc.errors |= kErrGroup;
+                E.count[idx] = 0;
+                E.status[idx] = kTraversed;
+            }
             else if (pass == 0 || E.status[idx] == kPending)
             {
                 rid = idx;
+                const uint32_t g = rays.group ? __ldg(rays.group + rid) : 0u;
                 active = true;
                 float3 d;
                 load_ray(rays, rid, o, d, tmax);
                 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
                 list = E.list + size_t(rid) * kChunk;
                 ncand = 0;
+                topIdx = __ldg(S.groupTop + g);
                 if (pass == 0)
                 {
                     node = 0; key = 1; post = 0; leaf = EMPTY; obj = -1; jumped = false;
                     leafEntry = -INFINITY; limit = tmax;
-                    B = topB;
+                    B = S.bvhs[topIdx];
                     nrays++;
                 }
                 else
@@ -145,7 +154,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     node = E.node[rid]; key = E.key[rid]; post = E.post[rid]; leaf = E.leaf[rid];
                     jumped = E.jumped[rid] != 0; leafEntry = E.leafEntry[rid]; obj = E.obj[rid];
                     limit = kAny ? tmax : E.limit[rid];
-                    B = topB;
+                    B = S.bvhs[topIdx];
                     if (obj >= 0)
                     {
                         tnode = E.tnode[rid]; tkey = E.tkey[rid]; tpost = E.tpost[rid]; tleaf = E.tleaf[rid];
@@ -257,7 +266,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 {
                     list[ncand++] = make_uint2(kLeave, uint32_t(obj));
                     obj = -1;
-                    B = topB;
+                    B = S.bvhs[topIdx];
                     node = tnode; key = tkey; post = tpost; leaf = tleaf;
                     leafEntry = -INFINITY;
                 }
@@ -423,12 +432,14 @@ __global__ void __launch_bounds__(128) k_rest(DevScene S, RaysSoA rays, uint32_t
         load_ray(rays, rid, o, d, tmax);
         Query q32 = q;
         q32.precision = 0;  // the polish kernel runs afterwards
+        const uint32_t g = rays.group ? rays.group[rid] : 0u;
+        if (g >= S.ngroups) continue;
         if (kAny)
-            occluded[rid] = scene_any(S, o, d, tmax, q32, lc) ? 0 : -1;
+            occluded[rid] = scene_any(S, g, o, d, tmax, q32, lc) ? 0 : -1;
         else
         {
             HitRecord h {tmax, 0.0f, 0.0f, -1, -1};
-            int ob = scene_closest(S, o, d, tmax, q32, h, lc);
+            int ob = scene_closest(S, g, o, d, tmax, q32, h, lc);
             hits.t[rid] = ob >= 0 ? h.t : tmax; hits.u[rid] = h.u; hits.v[rid] = h.v;
             hits.patch[rid] = ob >= 0 ? h.patch : -1; hits.object[rid] = ob;
         }

@@ -1,12 +1,17 @@
-// k_render.cu -- rendering: camera rays, PBR shading with shadow rays and
-// mirror bounces, sRGB packing.  Two schedules:
-//   plain     -- one thread per pixel runs the whole bounce chain, 8x8 blocks
-//                (the reference's launch shape, src/rt/RayTracer.cu:171-274);
-//   wavefront -- a closest-hit pass, a shading pass that queues shadow and
-//                bounce rays, an any-hit pass over the shadow queue and a
-//                resolve pass, per bounce level; persistent grid-stride kernels
-//                read queue sizes from device memory, so a frame needs no
-//                host round trip.
+// k_render.cu -- rendering a batch of requests: camera rays, PBR shading with
+// shadow rays and mirror bounces, sRGB packing (RayTracer::render and
+// Context::closestHit, src/rt/RayTracer.cu:107-544, non Monte-Carlo path).
+// A request is (group, camera, width, height, spp, depth); with spp > 1 the
+// primary rays of sample s are jittered by (s/spp, vdc(s)) as the reference's
+// sampled path does (src/rt/RayTracer.cu:226-236) and the samples are
+// averaged.  Two schedules:
+//   plain     -- one thread per pixel runs all of its samples and the whole
+//                bounce chain, 8x8 blocks, one launch per request (the
+//                reference's launch shape, src/rt/RayTracer.cu:171-274);
+//   wavefront -- all requests' samples together: a closest-hit query, a
+//                shading pass that queues shadow and bounce rays, an any-hit
+//                query over the shadow queue and a resolve pass per bounce
+//                level; queue sizes stay on the device.
 #include "kernels.h"
 
 namespace cgs {
@@ -14,6 +19,11 @@ namespace cgs {
 namespace {
 
 constexpr float kMinRadiance = 0x1p-8f;  // src/rt/RayTracer.h:16
+
+__device__ __forceinline__ float vdc(uint32_t i)  // Van der Corput, src/rt/PBR.h:143-157
+{
+    return 0x1p-32f * float(__brev(i));
+}
 
 __device__ __forceinline__ float3 pixel_dir(const CameraSetup& c, float x, float y)  // src/rt/RayTracer.cu:59-71
 {
@@ -76,53 +86,81 @@ __device__ __forceinline__ bool bounce(const Frame& f, float3 att, float3& R, fl
     return vmax3(a) > kMinRadiance;
 }
 
-__device__ __forceinline__ void store_pixel(const RenderParams& p, uint32_t px, float3 c, uint32_t* fb, float* linear)
+__device__ __forceinline__ void store_pixel(const DevRequest& r, uint32_t px, float3 c)
 {
     c = f3(__saturatef(c.x), __saturatef(c.y), __saturatef(c.z));
-    uint32_t i = px % p.width, j = px / p.width;
-    if (fb) fb[size_t(j) * p.stride + i] = pack_srgb(c);
-    if (linear) { linear[3ull * px] = c.x; linear[3ull * px + 1] = c.y; linear[3ull * px + 2] = c.z; }
+    const uint32_t i = px % r.width, j = px / r.width;
+    if (r.fb) r.fb[size_t(j) * r.stride + i] = pack_srgb(c);
+    if (r.linear) { r.linear[3ull * px] = c.x; r.linear[3ull * px + 1] = c.y; r.linear[3ull * px + 2] = c.z; }
+}
+
+__device__ __forceinline__ float2 sample_xy(const DevRequest& r, uint32_t pixel, uint32_t s)
+{
+    const float x = float(pixel % r.width), y = float(pixel / r.width);
+    if (r.spp <= 1) return make_float2(x, y);
+    return make_float2(x + float(s) * (1.0f / float(r.spp)), y + vdc(s));
+}
+
+// Request owning global index k, by binary search over the bases (field 0: samples, 1: pixels).
+__device__ __forceinline__ uint32_t find_request(const DevRequest* req, uint32_t n, uint32_t k, bool pixels)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t b = pixels ? req[mid].pixelBase : req[mid].sampleBase;
+        if (b <= k) lo = mid; else hi = mid;
+    }
+    return lo;
 }
 
 // ------------------------------------------------------------- plain --
-__global__ void __launch_bounds__(64) k_render_plain(DevScene S, RenderParams p, uint32_t* fb, float* linear,
-                                                     Counters* cnt)
+__global__ void __launch_bounds__(64) k_render_plain(DevScene S, DevRequest r, float eps, Query q, Counters* cnt)
 {
     const uint32_t i = blockIdx.x * 8 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
     LocalCounters lc;
     uint32_t nrays = 0;
-    if (i < p.width && j < p.height)
+    if (i < r.width && j < r.height)
     {
-        float3 o = f3(p.cam.pos[0], p.cam.pos[1], p.cam.pos[2]);
-        float3 d = pixel_dir(p.cam, float(i), float(j));
-        float3 color = f3(0.0f, 0.0f, 0.0f), att = f3(1.0f, 1.0f, 1.0f);
-        int depth = p.depth;
-        for (int level = 0; level <= p.depth; level++)
+        const uint32_t g = r.group;
+        const uint2 lights = S.groupLights[g];
+        float3 pixel = f3(0.0f, 0.0f, 0.0f);
+        for (uint32_t s = 0; s < r.spp; s++)
         {
-            nrays++;
-            HitRecord hit {INFINITY, 0.0f, 0.0f, -1, -1};
-            int ob = scene_closest(S, o, d, INFINITY, p.q, hit, lc);
-            if (ob < 0) { color = color + f3(S.background[0], S.background[1], S.background[2]) * att; break; }
-            Frame f = shade_frame(S, o, d, hit);
-            float3 c = f3(S.ambient[0], S.ambient[1], S.ambient[2]) * f.diffuse;
-            for (uint32_t l = 0; l < S.nlights; l++)
+            const float2 xy = sample_xy(r, j * r.width + i, s);
+            float3 o = f3(r.cam.pos[0], r.cam.pos[1], r.cam.pos[2]);
+            float3 d = pixel_dir(r.cam, xy.x, xy.y);
+            float3 color = f3(0.0f, 0.0f, 0.0f), att = f3(1.0f, 1.0f, 1.0f);
+            int depth = r.depth;
+            for (int level = 0; level <= r.depth; level++)
             {
-                float3 contrib, L; float dist;
-                if (!light_term(f, S.lights[l], contrib, L, dist)) continue;
                 nrays++;
-                if (scene_any(S, f.P + p.eps * L, L, dist, p.q, lc)) continue;
-                c = c + contrib;
+                HitRecord hit {INFINITY, 0.0f, 0.0f, -1, -1};
+                int ob = scene_closest(S, g, o, d, INFINITY, q, hit, lc);
+                if (ob < 0) { color = color + group_background(S, g) * att; break; }
+                Frame f = shade_frame(S, o, d, hit);
+                float3 c = group_ambient(S, g) * f.diffuse;
+                for (uint32_t l = 0; l < lights.y; l++)
+                {
+                    float3 contrib, L; float dist;
+                    if (!light_term(f, S.lights[lights.x + l], contrib, L, dist)) continue;
+                    nrays++;
+                    if (scene_any(S, g, f.P + eps * L, L, dist, q, lc)) continue;
+                    c = c + contrib;
+                }
+                color = color + (c * kPi) * att;
+                if (depth <= 0) break;
+                float3 R, a;
+                if (!bounce(f, att, R, a)) break;
+                o = f.P + eps * R;
+                d = R;
+                att = a;
+                depth--;
             }
-            color = color + (c * kPi) * att;
-            if (depth <= 0) break;
-            float3 R, a;
-            if (!bounce(f, att, R, a)) break;
-            o = f.P + p.eps * R;
-            d = R;
-            att = a;
-            depth--;
+            pixel = pixel + color;
         }
-        store_pixel(p, j * p.width + i, color, fb, linear);
+        if (r.spp > 1) pixel = pixel * (1.0f / float(r.spp));
+        store_pixel(r, j * r.width + i, pixel);
     }
     flush_counters(cnt, lc, nrays);
 }
@@ -130,16 +168,16 @@ __global__ void __launch_bounds__(64) k_render_plain(DevScene S, RenderParams p,
 // --------------------------------------------------------- wavefront --
 constexpr int kWfThreads = 128;
 
-// queue layout: 9 floats per ray (SoA with stride = capacity)
-struct Q
+struct Q  // a ray queue: 9 floats per ray (SoA with stride = capacity) + sample, group, depth
 {
-    float* r; uint32_t* px; uint32_t cap;
-    __device__ __forceinline__ void put(uint32_t k, float3 o, float3 d, float3 a, uint32_t pixel) const
+    float* r; uint32_t* sample; uint32_t* group; uint32_t* depth; uint32_t cap;
+    __device__ __forceinline__ void put(uint32_t k, float3 o, float3 d, float3 a, uint32_t smp, uint32_t g,
+                                        uint32_t dep) const
     {
         r[k] = o.x; r[cap + k] = o.y; r[2ull * cap + k] = o.z;
         r[3ull * cap + k] = d.x; r[4ull * cap + k] = d.y; r[5ull * cap + k] = d.z;
         r[6ull * cap + k] = a.x; r[7ull * cap + k] = a.y; r[8ull * cap + k] = a.z;
-        px[k] = pixel;
+        sample[k] = smp; group[k] = g; depth[k] = dep;
     }
     __device__ __forceinline__ void get(uint32_t k, float3& o, float3& d) const
     {
@@ -150,78 +188,91 @@ struct Q
     {
         return f3(r[6ull * cap + k], r[7ull * cap + k], r[8ull * cap + k]);
     }
+    RaysSoA rays() const
+    {
+        return RaysSoA {r, r + cap, r + 2ull * cap, r + 3ull * cap, r + 4ull * cap, r + 5ull * cap, nullptr, group};
+    }
 };
 
-__global__ void k_wf_camera(RenderParams p, Q q, float* accum, uint32_t* count)
+__global__ void k_wf_camera(RenderBatch b, Q q, float* accum, uint32_t* count)
 {
-    const uint32_t n = p.width * p.height;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < b.samples; k += gridDim.x * blockDim.x)
     {
-        uint32_t i = k % p.width, j = k / p.width;
-        float3 o = f3(p.cam.pos[0], p.cam.pos[1], p.cam.pos[2]);
-        q.put(k, o, pixel_dir(p.cam, float(i), float(j)), f3(1.0f, 1.0f, 1.0f), k);
+        const DevRequest& r = b.req[find_request(b.req, b.nreq, k, false)];
+        const uint32_t local = k - r.sampleBase, pixel = local / r.spp, s = local % r.spp;
+        const float2 xy = sample_xy(r, pixel, s);
+        const float3 o = f3(r.cam.pos[0], r.cam.pos[1], r.cam.pos[2]);
+        q.put(k, o, pixel_dir(r.cam, xy.x, xy.y), f3(1.0f, 1.0f, 1.0f), k, r.group, uint32_t(r.depth));
         accum[3ull * k] = 0.0f; accum[3ull * k + 1] = 0.0f; accum[3ull * k + 2] = 0.0f;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) { count[0] = n; count[1] = 0; count[2] = 0; }
+    if (blockIdx.x == 0 && threadIdx.x == 0) { count[0] = b.samples; count[1] = 0; count[2] = 0; }
 }
 
-__global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, RenderParams p, Q q, Q qn, const uint32_t* count,
+__global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, float eps, Q q, Q qn, const uint32_t* count,
                                                          uint32_t* nextCount, uint32_t* shadowCount, HitsSoA hits,
-                                                         float* shadow, uint32_t* shadowSlot, uint32_t shadowCap,
-                                                         float* contrib, int32_t* visible, float* base, float* accum,
-                                                         int depthLeft)
+                                                         float* shadow, uint32_t* shadowGroup, uint32_t* shadowSlot,
+                                                         uint32_t shadowCap, uint32_t lcap, float* contrib,
+                                                         int32_t* visible, float* base, float* accum)
 {
     const uint32_t n = *count;
-    const uint32_t nl = S.nlights;
     for (uint32_t k0 = blockIdx.x * blockDim.x; k0 < n; k0 += gridDim.x * blockDim.x)
     {
         const uint32_t k = k0 + threadIdx.x;
         const bool live = k < n;
         HitRecord h {INFINITY, 0.0f, 0.0f, -1, -1};
         float3 o = f3(0, 0, 0), d = f3(0, 0, 1), att = f3(0, 0, 0);
-        uint32_t pixel = 0;
+        uint32_t smp = 0, g = 0, dep = 0;
         if (live)
         {
             h = HitRecord {hits.t[k], hits.u[k], hits.v[k], hits.patch[k], hits.object[k]};
-            q.get(k, o, d); att = q.att(k); pixel = q.px[k];
+            q.get(k, o, d);
+            att = q.att(k);
+            smp = q.sample[k]; g = q.group[k]; dep = q.depth[k];
         }
         const bool isHit = live && h.object >= 0;
         if (live && !isHit)
         {
-            float3 bg = f3(S.background[0], S.background[1], S.background[2]) * att;
-            accum[3ull * pixel] += bg.x; accum[3ull * pixel + 1] += bg.y; accum[3ull * pixel + 2] += bg.z;
+            const float3 bg = group_background(S, g) * att;
+            accum[3ull * smp] += bg.x; accum[3ull * smp + 1] += bg.y; accum[3ull * smp + 2] += bg.z;
         }
         Frame f;
+        uint2 lights = make_uint2(0, 0);
         if (isHit)
         {
             f = shade_frame(S, o, d, h);
-            float3 c0 = f3(S.ambient[0], S.ambient[1], S.ambient[2]) * f.diffuse;
+            const float3 c0 = group_ambient(S, g) * f.diffuse;
             base[3ull * k] = c0.x; base[3ull * k + 1] = c0.y; base[3ull * k + 2] = c0.z;
+            lights = S.groupLights[g];
         }
+        // the warp walks the largest light count among its lanes (pushes are warp-wide)
+        uint32_t nl = lights.y;
+        for (int off = 16; off > 0; off >>= 1) nl = max(nl, __shfl_xor_sync(0xFFFFFFFFu, nl, off));
         for (uint32_t l = 0; l < nl; l++)
         {
             float3 c, L; float dist = 0.0f;
-            bool want = isHit && light_term(f, S.lights[l], c, L, dist);
-            uint32_t slot = k * nl + l;
-            if (isHit)
+            const bool mine = isHit && l < lights.y;
+            const bool want = mine && light_term(f, S.lights[lights.x + l], c, L, dist);
+            const uint32_t slot = k * lcap + l;
+            if (mine)
             {
                 visible[slot] = 0;
                 if (want) { contrib[3ull * slot] = c.x; contrib[3ull * slot + 1] = c.y; contrib[3ull * slot + 2] = c.z; }
             }
-            uint32_t sk = warp_push(shadowCount, want);
+            const uint32_t sk = warp_push(shadowCount, want);
             if (want && sk < shadowCap)
             {
-                float3 so = f.P + p.eps * L;
+                const float3 so = f.P + eps * L;
                 shadow[sk] = so.x; shadow[shadowCap + sk] = so.y; shadow[2ull * shadowCap + sk] = so.z;
                 shadow[3ull * shadowCap + sk] = L.x; shadow[4ull * shadowCap + sk] = L.y;
                 shadow[5ull * shadowCap + sk] = L.z; shadow[6ull * shadowCap + sk] = dist;
+                shadowGroup[sk] = g;
                 shadowSlot[sk] = slot;
             }
         }
         float3 R = f3(0, 0, 0), a = f3(0, 0, 0);
-        bool more = isHit && depthLeft > 0 && bounce(f, att, R, a);
-        uint32_t nk = warp_push(nextCount, more);
-        if (more) qn.put(nk, f.P + p.eps * R, R, a, pixel);
+        const bool more = isHit && dep > 0 && bounce(f, att, R, a);
+        const uint32_t nk = warp_push(nextCount, more);
+        if (more) qn.put(nk, f.P + eps * R, R, a, smp, g, dep - 1);
     }
 }
 
@@ -234,30 +285,38 @@ __global__ void k_wf_visibility(const int32_t* occluded, const uint32_t* shadowS
 }
 
 __global__ void k_wf_resolve(DevScene S, Q q, const uint32_t* count, HitsSoA hits, const float* contrib,
-                             const int32_t* visible, const float* base, float* accum)
+                             const int32_t* visible, const float* base, uint32_t lcap, float* accum)
 {
-    const uint32_t n = *count, nl = S.nlights;
+    const uint32_t n = *count;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
     {
         if (hits.object[k] < 0) continue;
+        const uint2 lights = S.groupLights[q.group[k]];
         float3 c = f3(base[3ull * k], base[3ull * k + 1], base[3ull * k + 2]);
-        for (uint32_t l = 0; l < nl; l++)
+        for (uint32_t l = 0; l < lights.y; l++)
         {
-            uint32_t slot = k * nl + l;
+            const uint32_t slot = k * lcap + l;
             if (visible[slot]) c = c + f3(contrib[3ull * slot], contrib[3ull * slot + 1], contrib[3ull * slot + 2]);
         }
-        float3 a = q.att(k);
-        uint32_t px = q.px[k];
-        float3 add = (c * kPi) * a;
-        accum[3ull * px] += add.x; accum[3ull * px + 1] += add.y; accum[3ull * px + 2] += add.z;
+        const float3 add = (c * kPi) * q.att(k);
+        const uint32_t smp = q.sample[k];
+        accum[3ull * smp] += add.x; accum[3ull * smp + 1] += add.y; accum[3ull * smp + 2] += add.z;
     }
 }
 
-__global__ void k_wf_finish(RenderParams p, const float* accum, uint32_t* fb, float* linear)
+__global__ void k_wf_finish(RenderBatch b, const float* accum)
 {
-    const uint32_t n = p.width * p.height;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        store_pixel(p, k, f3(accum[3ull * k], accum[3ull * k + 1], accum[3ull * k + 2]), fb, linear);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < b.pixels; p += gridDim.x * blockDim.x)
+    {
+        const DevRequest& r = b.req[find_request(b.req, b.nreq, p, true)];
+        const uint32_t local = p - r.pixelBase;
+        const size_t s0 = size_t(r.sampleBase) + size_t(local) * r.spp;
+        float3 c = f3(0.0f, 0.0f, 0.0f);
+        for (uint32_t s = 0; s < r.spp; s++)
+            c = c + f3(accum[3 * (s0 + s)], accum[3 * (s0 + s) + 1], accum[3 * (s0 + s) + 2]);
+        if (r.spp > 1) c = c * (1.0f / float(r.spp));
+        store_pixel(r, local, c);
+    }
 }
 
 int sm_count()
@@ -281,54 +340,59 @@ int blocks_for(const void* fn, int threads)
 
 }  // namespace
 
-cudaError_t launch_render_plain(const DevScene& S, const RenderParams& p, uint32_t* framebuffer, float* linear,
-                                Counters* counters, cudaStream_t stream)
+cudaError_t launch_render_plain(const DevScene& S, const RenderBatch& b, const DevRequest* hostReq,
+                                Counters* counters, cudaStream_t stream, int* launches)
 {
-    dim3 block(8, 8);
-    dim3 grid((p.width + 7) / 8, (p.height + 7) / 8);
-    k_render_plain<<<grid, block, 0, stream>>>(S, p, framebuffer, linear, counters);
+    for (uint32_t k = 0; k < b.nreq; k++)
+    {
+        const DevRequest& r = hostReq[k];
+        dim3 block(8, 8);
+        dim3 grid((r.width + 7) / 8, (r.height + 7) / 8);
+        k_render_plain<<<grid, block, 0, stream>>>(S, r, b.eps, b.q, counters);
+    }
+    if (launches) *launches += int(b.nreq);
     return cudaGetLastError();
 }
 
-cudaError_t launch_render_wavefront(const DevScene& S, const RenderParams& p, const WavefrontBuffers& wb,
-                                    uint32_t* framebuffer, float* linear, Counters* counters, cudaStream_t stream,
-                                    int* launches)
+cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, const WavefrontBuffers& wb,
+                                    Counters* counters, cudaStream_t stream, int* launches)
 {
     static int gShade = 0;
     if (!gShade) gShade = blocks_for((const void*)k_wf_shade, kWfThreads);
     const int gFlat = sm_count() * 8;
     int nl = 0;
     const uint32_t cap = wb.capacity;
-    const uint32_t scap = wb.capacity * (wb.lightCapacity ? wb.lightCapacity : 1);
-    Q q[2] = {{wb.ray[0], wb.pixel[0], cap}, {wb.ray[1], wb.pixel[1], cap}};
-    k_wf_camera<<<gFlat, 256, 0, stream>>>(p, q[0], wb.accum, wb.count);
+    const uint32_t lcap = wb.lightCapacity ? wb.lightCapacity : 1;
+    const uint32_t scap = cap * lcap;
+    Q q[2] = {{wb.ray[0], wb.sample[0], wb.group[0], wb.depth[0], cap},
+              {wb.ray[1], wb.sample[1], wb.group[1], wb.depth[1], cap}};
+    k_wf_camera<<<gFlat, 256, 0, stream>>>(b, q[0], wb.accum, wb.count);
     nl++;
-    Query qa = p.q;
+    Query qa = b.q;
     qa.precision = 0;
     const float* sh = wb.shadow;
-    RaysSoA shadowRays {sh, sh + scap, sh + 2ull * scap, sh + 3ull * scap, sh + 4ull * scap, sh + 5ull * scap,
-                        sh + 6ull * scap};
-    for (int level = 0, cur = 0; level <= p.depth; level++, cur ^= 1)
+    const RaysSoA shadowRays {sh, sh + scap, sh + 2ull * scap, sh + 3ull * scap, sh + 4ull * scap, sh + 5ull * scap,
+                              sh + 6ull * scap, wb.shadowGroup};
+    for (int level = 0, cur = 0; level <= b.maxDepth; level++, cur ^= 1)
     {
         cudaMemsetAsync(wb.count + (cur ^ 1), 0, sizeof(uint32_t), stream);
         cudaMemsetAsync(wb.count + 2, 0, sizeof(uint32_t), stream);
-        const float* r = wb.ray[cur];
-        RaysSoA rays {r, r + cap, r + 2ull * cap, r + 3ull * cap, r + 4ull * cap, r + 5ull * cap, nullptr};
-        cudaError_t e = run_query(S, rays, 0, wb.count + cur, p.q, false, wb.hit, nullptr, wb.engine, wb.engineCapacity,
-                                  kEnginePasses, counters, stream, &nl);
+        cudaError_t e = run_query(S, q[cur].rays(), 0, wb.count + cur, b.q, false, wb.hit, nullptr, wb.engine,
+                                  wb.engineCapacity, kEnginePasses, counters, stream, &nl);
         if (e != cudaSuccess) return e;
-        k_wf_shade<<<gShade, kWfThreads, 0, stream>>>(S, p, q[cur], q[cur ^ 1], wb.count + cur, wb.count + (cur ^ 1),
-                                                      wb.count + 2, wb.hit, wb.shadow, wb.shadowSlot, scap, wb.contrib,
-                                                      wb.visible, wb.base, wb.accum, p.depth - level);
+        k_wf_shade<<<gShade, kWfThreads, 0, stream>>>(S, b.eps, q[cur], q[cur ^ 1], wb.count + cur,
+                                                      wb.count + (cur ^ 1), wb.count + 2, wb.hit, wb.shadow,
+                                                      wb.shadowGroup, wb.shadowSlot, scap, lcap, wb.contrib,
+                                                      wb.visible, wb.base, wb.accum);
         e = run_query(S, shadowRays, 0, wb.count + 2, qa, true, HitsSoA {}, wb.occluded, wb.engine, wb.engineCapacity,
                       kEnginePasses, counters, stream, &nl);
         if (e != cudaSuccess) return e;
         k_wf_visibility<<<gFlat, 256, 0, stream>>>(wb.occluded, wb.shadowSlot, wb.count + 2, scap, wb.visible);
         k_wf_resolve<<<gFlat, 256, 0, stream>>>(S, q[cur], wb.count + cur, wb.hit, wb.contrib, wb.visible, wb.base,
-                                               wb.accum);
+                                               lcap, wb.accum);
         nl += 3;
     }
-    k_wf_finish<<<gFlat, 256, 0, stream>>>(p, wb.accum, framebuffer, linear);
+    k_wf_finish<<<gFlat, 256, 0, stream>>>(b, wb.accum);
     nl++;
     if (launches) *launches += nl;
     return cudaGetLastError();

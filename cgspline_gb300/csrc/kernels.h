@@ -9,15 +9,12 @@
 
 namespace cgs {
 
-struct RaysSoA { const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax; };
+// Rays as structure of arrays; tmax null = +inf; group null = group 0.
+struct RaysSoA { const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax; const uint32_t* group; };
 struct HitsSoA { float *t, *u, *v; int32_t *patch, *object; };
 
 // ---------------------------------------------------------- ray queries --
-// Persistent kernels: every warp takes 32 rays at a time from *next until n.
-cudaError_t launch_closest(const DevScene& S, RaysSoA rays, uint32_t n, Query q, HitsSoA hits, uint32_t* next,
-                           Counters* counters, cudaStream_t stream);
-cudaError_t launch_any(const DevScene& S, RaysSoA rays, uint32_t n, Query q, int32_t* occluded, uint32_t* next,
-                       Counters* counters, cudaStream_t stream);
+// spline::doBezierClipping on explicit (ray, patch) pairs, one thread per pair.
 cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, RaysSoA rays, const uint32_t* patch_ids,
                                uint32_t n, Query q, HitsSoA hits, Counters* counters, cudaStream_t stream);
 
@@ -40,41 +37,58 @@ struct CameraSetup
     float half_dx, half_dy;
 };
 
-struct RenderParams
+// One render request of a batch.  Its samples are the global sample indices
+// [sampleBase, sampleBase + width*height*spp); its pixels [pixelBase, pixelBase
+// + width*height).
+struct DevRequest
 {
     CameraSetup cam;
-    uint32_t width, height, stride;
+    uint32_t group, width, height, spp;
     int depth;
+    uint32_t sampleBase, pixelBase, stride;
+    uint32_t* fb;
+    float* linear;
+};
+
+struct RenderBatch
+{
+    const DevRequest* req;   // device
+    uint32_t nreq;
+    uint32_t samples;        // total samples (primary rays)
+    uint32_t pixels;         // total output pixels
+    int maxDepth;
     float eps;
     Query q;
 };
 
-// Work buffers of the wavefront schedule (device memory, sized for w*h rays).
+// Work buffers of the wavefront schedule (device memory, sized for `capacity` samples).
 struct WavefrontBuffers
 {
-    // ray queues (two, ping-pong): origin, direction, attenuation, pixel
-    float* ray[2];       // 9 floats per ray, SoA: ox oy oz dx dy dz ax ay az
-    uint32_t* pixel[2];
-    uint32_t* count;     // [0..1] queue sizes, [2] shadow count, [3..7] work counters
-    HitsSoA hit;         // per ray of the current queue
-    int32_t* occluded;   // per shadow ray
-    uint32_t* engine;    // query-engine scratch
+    // ray queues (two, ping-pong): 9 floats per ray SoA (ox oy oz dx dy dz ax ay az)
+    float* ray[2];
+    uint32_t* sample[2];  // the primary sample each ray belongs to
+    uint32_t* group[2];
+    uint32_t* depth[2];   // bounces still allowed
+    uint32_t* count;      // [0..1] queue sizes, [2] shadow count
+    HitsSoA hit;          // per ray of the current queue
+    int32_t* occluded;    // per shadow ray
+    uint32_t* engine;     // query-engine scratch
     uint32_t engineCapacity;
-    float* shadow;       // 7 floats per shadow ray SoA: ox oy oz dx dy dz max
-    uint32_t* shadowSlot;  // (ray index * nlights + light) of each shadow ray
-    float* contrib;      // 3 floats per (ray, light) slot
-    int32_t* visible;    // per (ray, light) slot: 1 = lit, 0 = not
-    float* base;         // 3 floats per ray: ambient term, then the resolved colour factor
-    float* accum;        // 3 floats per pixel
-    uint32_t capacity;   // rays
+    float* shadow;        // 7 floats per shadow ray SoA: ox oy oz dx dy dz max
+    uint32_t* shadowGroup;
+    uint32_t* shadowSlot; // (ray index * lightCapacity + light) of each shadow ray
+    float* contrib;       // 3 floats per (ray, light) slot
+    int32_t* visible;     // per (ray, light) slot: 1 = lit, 0 = not
+    float* base;          // 3 floats per ray: the ambient term
+    float* accum;         // 3 floats per sample
+    uint32_t capacity;    // rays
     uint32_t lightCapacity;
 };
 
-cudaError_t launch_render_plain(const DevScene& S, const RenderParams& p, uint32_t* framebuffer, float* linear,
-                                Counters* counters, cudaStream_t stream);
-cudaError_t launch_render_wavefront(const DevScene& S, const RenderParams& p, const WavefrontBuffers& wb,
-                                    uint32_t* framebuffer, float* linear, Counters* counters, cudaStream_t stream,
-                                    int* launches);
+cudaError_t launch_render_plain(const DevScene& S, const RenderBatch& b, const DevRequest* hostReq,
+                                Counters* counters, cudaStream_t stream, int* launches);
+cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, const WavefrontBuffers& wb,
+                                    Counters* counters, cudaStream_t stream, int* launches);
 
 // ---------------------------------------------------------- perfect hash --
 struct HashScratch

@@ -1,37 +1,15 @@
-// scene.cu -- host side of libcgspline_gb300.so: scene objects, BVH build,
-// device upload, perfect-hash build orchestration and the C ABI of
-// include/cgspline.h.
-#include <algorithm>
+// scene.cu -- the scene store of libcgspline_gb300.so: surfaces, objects and
+// groups, the host BVH build, device upload, the perfect-hash build of every
+// BVH, and the C ABI entry points that build and inspect a store.
 #include <bit>
-#include <cmath>
-#include <cstring>
-#include <mutex>
 #include <numeric>
 #include <random>
-#include <stdexcept>
-#include <vector>
 
-#include "../../include/cgspline.h"
-#include "kernels.h"
+#include "scene_impl.h"
 
 using namespace cgs;
 
-namespace {
-
-// ------------------------------------------------------------- host BVH --
-struct Box
-{
-    float lo[3] = {INFINITY, INFINITY, INFINITY};
-    float hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    void inflate(const float p[3])
-    {
-        for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); }
-    }
-    void inflate(const Box& b) { inflate(b.lo); inflate(b.hi); }
-};
-
-struct Element { Box bounds; float centroid[3]; uint32_t index; };
-struct Node { Box leftBox, rightBox; uint32_t left, right; };
+namespace cgs {
 
 // BVH::build / split / wrap (src/rt/BVH.cpp:9-108): top-down median split,
 // heap keys (root 1, children 2k and 2k+1), nodes in pre-order, leaves keep
@@ -40,55 +18,49 @@ struct Node { Box leftBox, rightBox; uint32_t left, right; };
 // i.e. an empty box whose three extents compare equal, which selects y; the
 // partition is std::nth_element with the same comparator, so the topology
 // matches the reference built with the same standard library.
-struct HostBVH
+uint32_t HostBVH::wrap(Element* e, size_t count, uint32_t key)
 {
-    std::vector<Node> nodes;
-    std::vector<uint32_t> keys, indices;
-    uint32_t perNode = 1;
-    bool emptyLeaf = false;
+    if (count == 0) emptyLeaf = true;
+    Box box;
+    size_t idx = indices.size();
+    indices.resize(idx + count + 1);
+    for (size_t i = 0; i < count; i++) { indices[idx + i] = e[i].index; box.inflate(e[i].bounds); }
+    indices[idx + count] = EMPTY;
+    keys.push_back(key);
+    nodes.push_back({box, Box {}, EMPTY, uint32_t(idx)});
+    return uint32_t(nodes.size() - 1);
+}
 
-    uint32_t wrap(Element* e, size_t count, uint32_t key)
-    {
-        if (count == 0) { emptyLeaf = true; count = 0; }
-        Box box;
-        size_t idx = indices.size();
-        indices.resize(idx + count + 1);
-        for (size_t i = 0; i < count; i++) { indices[idx + i] = e[i].index; box.inflate(e[i].bounds); }
-        indices[idx + count] = EMPTY;
-        keys.push_back(key);
-        nodes.push_back({box, Box {}, EMPTY, uint32_t(idx)});
-        return uint32_t(nodes.size() - 1);
-    }
-    uint32_t split(Element* e, size_t count, uint32_t key)
-    {
-        if (count <= perNode || (key & (1u << 31))) return wrap(e, count, key);
-        Box empty;
-        float v[3] = {empty.hi[0] - empty.lo[0], empty.hi[1] - empty.lo[1], empty.hi[2] - empty.lo[2]};
-        const int dim = v[2] > v[1] ? (v[0] > v[2] ? 0 : 2) : (v[0] > v[1] ? 0 : 1);
-        size_t middle = count / 2;
-        std::nth_element(e, e + middle, e + count,
-                         [=](const Element& a, const Element& b) { return a.centroid[dim] < b.centroid[dim]; });
-        keys.push_back(key);
-        size_t idx = nodes.size();
-        nodes.push_back({});
-        uint32_t l = split(e, middle, key << 1);
-        uint32_t r = split(e + middle, count - middle, (key << 1) ^ 1u);
-        Node& node = nodes[idx];
-        node.left = l;
-        node.right = r;
-        node.leftBox = nodes[l].leftBox;
-        node.rightBox = nodes[r].leftBox;
-        if (nodes[l].left != EMPTY) node.leftBox.inflate(nodes[l].rightBox);
-        if (nodes[r].left != EMPTY) node.rightBox.inflate(nodes[r].rightBox);
-        return uint32_t(idx);
-    }
-    void build(std::vector<Element>& el)
-    {
-        nodes.clear(); keys.clear(); indices.clear(); emptyLeaf = false;
-        nodes.reserve(2 * el.size()); keys.reserve(2 * el.size()); indices.reserve(2 * el.size());
-        split(el.data(), el.size(), 1u);
-    }
-};
+uint32_t HostBVH::split(Element* e, size_t count, uint32_t key)
+{
+    if (count <= perNode || (key & (1u << 31))) return wrap(e, count, key);
+    Box empty;
+    float v[3] = {empty.hi[0] - empty.lo[0], empty.hi[1] - empty.lo[1], empty.hi[2] - empty.lo[2]};
+    const int dim = v[2] > v[1] ? (v[0] > v[2] ? 0 : 2) : (v[0] > v[1] ? 0 : 1);
+    size_t middle = count / 2;
+    std::nth_element(e, e + middle, e + count,
+                     [=](const Element& a, const Element& b) { return a.centroid[dim] < b.centroid[dim]; });
+    keys.push_back(key);
+    size_t idx = nodes.size();
+    nodes.push_back({});
+    uint32_t l = split(e, middle, key << 1);
+    uint32_t r = split(e + middle, count - middle, (key << 1) ^ 1u);
+    Node& node = nodes[idx];
+    node.left = l;
+    node.right = r;
+    node.leftBox = nodes[l].leftBox;
+    node.rightBox = nodes[r].leftBox;
+    if (nodes[l].left != EMPTY) node.leftBox.inflate(nodes[l].rightBox);
+    if (nodes[r].left != EMPTY) node.rightBox.inflate(nodes[r].rightBox);
+    return uint32_t(idx);
+}
+
+void HostBVH::build(std::vector<Element>& el)
+{
+    nodes.clear(); keys.clear(); indices.clear(); emptyLeaf = false;
+    nodes.reserve(2 * el.size()); keys.reserve(2 * el.size()); indices.reserve(2 * el.size());
+    split(el.data(), el.size(), 1u);
+}
 
 // std::mt19937(42) with std::uniform_int_distribution<uint32_t>(0, n) and
 // gcd(n, A) == 1 retries (src/rt/PerfectHashFunction.cu:379-400): the 16
@@ -111,127 +83,24 @@ void hash_coefficients(uint32_t n, uint32_t A[16], uint32_t B[16])
     }
 }
 
-struct Surface
+// Table capacity: n plus 15 growth steps of max(4, 5% of n)
+// (src/rt/PerfectHashFunction.cu:249-251, 481).
+uint32_t table_capacity(uint32_t n)
 {
-    std::vector<float> points;   // 4 per point
-    std::vector<uint32_t> indices;
-    HostBVH bvh;
-    uint32_t patchCount() const { return uint32_t(indices.size() / 16); }
-};
-
-struct Object
-{
-    uint32_t surface;
-    float l2w[16], w2l[16];
-    cgs_material material;
-    std::vector<uint32_t> patchMaterial;
-    std::vector<cgs_material> materials;
-};
-
-template<class T> struct DBuf
-{
-    T* p = nullptr;
-    size_t n = 0;
-    cudaError_t reserve(size_t count)
-    {
-        if (count <= n) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr; n = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
-        if (e == cudaSuccess) n = count;
-        return e;
-    }
-    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
-};
-
-int cuda_status(cudaError_t e)
-{
-    if (e == cudaSuccess) return CGS_OK;
-    if (e == cudaErrorMemoryAllocation) return CGS_ERR_OUT_OF_MEMORY;
-    return CGS_ERR_CUDA;
+    uint32_t step = std::max<uint32_t>(4u, uint32_t(0.05f * float(n)));
+    return n + 15u * step;
 }
 
-#define CGS_TRY(expr)                          \
-    do {                                       \
-        cudaError_t _e = (expr);               \
-        if (_e != cudaSuccess) return cuda_status(_e); \
-    } while (0)
-
-}  // namespace
-
-struct cgs_scene
+// Displacement table size: the power of two at or below max(2, (n-1)/2)
+// (src/rt/PerfectHashFunction.cu:233-248).
+uint32_t displ_size(uint32_t n)
 {
-    int device = 0;
-    std::mutex mu;
-    std::vector<Surface> surfaces;
-    std::vector<Object> objects;
-    std::vector<cgs_light> lights;
-    float background[3] = {0.1f, 0.1f, 0.1f}, ambient[3] = {0.1f, 0.1f, 0.1f};
-    HostBVH top;
-    bool bvhBuilt = false, uploaded = false, hashed = false;
+    int s = int(n - 1) >> 1;
+    if (s < 2) s = 2;
+    return std::bit_floor(uint32_t(s));
+}
 
-    // device side
-    DBuf<float4> patches, nodes;
-    DBuf<uint32_t> indices, tables, disps, patchBase, patchMaterial, keys;
-    DBuf<DevBVH> bvhs;
-    DBuf<DevObject> dobjects;
-    DBuf<DevMaterial> materials;
-    DBuf<DevLight> dlights;
-    std::vector<DevBVH> hbvh;
-    std::vector<uint32_t> tableCap;  // per BVH
-    DBuf<uint32_t> scratch32;
-    DBuf<unsigned long long> scratch64;
-    DBuf<Counters> counters;
-    DBuf<uint32_t> work;
-
-    // query staging
-    DBuf<float> rayStage;
-    DBuf<float> hitF;
-    DBuf<int32_t> hitI;
-
-    // wavefront buffers
-    WavefrontBuffers wb {};
-    DBuf<float> wfRay0, wfRay1, wfShadow, wfContrib, wfBase, wfAccum, wfHitF;
-    DBuf<uint32_t> wfPix0, wfPix1, wfCount, wfShadowSlot;
-    DBuf<int32_t> wfVisible, wfHitI, wfOccluded;
-    DBuf<uint32_t> engine;
-    uint32_t engineCapacity = 0;
-    DBuf<uint32_t> fbStage;
-    DBuf<float> linStage;
-
-    cudaEvent_t finished = nullptr;
-    cudaStream_t lastStream = nullptr;
-    int launches = 0;
-    uint64_t primaryRays = 0, bounceRays = 0, shadowRays = 0;
-
-    DevScene dev() const
-    {
-        DevScene S {};
-        S.patches = patches.p; S.nodes = nodes.p; S.indices = indices.p; S.tables = tables.p; S.disps = disps.p;
-        S.bvhs = bvhs.p; S.patchBase = patchBase.p; S.objects = dobjects.p; S.materials = materials.p;
-        S.patchMaterial = patchMaterial.p; S.lights = dlights.p;
-        S.nobjects = uint32_t(objects.size()); S.nlights = uint32_t(lights.size());
-        S.nsurfaces = uint32_t(surfaces.size()); S.topBVH = uint32_t(surfaces.size());
-        for (int k = 0; k < 3; k++) { S.background[k] = background[k]; S.ambient[k] = ambient[k]; }
-        return S;
-    }
-    const HostBVH& bvh(uint32_t which) const { return which < surfaces.size() ? surfaces[which].bvh : top; }
-    ~cgs_scene()
-    {
-        cudaSetDevice(device);
-        for (auto* b : {&patches, &nodes}) b->release();
-        for (auto* b : {&indices, &tables, &disps, &patchBase, &patchMaterial, &keys, &scratch32, &work, &wfPix0,
-                        &wfPix1, &wfCount, &wfShadowSlot, &fbStage})
-            b->release();
-        for (auto* b : {&rayStage, &hitF, &wfRay0, &wfRay1, &wfShadow, &wfContrib, &wfBase, &wfAccum, &linStage,
-                        &wfHitF})
-            b->release();
-        bvhs.release(); dobjects.release(); materials.release(); dlights.release(); scratch64.release();
-        counters.release(); hitI.release(); wfHitF.release(); wfHitI.release(); wfOccluded.release();
-        wfVisible.release(); engine.release();
-        if (finished) cudaEventDestroy(finished);
-    }
-};
+}  // namespace cgs
 
 namespace {
 
@@ -265,15 +134,15 @@ void build_surface_bvh(Surface& s)
     s.bvh.build(el);
 }
 
-// Scene::buildBVH (src/rt/Scene.cu:218-232): object bounds of the transformed
-// points (BezierSurface::bounds(M), src/rt/Primitive.cu:172-179), centroid =
-// box centre.
-void build_top_bvh(cgs_scene* sc)
+// Scene::buildBVH (src/rt/Scene.cu:218-232) for one group: object bounds of
+// the transformed points (BezierSurface::bounds(M), src/rt/Primitive.cu:172-179),
+// centroid = box centre, element index = the global object id.
+void build_group_bvh(cgs_scene* sc, Group& g)
 {
-    std::vector<Element> el(sc->objects.size());
+    std::vector<Element> el(g.objects.size());
     for (uint32_t i = 0; i < el.size(); i++)
     {
-        const Object& ob = sc->objects[i];
+        const Object& ob = sc->objects[g.objects[i]];
         const Surface& s = sc->surfaces[ob.surface];
         const float* M = ob.l2w;
         Box b;
@@ -287,11 +156,11 @@ void build_top_bvh(cgs_scene* sc)
             float p[3] = {x / ww, y / ww, z / ww};
             b.inflate(p);
         }
-        el[i].index = i;
+        el[i].index = g.objects[i];
         el[i].bounds = b;
         for (int k = 0; k < 3; k++) el[i].centroid[k] = 0.5f * (b.lo[k] + b.hi[k]);
     }
-    sc->top.build(el);
+    g.top.build(el);
 }
 
 void pack_nodes(const HostBVH& b, std::vector<float4>& out)
@@ -311,24 +180,34 @@ void pack_nodes(const HostBVH& b, std::vector<float4>& out)
     }
 }
 
-uint32_t table_capacity(uint32_t n)
+// Lights of all groups, concatenated; groupLights[g] = (first, count);
+// groupEnv[g] = background rgb, ambient rgb.
+int upload_lights(cgs_scene* sc)
 {
-    uint32_t step = std::max<uint32_t>(4u, uint32_t(0.05f * float(n)));
-    return n + 15u * step;
-}
-
-uint32_t displ_size(uint32_t n)
-{
-    int s = int(n - 1) >> 1;
-    if (s < 2) s = 2;
-    return std::bit_floor(uint32_t(s));
+    std::vector<DevLight> hl;
+    std::vector<uint2> gl;
+    std::vector<float> env;
+    for (const Group& g : sc->groups)
+    {
+        gl.push_back(make_uint2(uint32_t(hl.size()), uint32_t(g.lights.size())));
+        for (const auto& l : g.lights) { DevLight d; std::memcpy(&d, &l, sizeof d); hl.push_back(d); }
+        for (int k = 0; k < 3; k++) env.push_back(g.background[k]);
+        for (int k = 0; k < 3; k++) env.push_back(g.ambient[k]);
+    }
+    CGS_TRY(sc->dlights.reserve(std::max<size_t>(hl.size(), 1)));
+    CGS_TRY(sc->groupLights.reserve(gl.size()));
+    CGS_TRY(sc->groupEnv.reserve(env.size()));
+    if (!hl.empty()) CGS_TRY(cudaMemcpy(sc->dlights.p, hl.data(), hl.size() * sizeof(DevLight), cudaMemcpyHostToDevice));
+    CGS_TRY(cudaMemcpy(sc->groupLights.p, gl.data(), gl.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    CGS_TRY(cudaMemcpy(sc->groupEnv.p, env.data(), env.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return CGS_OK;
 }
 
 int upload(cgs_scene* sc)
 {
-    const uint32_t nb = uint32_t(sc->surfaces.size()) + 1;
+    const uint32_t nb = sc->nbvh();
     std::vector<float4> hp, hn;
-    std::vector<uint32_t> hi, pbase, pmat;
+    std::vector<uint32_t> hi, pbase, pmat, gtop;
     std::vector<DevMaterial> hm;
     std::vector<DevObject> ho;
     sc->hbvh.assign(nb, DevBVH {});
@@ -352,6 +231,7 @@ int upload(cgs_scene* sc)
         d.N = n; d.A = 31; d.B = 19;
         d.Nmagic = fastmod_magic(std::max<uint32_t>(n, 1));
     }
+    for (uint32_t g = 0; g < sc->groups.size(); g++) gtop.push_back(uint32_t(sc->surfaces.size()) + g);
     for (const Surface& s : sc->surfaces)
     {
         pbase.push_back(patchCursor);
@@ -381,8 +261,6 @@ int upload(cgs_scene* sc)
             d.patchMaterialBase = -1;
         ho.push_back(d);
     }
-    std::vector<DevLight> hl;
-    for (const auto& l : sc->lights) { DevLight d; std::memcpy(&d, &l, sizeof d); hl.push_back(d); }
     CGS_TRY(sc->patches.reserve(hp.size()));
     CGS_TRY(sc->nodes.reserve(hn.size()));
     CGS_TRY(sc->indices.reserve(hi.size()));
@@ -391,11 +269,10 @@ int upload(cgs_scene* sc)
     CGS_TRY(sc->patchBase.reserve(pbase.size()));
     CGS_TRY(sc->patchMaterial.reserve(std::max<size_t>(pmat.size(), 1)));
     CGS_TRY(sc->bvhs.reserve(nb));
+    CGS_TRY(sc->groupTop.reserve(gtop.size()));
     CGS_TRY(sc->dobjects.reserve(ho.size()));
     CGS_TRY(sc->materials.reserve(hm.size()));
-    CGS_TRY(sc->dlights.reserve(std::max<size_t>(hl.size(), 1)));
     CGS_TRY(sc->counters.reserve(1));
-    CGS_TRY(sc->work.reserve(8));
     CGS_TRY(cudaMemcpy(sc->patches.p, hp.data(), hp.size() * sizeof(float4), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->nodes.p, hn.data(), hn.size() * sizeof(float4), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->indices.p, hi.data(), hi.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -404,15 +281,18 @@ int upload(cgs_scene* sc)
         CGS_TRY(cudaMemcpy(sc->patchMaterial.p, pmat.data(), pmat.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->dobjects.p, ho.data(), ho.size() * sizeof(DevObject), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->materials.p, hm.data(), hm.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice));
-    if (!hl.empty()) CGS_TRY(cudaMemcpy(sc->dlights.p, hl.data(), hl.size() * sizeof(DevLight), cudaMemcpyHostToDevice));
+    CGS_TRY(cudaMemcpy(sc->groupTop.p, gtop.data(), gtop.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->bvhs.p, sc->hbvh.data(), nb * sizeof(DevBVH), cudaMemcpyHostToDevice));
+    int r = upload_lights(sc);
+    if (r) return r;
     sc->uploaded = true;
     return CGS_OK;
 }
 
+// BVH::buildHashTable (src/rt/BVH.cpp:24-39) for every BVH of the store.
 int hash_all(cgs_scene* sc, cudaStream_t stream)
 {
-    const uint32_t nb = uint32_t(sc->surfaces.size()) + 1;
+    const uint32_t nb = sc->nbvh();
     uint32_t maxn = 1;
     for (uint32_t k = 0; k < nb; k++) maxn = std::max<uint32_t>(maxn, uint32_t(sc->bvh(k).keys.size()));
     size_t w32 = 0, w64 = 0;
@@ -444,81 +324,49 @@ int hash_all(cgs_scene* sc, cudaStream_t stream)
     return CGS_OK;
 }
 
-void camera_setup(const cgs_camera& c, uint32_t w, uint32_t h, int flip, CameraSetup& s)
+Group& current_group(cgs_scene* s) { return s->groups[s->current]; }
+
+bool bvh_index(const cgs_scene* s, int32_t which, uint32_t& k)
 {
-    // Transform::matrix() = T R S with the quaternion rotation of src/AlignedTypes.h:99-115
-    float i = c.rotation[0], j = c.rotation[1], k = c.rotation[2], r = c.rotation[3];
-    float ii = 2 * i * i, ij = 2 * i * j, ik = 2 * i * k, jj = 2 * j * j, jk = 2 * j * k, kk = 2 * k * k,
-          ri = 2 * r * i, rj = 2 * r * j, rk = 2 * r * k;
-    float c0[3] = {1 - jj - kk, ij + rk, ik - rj}, c1[3] = {ij - rk, 1 - ii - kk, jk + ri},
-          c2[3] = {ik + rj, jk - ri, 1 - ii - jj};
-    for (int q = 0; q < 3; q++)
+    if (which >= 0)
     {
-        s.c2w[q] = c0[q] * c.scale[0];
-        s.c2w[4 + q] = c1[q] * c.scale[1];
-        s.c2w[8 + q] = c2[q] * c.scale[2];
-        s.c2w[12 + q] = c.position[q];
-        s.pos[q] = c.position[q];
+        if (uint32_t(which) >= s->surfaces.size()) return false;
+        k = uint32_t(which);
+        return true;
     }
-    s.c2w[3] = s.c2w[7] = s.c2w[11] = 0.0f;
-    s.c2w[15] = 1.0f;
-    // src/rt/RayTracer.cu:152-163
-    float halfHeight = std::tan(0.5f * c.fovy);
-    s.half_dy = halfHeight / float(h);
-    s.half_dx = s.half_dy;
-    s.tl[0] = -s.half_dx * float(w - 1);
-    s.tl[1] = halfHeight - s.half_dy;
-    if (flip) { s.tl[1] = -s.tl[1]; s.half_dy = -s.half_dy; }
+    uint32_t g = uint32_t(-1 - int64_t(which));
+    if (g >= s->groups.size()) return false;
+    k = uint32_t(s->surfaces.size()) + g;
+    return true;
 }
-
-int ensure_engine(cgs_scene* sc, uint32_t capacity)
-{
-    if (sc->engineCapacity >= capacity) return CGS_OK;
-    CGS_TRY(sc->engine.reserve(engine_words(capacity, kEnginePasses)));
-    sc->engineCapacity = capacity;
-    return CGS_OK;
-}
-
-int ensure_wavefront(cgs_scene* sc, uint32_t nrays)
-{
-    uint32_t nl = std::max<uint32_t>(1, uint32_t(sc->lights.size()));
-    if (sc->wb.capacity >= nrays && sc->wb.lightCapacity >= nl && sc->wb.engine == sc->engine.p) return CGS_OK;
-    size_t cap = nrays, sc_ = size_t(nrays) * nl;
-    CGS_TRY(sc->wfRay0.reserve(9 * cap));
-    CGS_TRY(sc->wfRay1.reserve(9 * cap));
-    CGS_TRY(sc->wfPix0.reserve(cap));
-    CGS_TRY(sc->wfPix1.reserve(cap));
-    CGS_TRY(sc->wfCount.reserve(8));
-    CGS_TRY(sc->wfHitF.reserve(3 * cap));
-    CGS_TRY(sc->wfHitI.reserve(2 * cap));
-    CGS_TRY(sc->wfOccluded.reserve(sc_));
-    {
-        int r = ensure_engine(sc, uint32_t(std::max<size_t>(cap, sc_)));
-        if (r) return r;
-    }
-    CGS_TRY(sc->wfShadow.reserve(7 * sc_));
-    CGS_TRY(sc->wfShadowSlot.reserve(sc_));
-    CGS_TRY(sc->wfContrib.reserve(3 * sc_));
-    CGS_TRY(sc->wfVisible.reserve(sc_));
-    CGS_TRY(sc->wfBase.reserve(3 * cap));
-    CGS_TRY(sc->wfAccum.reserve(3 * cap));
-    WavefrontBuffers& wb = sc->wb;
-    wb.ray[0] = sc->wfRay0.p; wb.ray[1] = sc->wfRay1.p;
-    wb.pixel[0] = sc->wfPix0.p; wb.pixel[1] = sc->wfPix1.p;
-    wb.count = sc->wfCount.p; wb.shadow = sc->wfShadow.p; wb.shadowSlot = sc->wfShadowSlot.p;
-    wb.hit = HitsSoA {sc->wfHitF.p, sc->wfHitF.p + cap, sc->wfHitF.p + 2 * cap, sc->wfHitI.p, sc->wfHitI.p + cap};
-    wb.occluded = sc->wfOccluded.p;
-    wb.engine = sc->engine.p;
-    wb.engineCapacity = sc->engineCapacity;
-    wb.contrib = sc->wfContrib.p; wb.visible = sc->wfVisible.p; wb.base = sc->wfBase.p; wb.accum = sc->wfAccum.p;
-    wb.capacity = nrays;
-    wb.lightCapacity = nl;
-    return CGS_OK;
-}
-
-bool valid_query(int method, int precision) { return (method == 0 || method == 1) && precision >= 0 && precision <= 2; }
 
 }  // namespace
+
+cgs::DevScene cgs_scene::dev() const
+{
+    DevScene S {};
+    S.patches = patches.p; S.nodes = nodes.p; S.indices = indices.p; S.tables = tables.p; S.disps = disps.p;
+    S.bvhs = bvhs.p; S.patchBase = patchBase.p; S.objects = dobjects.p; S.materials = materials.p;
+    S.patchMaterial = patchMaterial.p; S.lights = dlights.p;
+    S.groupTop = groupTop.p; S.groupLights = groupLights.p; S.groupEnv = groupEnv.p;
+    S.nobjects = uint32_t(objects.size()); S.nsurfaces = uint32_t(surfaces.size());
+    S.ngroups = uint32_t(groups.size());
+    return S;
+}
+
+cgs_scene::~cgs_scene()
+{
+    cudaSetDevice(device);
+    patches.release(); nodes.release();
+    for (auto* b : {&indices, &tables, &disps, &patchBase, &patchMaterial, &keys, &groupTop, &scratch32, &groupStage,
+                    &engine, &fbStage})
+        b->release();
+    rayStage.release(); hitF.release(); linStage.release(); groupEnv.release();
+    groupLights.release(); bvhs.release(); dobjects.release(); materials.release(); dlights.release();
+    scratch64.release(); counters.release(); hitI.release();
+    slot.release();
+    if (finished) cudaEventDestroy(finished);
+}
 
 // =========================================================== C ABI ====
 extern "C" {
@@ -544,7 +392,7 @@ const char* cgs_status_string(int s)
     }
 }
 
-int cgs_version(void) { return 1; }
+int cgs_version(void) { return 2; }
 
 int cgs_scene_create(cgs_scene** out, int device)
 {
@@ -556,6 +404,7 @@ int cgs_scene_create(cgs_scene** out, int device)
     auto* s = new (std::nothrow) cgs_scene();
     if (!s) return CGS_ERR_OUT_OF_MEMORY;
     s->device = device;
+    s->groups.emplace_back();
     if (cudaEventCreateWithFlags(&s->finished, cudaEventDisableTiming) != cudaSuccess) { delete s; return CGS_ERR_CUDA; }
     *out = s;
     return CGS_OK;
@@ -585,6 +434,20 @@ int cgs_scene_add_surface(cgs_scene* s, const float* pts, uint32_t npoints, cons
     return CGS_OK;
 }
 
+int cgs_scene_add_group(cgs_scene* s, uint32_t* gid)
+{
+    if (!s) return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (current_group(s).touched)
+    {
+        s->groups.emplace_back();
+        s->current = uint32_t(s->groups.size() - 1);
+        s->bvhBuilt = s->uploaded = s->hashed = false;
+    }
+    if (gid) *gid = s->current;
+    return CGS_OK;
+}
+
 int cgs_scene_add_object(cgs_scene* s, uint32_t surface, const float l2w[16], const float w2l[16],
                          const cgs_material* material, const uint32_t* pm, const cgs_material* mats, uint32_t nm,
                          uint32_t* oid)
@@ -594,6 +457,7 @@ int cgs_scene_add_object(cgs_scene* s, uint32_t surface, const float l2w[16], co
     if (surface >= s->surfaces.size()) return CGS_ERR_INVALID_ARGUMENT;
     Object ob;
     ob.surface = surface;
+    ob.group = s->current;
     std::memcpy(ob.l2w, l2w, sizeof ob.l2w);
     std::memcpy(ob.w2l, w2l, sizeof ob.w2l);
     ob.material = *material;
@@ -606,6 +470,8 @@ int cgs_scene_add_object(cgs_scene* s, uint32_t surface, const float l2w[16], co
         ob.materials.assign(mats, mats + nm);
     }
     s->objects.push_back(std::move(ob));
+    current_group(s).objects.push_back(uint32_t(s->objects.size() - 1));
+    current_group(s).touched = true;
     s->bvhBuilt = s->uploaded = s->hashed = false;
     if (oid) *oid = uint32_t(s->objects.size() - 1);
     return CGS_OK;
@@ -615,22 +481,23 @@ int cgs_scene_set_lights(cgs_scene* s, const cgs_light* lights, uint32_t n)
 {
     if (!s || (n && !lights)) return CGS_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(s->mu);
-    s->lights.assign(lights, lights + n);
-    if (s->uploaded)
-    {
-        cudaSetDevice(s->device);
-        CGS_TRY(s->dlights.reserve(std::max<uint32_t>(n, 1)));
-        if (n) CGS_TRY(cudaMemcpy(s->dlights.p, lights, n * sizeof(cgs_light), cudaMemcpyHostToDevice));
-    }
-    return CGS_OK;
+    current_group(s).lights.assign(lights, lights + n);
+    current_group(s).touched = true;
+    if (!s->uploaded) return CGS_OK;
+    CGS_TRY(cudaSetDevice(s->device));
+    return upload_lights(s);
 }
 
 int cgs_scene_set_environment(cgs_scene* s, const float bg[3], const float amb[3])
 {
     if (!s || !bg || !amb) return CGS_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(s->mu);
-    for (int k = 0; k < 3; k++) { s->background[k] = bg[k]; s->ambient[k] = amb[k]; }
-    return CGS_OK;
+    Group& gr = current_group(s);
+    for (int k = 0; k < 3; k++) { gr.background[k] = bg[k]; gr.ambient[k] = amb[k]; }
+    gr.touched = true;
+    if (!s->uploaded) return CGS_OK;
+    CGS_TRY(cudaSetDevice(s->device));
+    return upload_lights(s);
 }
 
 int cgs_bvh_build(cgs_scene* s)
@@ -638,13 +505,18 @@ int cgs_bvh_build(cgs_scene* s)
     if (!s) return CGS_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(s->mu);
     if (s->objects.empty()) return CGS_ERR_INVALID_ARGUMENT;
+    for (const Group& gr : s->groups)
+        if (gr.objects.empty()) return CGS_ERR_EMPTY_LEAF;
     for (auto& sf : s->surfaces)
     {
         build_surface_bvh(sf);
         if (sf.bvh.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
     }
-    build_top_bvh(s);
-    if (s->top.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
+    for (auto& gr : s->groups)
+    {
+        build_group_bvh(s, gr);
+        if (gr.top.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
+    }
     s->bvhBuilt = true;
     s->uploaded = s->hashed = false;
     return CGS_OK;
@@ -675,10 +547,10 @@ int cgs_scene_footprint(const cgs_scene* s, uint64_t* bytes)
 {
     if (!s || !bytes) return CGS_ERR_INVALID_ARGUMENT;
     uint64_t b = 0;
-    b += s->patches.n * sizeof(float4) + s->nodes.n * sizeof(float4);
-    b += (s->indices.n + s->tables.n + s->disps.n + s->patchBase.n + s->patchMaterial.n) * sizeof(uint32_t);
-    b += s->bvhs.n * sizeof(DevBVH) + s->dobjects.n * sizeof(DevObject) + s->materials.n * sizeof(DevMaterial);
-    b += s->dlights.n * sizeof(DevLight);
+    b += s->patches.bytes() + s->nodes.bytes() + s->indices.bytes() + s->tables.bytes() + s->disps.bytes();
+    b += s->patchBase.bytes() + s->patchMaterial.bytes() + s->bvhs.bytes() + s->dobjects.bytes();
+    b += s->materials.bytes() + s->dlights.bytes() + s->groupTop.bytes() + s->groupLights.bytes();
+    b += s->groupEnv.bytes();
     *bytes = b;
     return CGS_OK;
 }
@@ -687,8 +559,8 @@ int cgs_bvh_sizes(const cgs_scene* s, int32_t which, uint32_t sizes[5])
 {
     if (!s || !sizes) return CGS_ERR_INVALID_ARGUMENT;
     if (!s->bvhBuilt) return CGS_ERR_NOT_BUILT;
-    uint32_t k = which < 0 ? uint32_t(s->surfaces.size()) : uint32_t(which);
-    if (k > s->surfaces.size()) return CGS_ERR_INVALID_ARGUMENT;
+    uint32_t k;
+    if (!bvh_index(s, which, k)) return CGS_ERR_INVALID_ARGUMENT;
     const HostBVH& b = s->bvh(k);
     sizes[0] = uint32_t(b.nodes.size());
     sizes[1] = uint32_t(b.indices.size());
@@ -703,8 +575,8 @@ int cgs_bvh_export(const cgs_scene* s, int32_t which, uint32_t* nodes, uint32_t*
 {
     if (!s) return CGS_ERR_INVALID_ARGUMENT;
     if (!s->bvhBuilt) return CGS_ERR_NOT_BUILT;
-    uint32_t k = which < 0 ? uint32_t(s->surfaces.size()) : uint32_t(which);
-    if (k > s->surfaces.size()) return CGS_ERR_INVALID_ARGUMENT;
+    uint32_t k;
+    if (!bvh_index(s, which, k)) return CGS_ERR_INVALID_ARGUMENT;
     const HostBVH& b = s->bvh(k);
     if (nodes)
         for (size_t i = 0; i < b.nodes.size(); i++)
@@ -721,7 +593,7 @@ int cgs_bvh_export(const cgs_scene* s, int32_t which, uint32_t* nodes, uint32_t*
     if (indices) std::copy(b.indices.begin(), b.indices.end(), indices);
     if (s->hashed)
     {
-        cudaSetDevice(s->device);
+        CGS_TRY(cudaSetDevice(s->device));
         const DevBVH& d = s->hbvh[k];
         if (table) CGS_TRY(cudaMemcpy(table, s->tables.p + d.tableBase, d.N * sizeof(uint32_t), cudaMemcpyDeviceToHost));
         if (disp) CGS_TRY(cudaMemcpy(disp, s->disps.p + d.dispBase, (d.mask + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -732,192 +604,18 @@ int cgs_bvh_export(const cgs_scene* s, int32_t which, uint32_t* nodes, uint32_t*
     return CGS_OK;
 }
 
-int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, int precision, float tol, int any_hit,
-                  const cgs_hits* hits, void* stream)
-{
-    if (!s || !rays || !hits || !valid_query(method, precision) || !(tol > 0.0f)) return CGS_ERR_INVALID_ARGUMENT;
-    if (!hits->patch || (!any_hit && (!hits->t || !hits->u || !hits->v || !hits->object)))
-        return CGS_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> g(s->mu);
-    if (!s->hashed) return CGS_ERR_NOT_BUILT;
-    CGS_TRY(cudaSetDevice(s->device));
-    cudaStream_t st = (cudaStream_t)stream;
-    CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
-    RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax};
-    Query q {method, precision, tol};
-    s->launches = 0;
-    s->primaryRays = n; s->bounceRays = 0; s->shadowRays = 0;
-    {
-        int er = ensure_engine(s, n);
-        if (er) return er;
-    }
-    cudaError_t e = run_query(s->dev(), r, n, nullptr, q, any_hit != 0,
-                              HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, hits->patch,
-                              s->engine.p, s->engineCapacity, kEnginePasses, s->counters.p, st, &s->launches);
-    s->lastStream = st;
-    return cuda_status(e);
-}
-
-int cgs_intersect_host(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, int precision, float tol,
-                       int any_hit, const cgs_hits* hits, void* stream)
-{
-    if (!s || !rays || !hits) return CGS_ERR_INVALID_ARGUMENT;
-    cudaStream_t st = (cudaStream_t)stream;
-    {
-        std::lock_guard<std::mutex> g(s->mu);
-        CGS_TRY(cudaSetDevice(s->device));
-        CGS_TRY(s->rayStage.reserve(7ull * std::max<uint32_t>(n, 1)));
-        CGS_TRY(s->hitF.reserve(3ull * std::max<uint32_t>(n, 1)));
-        CGS_TRY(s->hitI.reserve(2ull * std::max<uint32_t>(n, 1)));
-        const float* src[7] = {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax};
-        for (int k = 0; k < 7; k++)
-        {
-            if (!src[k]) return CGS_ERR_INVALID_ARGUMENT;
-            CGS_TRY(cudaMemcpyAsync(s->rayStage.p + size_t(k) * n, src[k], n * sizeof(float), cudaMemcpyHostToDevice, st));
-        }
-    }
-    float* R = s->rayStage.p;
-    cgs_rays dr {R, R + n, R + 2ull * n, R + 3ull * n, R + 4ull * n, R + 5ull * n, R + 6ull * n};
-    cgs_hits dh {s->hitF.p, s->hitF.p + n, s->hitF.p + 2ull * n, s->hitI.p, s->hitI.p + n};
-    int r = cgs_intersect(s, &dr, n, method, precision, tol, any_hit, &dh, stream);
-    if (r) return r;
-    if (hits->patch) CGS_TRY(cudaMemcpyAsync(hits->patch, dh.patch, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    if (!any_hit)
-    {
-        if (hits->t) CGS_TRY(cudaMemcpyAsync(hits->t, dh.t, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (hits->u) CGS_TRY(cudaMemcpyAsync(hits->u, dh.u, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (hits->v) CGS_TRY(cudaMemcpyAsync(hits->v, dh.v, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (hits->object) CGS_TRY(cudaMemcpyAsync(hits->object, dh.object, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    }
-    CGS_TRY(cudaStreamSynchronize(st));
-    return CGS_OK;
-}
-
-int cgs_patch_intersect(cgs_scene* s, uint32_t surface, const cgs_rays* rays, const uint32_t* pids, uint32_t n,
-                        int method, float tol, const cgs_hits* hits, void* stream)
-{
-    if (!s || !rays || !pids || !hits || !hits->t || !hits->u || !hits->v || !hits->patch) return CGS_ERR_INVALID_ARGUMENT;
-    if (!valid_query(method, 0) || !(tol > 0.0f)) return CGS_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> g(s->mu);
-    if (!s->uploaded) return CGS_ERR_NOT_BUILT;
-    if (surface >= s->surfaces.size()) return CGS_ERR_INVALID_ARGUMENT;
-    CGS_TRY(cudaSetDevice(s->device));
-    cudaStream_t st = (cudaStream_t)stream;
-    CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
-    RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax};
-    Query q {method, 0, tol};
-    s->launches = 1;
-    s->lastStream = st;
-    return cuda_status(launch_patch_pairs(s->dev(), surface, r, pids, n, q,
-                                          HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, s->counters.p,
-                                          st));
-}
-
-int cgs_render(cgs_scene* s, const cgs_camera* cam, uint32_t w, uint32_t h, const cgs_render_options* opt,
-               uint32_t* fb, uint32_t stride, float* linear, void* stream)
-{
-    if (!s || !cam || !opt || w == 0 || h == 0 || (!fb && !linear) || (fb && stride < w)) return CGS_ERR_INVALID_ARGUMENT;
-    if (!valid_query(opt->method, opt->precision) || opt->recursion_depth < 0 || opt->recursion_depth > 64 ||
-        !(opt->tol > 0.0f) || (opt->schedule != 0 && opt->schedule != 1))
-        return CGS_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> g(s->mu);
-    if (!s->hashed) return CGS_ERR_NOT_BUILT;
-    CGS_TRY(cudaSetDevice(s->device));
-    cudaError_t q = cudaEventQuery(s->finished);
-    if (q == cudaErrorNotReady) return CGS_ERR_BUSY;
-    cudaStream_t st = (cudaStream_t)stream;
-    RenderParams p {};
-    camera_setup(*cam, w, h, opt->flip_y, p.cam);
-    p.width = w; p.height = h; p.stride = fb ? stride : w;
-    p.depth = opt->recursion_depth; p.eps = opt->eps;
-    p.q = Query {opt->method, opt->precision, opt->tol};
-    CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
-    s->launches = 0;
-    cudaError_t e;
-    if (opt->schedule == CGS_SCHED_PLAIN)
-    {
-        e = launch_render_plain(s->dev(), p, fb, linear, s->counters.p, st);
-        s->launches = 1;
-    }
-    else
-    {
-        int r = ensure_wavefront(s, w * h);
-        if (r) return r;
-        e = launch_render_wavefront(s->dev(), p, s->wb, fb, linear, s->counters.p, st, &s->launches);
-    }
-    if (e != cudaSuccess) return cuda_status(e);
-    CGS_TRY(cudaEventRecord(s->finished, st));
-    s->lastStream = st;
-    return CGS_OK;
-}
-
-int cgs_render_host(cgs_scene* s, const cgs_camera* cam, uint32_t w, uint32_t h, const cgs_render_options* opt,
-                    uint32_t* fb, float* linear, void* stream)
-{
-    if (!s || (!fb && !linear)) return CGS_ERR_INVALID_ARGUMENT;
-    cudaStream_t st = (cudaStream_t)stream;
-    {
-        std::lock_guard<std::mutex> g(s->mu);
-        CGS_TRY(cudaSetDevice(s->device));
-        if (fb) CGS_TRY(s->fbStage.reserve(size_t(w) * h));
-        if (linear) CGS_TRY(s->linStage.reserve(3ull * w * h));
-    }
-    int r = cgs_render(s, cam, w, h, opt, fb ? s->fbStage.p : nullptr, w, linear ? s->linStage.p : nullptr, stream);
-    if (r) return r;
-    if (fb) CGS_TRY(cudaMemcpyAsync(fb, s->fbStage.p, size_t(w) * h * 4, cudaMemcpyDeviceToHost, st));
-    if (linear) CGS_TRY(cudaMemcpyAsync(linear, s->linStage.p, 12ull * w * h, cudaMemcpyDeviceToHost, st));
-    CGS_TRY(cudaStreamSynchronize(st));
-    return CGS_OK;
-}
-
-int cgs_render_running(cgs_scene* s)
-{
-    if (!s) return 0;
-    return cudaEventQuery(s->finished) == cudaErrorNotReady ? 1 : 0;
-}
-
 int cgs_scene_counters(cgs_scene* s, cgs_counters* out)
 {
     if (!s || !out) return CGS_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(s->mu);
+    std::memset(out, 0, sizeof *out);
+    if (!s->lastCounters) return CGS_OK;
     CGS_TRY(cudaSetDevice(s->device));
-    if (!s->counters.p) { std::memset(out, 0, sizeof *out); return CGS_OK; }
     CGS_TRY(cudaStreamSynchronize(s->lastStream));
     Counters c;
-    CGS_TRY(cudaMemcpy(&c, s->counters.p, sizeof c, cudaMemcpyDeviceToHost));
-    std::memset(out, 0, sizeof *out);
+    CGS_TRY(cudaMemcpy(&c, s->lastCounters, sizeof c, cudaMemcpyDeviceToHost));
     out->rays = c.rays; out->nodes = c.nodes; out->hash_lookups = c.hashLookups; out->candidates = c.candidates;
     out->iterations = c.iterations; out->device_errors = c.errors; out->kernel_launches = uint64_t(s->launches);
-    return CGS_OK;
-}
-
-int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t dcap, uint32_t* table,
-                           uint32_t tcap, uint32_t params[5], void* stream)
-{
-    if (!keys || !disp || !table || !params || n == 0) return CGS_ERR_INVALID_ARGUMENT;
-    if (dcap < displ_size(n) || tcap < table_capacity(n)) return CGS_ERR_INVALID_ARGUMENT;
-    cudaStream_t st = (cudaStream_t)stream;
-    size_t w32 = 0, w64 = 0;
-    hash_scratch_words(n, w32, w64);
-    uint32_t* s32 = nullptr;
-    unsigned long long* s64 = nullptr;
-    CGS_TRY(cudaMallocAsync(&s32, w32 * sizeof(uint32_t), st));
-    if (cudaMallocAsync(&s64, w64 * sizeof(unsigned long long), st) != cudaSuccess)
-    {
-        cudaFreeAsync(s32, st);
-        return CGS_ERR_OUT_OF_MEMORY;
-    }
-    HashScratch hs {};
-    hash_scratch_carve(hs, n, s32, s64);
-    uint32_t A[16], B[16];
-    hash_coefficients(n, A, B);
-    int r = hash_build_device(keys, n, A, B, disp, table, tcap, hs, params, st, nullptr);
-    cudaFreeAsync(s32, st);
-    cudaFreeAsync(s64, st);
-    cudaStreamSynchronize(st);
-    if (r == 4) return CGS_ERR_HASH_BUCKET_OVERFLOW;
-    if (r < 0) return CGS_ERR_CUDA;
-    if (r) return CGS_ERR_HASH_FAILED;
     return CGS_OK;
 }
 

@@ -1,0 +1,196 @@
+// scene_impl.h -- host-side structures of libcgspline_gb300.so shared by
+// scene.cu (store, BVH build, upload, perfect hash) and api.cu (queries,
+// rendering, serving).
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/cgspline.h"
+#include "kernels.h"
+
+namespace cgs {
+
+// ------------------------------------------------------------- host BVH --
+struct Box
+{
+    float lo[3] = {INFINITY, INFINITY, INFINITY};
+    float hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    void inflate(const float p[3])
+    {
+        for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); }
+    }
+    void inflate(const Box& b) { inflate(b.lo); inflate(b.hi); }
+};
+
+struct Element { Box bounds; float centroid[3]; uint32_t index; };
+struct Node { Box leftBox, rightBox; uint32_t left, right; };
+
+// BVH::build / split / wrap (src/rt/BVH.cpp:9-108), see scene.cu.
+struct HostBVH
+{
+    std::vector<Node> nodes;
+    std::vector<uint32_t> keys, indices;
+    uint32_t perNode = 1;
+    bool emptyLeaf = false;
+    uint32_t wrap(Element* e, size_t count, uint32_t key);
+    uint32_t split(Element* e, size_t count, uint32_t key);
+    void build(std::vector<Element>& el);
+};
+
+struct Surface
+{
+    std::vector<float> points;   // 4 per point
+    std::vector<uint32_t> indices;
+    HostBVH bvh;
+    uint32_t patchCount() const { return uint32_t(indices.size() / 16); }
+};
+
+struct Object
+{
+    uint32_t surface, group;
+    float l2w[16], w2l[16];
+    cgs_material material;
+    std::vector<uint32_t> patchMaterial;
+    std::vector<cgs_material> materials;
+};
+
+// A group is one scene of the store: its objects, its object-level BVH, its
+// lights and environment (rt::Scene, src/rt/Scene.h:97-159).
+struct Group
+{
+    std::vector<uint32_t> objects;  // global object ids
+    std::vector<cgs_light> lights;
+    float background[3] = {0.1f, 0.1f, 0.1f};
+    float ambient[3] = {0.1f, 0.1f, 0.1f};
+    HostBVH top;
+    bool touched = false;  // objects, lights or environment were set
+};
+
+template<class T> struct DBuf
+{
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t reserve(size_t count)
+    {
+        if (count <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr; n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+inline int cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return CGS_OK;
+    if (e == cudaErrorMemoryAllocation) return CGS_ERR_OUT_OF_MEMORY;
+    return CGS_ERR_CUDA;
+}
+
+#define CGS_TRY(expr)                                  \
+    do {                                               \
+        cudaError_t _e = (expr);                       \
+        if (_e != cudaSuccess) return cuda_status(_e); \
+    } while (0)
+
+// Device buffers of one in-flight render batch (wavefront queues, engine
+// scratch, request table, counters).  A scene owns one; the server owns one
+// per concurrently running batch.
+struct RenderSlot
+{
+    WavefrontBuffers wb {};
+    DBuf<float> ray0, ray1, shadow, contrib, base, accum, hitF;
+    DBuf<uint32_t> smp0, smp1, grp0, grp1, dep0, dep1, count, shadowSlot, shadowGroup, engine;
+    DBuf<int32_t> visible, hitI, occluded;
+    DBuf<DevRequest> req;
+    DBuf<Counters> counters;
+    uint32_t engineCapacity = 0;
+    int ensure(uint32_t samples, uint32_t lights, uint32_t nreq);
+    void release();
+    static uint64_t bytes_for(uint32_t samples, uint32_t lights);
+};
+
+}  // namespace cgs
+
+struct cgs_scene
+{
+    int device = 0;
+    std::mutex mu;
+    std::vector<cgs::Surface> surfaces;
+    std::vector<cgs::Object> objects;
+    std::vector<cgs::Group> groups;
+    uint32_t current = 0;  // group receiving add_object / set_lights / set_environment
+    bool bvhBuilt = false, uploaded = false, hashed = false;
+
+    // device side
+    cgs::DBuf<float4> patches, nodes;
+    cgs::DBuf<uint32_t> indices, tables, disps, patchBase, patchMaterial, keys, groupTop;
+    cgs::DBuf<uint2> groupLights;
+    cgs::DBuf<float> groupEnv;
+    cgs::DBuf<cgs::DevBVH> bvhs;
+    cgs::DBuf<cgs::DevObject> dobjects;
+    cgs::DBuf<cgs::DevMaterial> materials;
+    cgs::DBuf<cgs::DevLight> dlights;
+    std::vector<cgs::DevBVH> hbvh;
+    std::vector<uint32_t> tableCap;  // per BVH
+    cgs::DBuf<uint32_t> scratch32;
+    cgs::DBuf<unsigned long long> scratch64;
+    cgs::DBuf<cgs::Counters> counters;
+
+    // query staging and engine scratch
+    cgs::DBuf<float> rayStage, hitF;
+    cgs::DBuf<int32_t> hitI;
+    cgs::DBuf<uint32_t> groupStage, engine;
+    uint32_t engineCapacity = 0;
+
+    // rendering
+    cgs::RenderSlot slot;
+    cgs::DBuf<uint32_t> fbStage;
+    cgs::DBuf<float> linStage;
+    cudaEvent_t finished = nullptr;
+    cudaStream_t lastStream = nullptr;
+    cgs::Counters* lastCounters = nullptr;
+    int launches = 0;
+
+    cgs::DevScene dev() const;
+    // bvhs: surfaces 0..S-1, then one object-level BVH per group
+    const cgs::HostBVH& bvh(uint32_t which) const
+    {
+        return which < surfaces.size() ? surfaces[which].bvh : groups[which - surfaces.size()].top;
+    }
+    uint32_t nbvh() const { return uint32_t(surfaces.size() + groups.size()); }
+    uint32_t maxLights() const
+    {
+        size_t m = 1;
+        for (const auto& g : groups) m = std::max(m, g.lights.size());
+        return uint32_t(m);
+    }
+    ~cgs_scene();
+};
+
+namespace cgs {
+
+void camera_setup(const cgs_camera& c, uint32_t w, uint32_t h, int flip, CameraSetup& s);
+uint32_t table_capacity(uint32_t n);
+uint32_t displ_size(uint32_t n);
+void hash_coefficients(uint32_t n, uint32_t A[16], uint32_t B[16]);
+int ensure_engine(cgs_scene* sc, uint32_t capacity);
+inline bool valid_query(int method, int precision)
+{
+    return (method == 0 || method == 1) && precision >= 0 && precision <= 2;
+}
+// Fill `out` (device request table of `slot`) and the batch description for
+// n requests; validates them.  Returns a status.
+int prepare_batch(cgs_scene* sc, const cgs_render_request* reqs, uint32_t n, const cgs_render_options* opt,
+                  std::vector<DevRequest>& host, RenderBatch& b);
+int run_batch(cgs_scene* sc, RenderSlot& slot, const std::vector<DevRequest>& host, RenderBatch& b, int schedule,
+              cudaStream_t stream, int* launches);
+
+}  // namespace cgs

@@ -55,22 +55,46 @@ def _material(m) -> _capi.Material:
 
 
 class GpuScene:
-    """A scene resident on one GPU: surfaces, objects, lights, BVHs and hash tables."""
+    """Scenes resident on one GPU: surfaces, objects, lights, BVHs and hash tables.
+
+    `scene` is one scenes.Scene or a list of them; scene k of a list becomes
+    group k of the store (its own object-level BVH, lights and environment,
+    sharing the patch and BVH arrays with the others)."""
 
     def __init__(self, scene, device: int = 0, build: bool = True, stream=None):
         self.lib = _capi.load()
-        self.scene = scene
+        self.scenes = list(scene) if isinstance(scene, (list, tuple)) else [scene]
+        self.scene = self.scenes[0]
         self.device = device
         h = C.c_void_p()
         check(self.lib.cgs_scene_create(C.byref(h), device), "cgs_scene_create")
         self.h = h
         self._keep = []
+        self.surface_base = []
+        for g, sc in enumerate(self.scenes):
+            if g > 0:
+                gid = C.c_uint32()
+                check(self.lib.cgs_scene_add_group(self.h, C.byref(gid)), "cgs_scene_add_group")
+                assert gid.value == g
+            self._add(sc)
+        if build:
+            self.build(stream)
+
+    @property
+    def groups(self) -> int:
+        return len(self.scenes)
+
+    def _add(self, scene):
+        first = None
         for s in scene.surfaces:
             pts = np.ascontiguousarray(s.points, np.float32)
             idx = np.ascontiguousarray(s.indices, np.uint32)
             sid = C.c_uint32()
             check(self.lib.cgs_scene_add_surface(self.h, _np_ptr(pts), pts.shape[0], _np_ptr(idx), idx.size,
                                                  C.byref(sid)), "cgs_scene_add_surface")
+            first = sid.value if first is None else first
+        base = first if first is not None else 0
+        self.surface_base.append(base)
         for o in scene.objects:
             l2w = np.ascontiguousarray(o.local2world, np.float32)
             w2l = np.ascontiguousarray(o.world2local, np.float32)
@@ -82,7 +106,7 @@ class GpuScene:
                 mats, nm = arr, len(o.materials)
                 self._keep.append(arr)
             oid = C.c_uint32()
-            check(self.lib.cgs_scene_add_object(self.h, o.surface, _np_ptr(l2w), _np_ptr(w2l),
+            check(self.lib.cgs_scene_add_object(self.h, base + o.surface, _np_ptr(l2w), _np_ptr(w2l),
                                                 C.byref(_material(o.material)), _np_ptr(pm),
                                                 C.cast(mats, C.c_void_p) if mats is not None else None, nm,
                                                 C.byref(oid)), "cgs_scene_add_object")
@@ -90,10 +114,9 @@ class GpuScene:
         bg = np.asarray(scene.background, np.float32)
         amb = np.asarray(scene.ambient, np.float32)
         check(self.lib.cgs_scene_set_environment(self.h, _np_ptr(bg), _np_ptr(amb)), "cgs_scene_set_environment")
-        if build:
-            self.build(stream)
 
     def set_lights(self, lights):
+        """Lights of the group being added (the last group)."""
         arr = (_capi.Light * max(1, len(lights)))()
         for k, l in enumerate(lights):
             arr[k] = _capi.Light((C.c_float * 3)(*l.color), l.strength, (C.c_float * 3)(*l.position), l.range,
@@ -124,7 +147,7 @@ class GpuScene:
         return int(b.value)
 
     def bvh(self, which: int):
-        """Export one BVH: which = surface id, or -1 for the object level."""
+        """Export one BVH: which = surface id, or -1-g for the object level of group g."""
         sz = np.zeros(5, np.uint32)
         check(self.lib.cgs_bvh_sizes(self.h, which, _np_ptr(sz)), "cgs_bvh_sizes")
         nodes = np.zeros((int(sz[0]), 14), np.uint32)
@@ -144,11 +167,13 @@ class GpuScene:
         return {k: int(getattr(c, k)) for k, _ in _capi.Counters._fields_}
 
     # rt::intersect / BVH::hashIntersect over a batch of rays
-    def intersect(self, rays, method=CLIP, precision=FP32, tol=DEFAULT_TOL, any_hit=False, stream=None, out=None):
-        """rays: (7, n) float32 torch CUDA tensor (ox oy oz dx dy dz tmax) or numpy array (host path).
+    def intersect(self, rays, method=CLIP, precision=FP32, tol=DEFAULT_TOL, any_hit=False, stream=None, out=None,
+                  group=None):
+        """rays: (7, n) float32 torch CUDA tensor (ox oy oz dx dy dz tmax) or numpy array (host path);
+        group: per-ray group ids (same kind as rays; None = group 0).
         Returns dict t, u, v, patch, object (patch = -1 on a miss)."""
         if isinstance(rays, np.ndarray):
-            return self._intersect_host(rays, method, precision, tol, any_hit, stream)
+            return self._intersect_host(rays, method, precision, tol, any_hit, stream, group)
         torch = _torch()
         assert rays.is_cuda and rays.dtype == torch.float32 and rays.dim() == 2 and rays.shape[0] == 7
         rays = rays.contiguous()
@@ -158,18 +183,28 @@ class GpuScene:
             io = torch.empty((2, n), dtype=torch.int32, device=rays.device)
         else:
             fo, io = out
-        r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)])
+        gp = None
+        if group is not None:
+            group = group.to(device=rays.device, dtype=torch.int32).contiguous()
+            assert group.numel() == n
+            gp = group.data_ptr()
+        r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)], gp)
         h = _capi.Hits(fo[0].data_ptr(), fo[1].data_ptr(), fo[2].data_ptr(), io[0].data_ptr(), io[1].data_ptr())
         check(self.lib.cgs_intersect(self.h, C.byref(r), n, method, precision, tol, int(any_hit), C.byref(h),
                                      _stream_handle(stream)), "cgs_intersect")
         return dict(t=fo[0], u=fo[1], v=fo[2], patch=io[0], object=io[1])
 
-    def _intersect_host(self, rays, method, precision, tol, any_hit, stream):
+    def _intersect_host(self, rays, method, precision, tol, any_hit, stream, group=None):
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[1]
         fo = np.zeros((3, n), np.float32)
         io = np.zeros((2, n), np.int32)
-        r = _capi.Rays(*[rays[k].ctypes.data for k in range(7)])
+        gp = None
+        if group is not None:
+            group = np.ascontiguousarray(group, np.uint32)
+            assert group.size == n
+            gp = group.ctypes.data
+        r = _capi.Rays(*[rays[k].ctypes.data for k in range(7)], gp)
         h = _capi.Hits(fo[0].ctypes.data, fo[1].ctypes.data, fo[2].ctypes.data, io[0].ctypes.data, io[1].ctypes.data)
         check(self.lib.cgs_intersect_host(self.h, C.byref(r), n, method, precision, tol, int(any_hit), C.byref(h),
                                           _stream_handle(stream) if stream is not None else None),
@@ -190,7 +225,7 @@ def do_bezier_clipping(scene: GpuScene, surface: int, rays, patch_ids, t=None, t
     v = torch.zeros(n, dtype=torch.float32, device=dev)
     found = torch.zeros(n, dtype=torch.int32, device=dev)
     pid = patch_ids.to(torch.int32).contiguous()
-    r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)])
+    r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)], None)
     h = _capi.Hits(tt.data_ptr(), u.data_ptr(), v.data_ptr(), found.data_ptr(), None)
     check(scene.lib.cgs_patch_intersect(scene.h, surface, C.byref(r), _ptr(pid), n, method, tol, C.byref(h),
                                         _stream_handle(stream)), "cgs_patch_intersect")
@@ -232,6 +267,38 @@ class Frame:
         return d.reshape(self.height, self.width, 4)
 
 
+@dataclasses.dataclass
+class Request:
+    """One render request of a batch: `spp` jittered samples per pixel of a
+    width x height image of group `group`; outputs are device tensors
+    (framebuffer (h, w) int32 packed RGBA8 sRGB, linear (h, w, 3) float32)."""
+    group: int
+    camera: object
+    width: int
+    height: int
+    spp: int = 1
+    recursion_depth: int = -1
+    framebuffer: object = None
+    linear: object = None
+
+    @classmethod
+    def alloc(cls, group, camera, width, height, spp=1, recursion_depth=-1, linear=False, device=0):
+        torch = _torch()
+        fb = torch.zeros((height, width), dtype=torch.int32, device=f"cuda:{device}")
+        lin = torch.zeros((height, width, 3), dtype=torch.float32, device=f"cuda:{device}") if linear else None
+        return cls(group, camera, width, height, spp, recursion_depth, fb, lin)
+
+    def c(self) -> _capi.RenderRequest:
+        return _capi.RenderRequest(self.group, camera_struct(self.camera), self.width, self.height, self.spp,
+                                   self.recursion_depth,
+                                   self.framebuffer.data_ptr() if self.framebuffer is not None else None,
+                                   self.linear.data_ptr() if self.linear is not None else None)
+
+    def rgba(self):
+        d = self.framebuffer.contiguous().cpu().numpy().view(np.uint8)
+        return d.reshape(self.height, self.width, 4)
+
+
 def camera_struct(cam) -> _capi.Camera:
     return _capi.Camera((C.c_float * 4)(*cam.rotation), (C.c_float * 3)(*cam.position), (C.c_float * 3)(*cam.scale),
                         cam.fovy)
@@ -261,6 +328,17 @@ class RayTracer:
                                        _np_ptr(fb), _np_ptr(lin),
                                        _stream_handle(stream) if stream is not None else None), "cgs_render_host")
         return fb, lin
+
+    def render_batch(self, requests, scene: GpuScene, stream=None):
+        """Render a list of Request objects of any groups of `scene` together
+        (one wavefront for all of them, or one launch each with PLAIN)."""
+        self._scene = scene
+        arr = (_capi.RenderRequest * len(requests))()
+        for k, q in enumerate(requests):
+            arr[k] = q.c()
+        o = self.options.c()
+        check(self.lib.cgs_render_batch(scene.h, arr, len(requests), C.byref(o), _stream_handle(stream)),
+              "cgs_render_batch")
 
     def running(self) -> bool:
         return bool(self._scene is not None and self.lib.cgs_render_running(self._scene.h))

@@ -301,6 +301,110 @@ def camera_c2() -> Camera:
 
 
 # ---------------------------------------------------------- evaluation ---
+# ----------------------------------------------------------------- C4 ----
+def cube_sphere_surface(radius: float = 1.0, n: int = 2, sigma: float = 0.02, seed: int = 0) -> Surface:
+    """Sphere as the six faces of a cube, each an n x n grid of bicubic Bezier
+    patches over a (3n+1)^2 control grid: the face's uniform grid points
+    pushed onto the sphere.  Face edges use the same grid values on both
+    faces, so the net is watertight; the four interior control points of
+    every patch then move radially by sigma * N(0,1) (edges stay C0)."""
+    g = 3 * n + 1
+    a = np.linspace(-1.0, 1.0, g)
+    A, B = np.meshgrid(a, a, indexing="ij")  # [i along u][j along v]
+    one = np.ones_like(A)
+    faces = [(one, A, B), (-one, B, A), (A, one, B), (B, -one, A), (A, B, one), (B, A, -one)]
+    rng = SplitMix64(seed)
+    inter = (np.arange(g)[:, None] % 3 != 0) & (np.arange(g)[None, :] % 3 != 0)
+    pts, idx = [], []
+    for f, (x, y, z) in enumerate(faces):
+        ln = np.sqrt(x * x + y * y + z * z)
+        nrm = np.stack([x / ln, y / ln, z / ln], -1)
+        r = np.full((g, g), radius)
+        r[inter] = radius + sigma * rng.normal(int(inter.sum()))
+        P = nrm * r[..., None]
+        pts.append(np.concatenate([P.reshape(-1, 3), np.ones((g * g, 1))], axis=1))
+        base = f * g * g
+        for pb in range(n):
+            for pa in range(n):
+                for j in range(4):
+                    for i in range(4):
+                        idx.append(base + (3 * pa + i) * g + (3 * pb + j))
+    return Surface(np.concatenate(pts).astype(np.float32), np.asarray(idx, dtype=np.uint32))
+
+
+def _rotation(q):
+    """3x3 rotation (row-major) of a unit quaternion (x, y, z, w)."""
+    x, y, z, w = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def _transforms(R, scale, t):
+    """Column-major local->world (T R S, uniform scale) and its inverse."""
+    M = np.eye(4)
+    M[:3, :3] = R * scale
+    M[:3, 3] = t
+    W = np.eye(4)
+    W[:3, :3] = R.T * (1.0 / scale)
+    W[:3, 3] = -(W[:3, :3] @ np.asarray(t))
+    return M.T.reshape(16).astype(np.float32), W.T.reshape(16).astype(np.float32)
+
+
+def scene_c4(index: int, seed: int = 4, min_patches: int = 256, max_patches: int = 65536) -> Scene:
+    """Scene `index` of the 64-scene batching workload: a seeded random union
+    of 8..64 displaced cube-spheres and tori (the torus of scene_c2 on a
+    coarser grid) with random rotations, uniform scales in [0.5, 1.5] and
+    positions in [-4, 4]^3; the total patch count is log-uniform in
+    [min_patches, max_patches]; per-object PBR materials; two point lights."""
+    rng = SplitMix64(seed * 1000003 + index)
+    u = rng.uniform(1)[0]
+    total = float(min_patches) * (float(max_patches) / float(min_patches)) ** u
+    k = 8 + int(rng.integers(1, 57)[0])
+    per = total / k
+    surfaces, objects = [], []
+    for o in range(k):
+        kind, sc, cr, metal, rough = rng.uniform(5)
+        qv = rng.normal(4)
+        qv = qv / np.sqrt(qv @ qv)
+        pos = rng.uniform(3, -4.0, 4.0)
+        sseed = int(rng.u64(1)[0] >> np.uint64(12))
+        if kind < 0.5:
+            n = max(1, int(np.floor(np.sqrt(per / 6.0) + 0.5)))
+            surf = cube_sphere_surface(1.0, n, 0.03, sseed)
+        else:
+            nv = max(3, int(np.floor(np.sqrt(per / 2.0) + 0.5)))
+            surf = torus_surface(1.0, 0.35, 2 * nv, nv, 0.02, sseed)
+        surfaces.append(surf)
+        l2w, w2l = _transforms(_rotation(qv), 0.5 + sc, pos)
+        col = (0.3 + 0.6 * cr, 0.3 + 0.6 * (1.0 - cr), 0.5)
+        m = Material(tuple(float(np.float32(c)) for c in col), (0.9, 0.85, 0.8) if metal < 0.3 else (0.04, 0.04, 0.04),
+                     1.0 if metal < 0.3 else 0.0, float(np.float32(0.1 + 0.8 * rough)))
+        objects.append(Object(o, l2w, w2l, m))
+    lp = rng.uniform(6, -1.0, 1.0).reshape(2, 3)
+    lights = []
+    for v in lp:
+        v = v / np.sqrt(v @ v) * 14.0
+        lights.append(Light((120.0, 120.0, 120.0), 1.0, tuple(float(np.float32(c)) for c in v), 0.0, (0.0, 0.0, -1.0),
+                            math.pi))
+    return Scene(surfaces, objects, lights, name=f"union{index}")
+
+
+def camera_c4(index: int, seed: int = 4):
+    """Camera of scene_c4(index): looks at the origin from distance 13 in a
+    seeded direction, 50 degree fovy; the square resolution side is
+    64 * 2^U(0,4) rounded to a multiple of 8 (64^2..1024^2 primary rays,
+    log-uniform)."""
+    rng = SplitMix64(seed * 7919 + index + 17)
+    d = rng.normal(3)
+    d = d / np.sqrt(d @ d) * 13.0
+    side = int(np.floor(64.0 * 2.0 ** (4.0 * rng.uniform(1)[0]) / 8.0 + 0.5)) * 8
+    up = (0.0, 0.0, 1.0) if abs(d[2]) < 12.0 else (0.0, 1.0, 0.0)
+    cam = Camera(look_at(d, (0.0, 0.0, 0.0), up), tuple(float(np.float32(c)) for c in d), (1, 1, 1),
+                 float(np.float32(math.radians(50.0))))
+    return cam, side
+
+
 def bernstein(t: np.ndarray):
     t = np.asarray(t, np.float64)
     s = 1.0 - t

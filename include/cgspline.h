@@ -88,7 +88,8 @@ typedef struct cgs_render_options {
 typedef struct cgs_rays {
     const float* ox; const float* oy; const float* oz;
     const float* dx; const float* dy; const float* dz;
-    const float* tmax;   /* ray.max (src/rt/Intersection.h:16-24) */
+    const float* tmax;     /* ray.max (src/rt/Intersection.h:16-24) */
+    const uint32_t* group; /* nullable: the scene group of each ray (default group 0) */
 } cgs_rays;
 
 /* Closest-hit results (src/rt/Intersection.h:28-34); patch = object = -1 on a miss.
@@ -106,7 +107,8 @@ typedef struct cgs_counters {
     uint64_t hash_lookups;    /* stackless backtracks through the perfect hash */
     uint64_t candidates;      /* (ray, patch) pairs searched */
     uint64_t iterations;      /* clip / subdivision iterations */
-    uint64_t device_errors;   /* bounded-loop or stack-limit exits */
+    uint64_t device_errors;   /* bit mask: 1 clip stack full, 2 clip iteration limit,
+                                 4 traversal step limit, 8 ray of an unknown group */
     uint64_t kernel_launches;
 } cgs_counters;
 
@@ -129,8 +131,18 @@ int cgs_scene_add_object(cgs_scene* scene, uint32_t surface, const float local2w
                          const uint32_t* patch_material, const cgs_material* materials,
                          uint32_t nmaterials, uint32_t* object_id);
 
+/* Lights, background and ambient colour of the current group (rt::Scene::lights,
+ * backgroundColor, ambientLight, src/rt/Scene.h:113-119). */
 int cgs_scene_set_lights(cgs_scene* scene, const cgs_light* lights, uint32_t n);
 int cgs_scene_set_environment(cgs_scene* scene, const float background[3], const float ambient[3]);
+
+/* Groups: several independent scenes (each an rt::Scene with its own objects,
+ * object-level BVH, lights and environment) resident in one store, so that
+ * one launch can trace rays of different scenes.  A store starts with group 0
+ * current; cgs_scene_add_group makes a new group current (or returns the
+ * current one if nothing was added to it yet).  Objects, lights and
+ * environment calls apply to the current group; surfaces are shared. */
+int cgs_scene_add_group(cgs_scene* scene, uint32_t* group_id);
 
 /* BVH::build for every surface (BezierSurface::buildBVH, src/rt/Primitive.cu:199-220)
  * and the object level (Scene::buildBVH, src/rt/Scene.cu:218-232): host median
@@ -149,7 +161,7 @@ int cgs_scene_build(cgs_scene* scene, void* stream);
 /* Device bytes held by a built scene. */
 int cgs_scene_footprint(const cgs_scene* scene, uint64_t* bytes);
 
-/* which = surface id, or -1 for the object-level BVH.
+/* which = surface id, or -1 - g for the object-level BVH of group g.
  * sizes = nodes, indices, table size, displacement size, keys. */
 int cgs_bvh_sizes(const cgs_scene* scene, int32_t which, uint32_t sizes[5]);
 /* nodes: 14 uint32 per node = leftBox lo,hi; rightBox lo,hi (float bits); left; right|first
@@ -193,6 +205,28 @@ int cgs_render(cgs_scene* scene, const cgs_camera* camera, uint32_t width, uint3
 int cgs_render_host(cgs_scene* scene, const cgs_camera* camera, uint32_t width, uint32_t height,
                     const cgs_render_options* options, uint32_t* framebuffer, float* linear_rgb,
                     void* stream);
+
+/* A render request of a batch: `spp` jittered primary samples per pixel,
+ * averaged (sample s offset by (s/spp, vdc(s)) as src/rt/RayTracer.cu:226-236;
+ * spp = 1 is the unjittered pixel centre of the reference's default path). */
+typedef struct cgs_render_request {
+    uint32_t group;
+    cgs_camera camera;
+    uint32_t width, height, spp;
+    int recursion_depth;
+    uint32_t* framebuffer;   /* device RGBA8 sRGB, row stride = width (nullable) */
+    float* linear_rgb;       /* device (height, width, 3) (nullable) */
+} cgs_render_request;
+
+/* Render n requests of any groups together.  options supplies eps, method,
+ * precision, tol and schedule; a request's negative recursion_depth takes
+ * options->recursion_depth.
+ * With CGS_SCHED_WAVEFRONT all samples of all requests share one wavefront;
+ * with CGS_SCHED_PLAIN each request is its own launch (the plain
+ * one-request-per-launch path).  Asynchronous; CGS_ERR_BUSY while the
+ * scene's previous render is in flight. */
+int cgs_render_batch(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,
+                     const cgs_render_options* options, void* stream);
 
 /* RayTracer::running (src/rt/RayTracer.h:45-48): 1 while a render is in flight. */
 int cgs_render_running(cgs_scene* scene);

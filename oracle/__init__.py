@@ -61,6 +61,8 @@ def lib():
                                  P, P, P, C.c_int, P]
         L.ora_render_rows.argtypes = [P, fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_float,
                                       C.c_int, C.c_float, P, P, P, C.c_int, P]
+        L.ora_render_spp.argtypes = [P, fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_int,
+                                     C.c_float, P, P, C.c_int]
         L.ora_intersect_stats.argtypes = [P, fp, C.c_uint64, C.c_int, C.c_float, C.c_int, u32, C.c_int]
         L.ora_camera_rays.argtypes = [fp, C.c_uint32, C.c_uint32, fp]
         L.ora_patch_intersect.argtypes = [fp, u32, fp, C.c_float, C.c_int, P, P, P]
@@ -170,6 +172,17 @@ class OracleScene:
         return dict(rgb=rgb, packed=packed, primary=int(counts[0]), bounce=int(counts[1]),
                     shadow=int(counts[2]), seconds=float(secs[0]))
 
+
+    def render_spp(self, camera, w, h, spp, depth=1, eps=1e-4, method=CLIP_HOST, tol=2.0 ** -12, nthreads=None):
+        """spp jittered samples per pixel, averaged (linear rgb and packed sRGB)."""
+        L = lib()
+        rgb = np.zeros((h, w, 3), np.float32)
+        packed = np.zeros((h, w), np.uint32)
+        nt = nthreads or os.cpu_count() or 1
+        r = L.ora_render_spp(self.h, camera.packed(), w, h, spp, depth, eps, method, tol, _ptr(rgb), _ptr(packed), nt)
+        if r:
+            raise RuntimeError(f"ora_render_spp failed ({r})")
+        return dict(rgb=rgb, packed=packed)
 
     def render_rows(self, camera, w, h, row0, row_step, depth=1, eps=1e-4, method=CLIP_HOST, tol=2.0 ** -12,
                     nthreads=None):

@@ -1637,6 +1637,57 @@ int ora_render_rows(void* s_, const float* camera11, uint32_t w, uint32_t h, uin
     return 0;
 }
 
+// Van der Corput radical inverse in base 2 (src/rt/PBR.h:143-157).
+static float vdc(uint32_t i)
+{
+    i = (i << 16) | (i >> 16);
+    i = ((i & 0x55555555u) << 1) | ((i & 0xAAAAAAAAu) >> 1);
+    i = ((i & 0x33333333u) << 2) | ((i & 0xCCCCCCCCu) >> 2);
+    i = ((i & 0x0F0F0F0Fu) << 4) | ((i & 0xF0F0F0F0u) >> 4);
+    i = ((i & 0x00FF00FFu) << 8) | ((i & 0xFF00FF00u) >> 8);
+    return float(i) * 0x1p-32f;
+}
+
+// spp jittered samples per pixel, averaged: sample s of pixel (i, j) traces
+// the primary ray through (i + s/spp, j + vdc(s)) (the sampled path's jitter,
+// src/rt/RayTracer.cu:226-236); spp = 1 is the unjittered pixel of ora_render.
+// The sum runs over s in order and is scaled by 1/spp before clamping.
+int ora_render_spp(void* s_, const float* camera11, uint32_t w, uint32_t h, uint32_t spp, int depth, float eps,
+                   int method, float tol, float* out_rgb, uint32_t* out_packed, int nthreads)
+{
+    if (spp == 0) return -2;
+    auto* s = static_cast<Scene*>(s_);
+    if (!s->built) return -1;
+    Camera cam;
+    std::memcpy(cam.rot, camera11, 4 * sizeof(float));
+    std::memcpy(cam.pos, camera11 + 4, 3 * sizeof(float));
+    std::memcpy(cam.scale, camera11 + 7, 3 * sizeof(float));
+    cam.fovy = camera11[10];
+    RenderOpts op; op.depth = depth; op.eps = eps; op.method = method; op.tol = tol;
+    Renderer R(*s, cam, w, h, op);
+    parallel_for(uint64_t(w) * h, std::max(1, nthreads), [&](uint64_t px, int) {
+        const uint32_t i = uint32_t(px % w), j = uint32_t(px / w);
+        V3<float> c {0, 0, 0};
+        for (uint32_t k = 0; k < spp; k++)
+        {
+            float x = float(i), y = float(j);
+            if (spp > 1) { x = x + float(k) * (1.0f / float(spp)); y = y + vdc(k); }
+            Ray<float> pr {R.camPos, R.pixelRayDirection(x, y), INFINITY};
+            V3<float> ck = R.trace(pr, V3<float>{1, 1, 1}, depth, nullptr, nullptr);
+            c = {c.x + ck.x, c.y + ck.y, c.z + ck.z};
+        }
+        if (spp > 1)
+        {
+            const float inv = 1.0f / float(spp);
+            c = {c.x * inv, c.y * inv, c.z * inv};
+        }
+        c = {std::clamp(c.x, 0.0f, 1.0f), std::clamp(c.y, 0.0f, 1.0f), std::clamp(c.z, 0.0f, 1.0f)};
+        if (out_rgb) { out_rgb[3 * px] = c.x; out_rgb[3 * px + 1] = c.y; out_rgb[3 * px + 2] = c.z; }
+        if (out_packed) out_packed[px] = srgb8(c.x) | (srgb8(c.y) << 8) | (srgb8(c.z) << 16) | 0xFF000000u;
+    });
+    return 0;
+}
+
 // Primary ray directions for a camera (the same set-up as ora_render), SoA (7, w*h).
 int ora_camera_rays(const float* camera11, uint32_t w, uint32_t h, float* rays)
 {

@@ -1,0 +1,170 @@
+"""GPU tests of scene groups (many resident scenes in one store) and batched
+rendering through cgs_render_batch.
+
+Bars: a group's BVHs and hash tables equal those of the same scene stored
+alone (bit-exact); per-ray group queries agree with the oracle of each scene
+as the single-scene queries do; a request rendered inside a batch of other
+requests, groups and sizes is bit-identical to the same request rendered
+alone; spp > 1 matches the oracle's jittered average within the single-sample
+render tolerance.
+"""
+import numpy as np
+import pytest
+
+from cgspline_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    return torch
+
+
+@pytest.fixture(scope="module")
+def rt():
+    from cgspline_gb300 import rt
+    return rt
+
+
+@pytest.fixture(scope="module")
+def pair():
+    return [S.scene_c1(), S.scene_c2(nu=32, nv=32)]
+
+
+@pytest.fixture(scope="module")
+def store(rt, pair):
+    return rt.GpuScene(pair)
+
+
+@pytest.fixture(scope="module")
+def alone(rt, pair):
+    return [rt.GpuScene(s) for s in pair]
+
+
+@pytest.fixture(scope="module")
+def oracles(oracle_mod, pair):
+    return [oracle_mod.OracleScene(s) for s in pair]
+
+
+CAMS = [S.camera_c1, S.camera_c2]
+
+
+def test_group_bvhs_equal_single_scene_bvhs(store, alone, pair):
+    for g in range(2):
+        a = store.bvh(-1 - g)
+        b = alone[g].bvh(-1)
+        for k in ("nodes", "keys", "table", "disp"):
+            assert np.array_equal(a[k], b[k]), (g, k)
+        assert (a["A"], a["B"], a["N"], a["mask"]) == (b["A"], b["B"], b["N"], b["mask"])
+        # object ids of group g are global: offset by the objects of earlier groups
+        off = sum(len(p.objects) for p in pair[:g])
+        ia, ib = a["indices"].astype(np.int64), b["indices"].astype(np.int64)
+        leaf = ib != 0xFFFFFFFF
+        assert np.array_equal(ia[leaf], ib[leaf] + off) and np.array_equal(ia[~leaf], ib[~leaf])
+        base = store.surface_base[g]
+        for s in range(len(pair[g].surfaces)):
+            sa, sb = store.bvh(base + s), alone[g].bvh(s)
+            for k in ("nodes", "keys", "indices", "table", "disp"):
+                assert np.array_equal(sa[k], sb[k]), (g, s, k)
+
+
+def test_grouped_queries_match_each_scene(store, alone, oracles, oracle_mod, pair, torch):
+    rays = [oracle_mod.camera_rays(CAMS[g](), 96, 64) for g in range(2)]
+    allr = np.concatenate(rays, axis=1)
+    grp = np.concatenate([np.full(r.shape[1], g, np.uint32) for g, r in enumerate(rays)])
+    # interleave the groups so that warps mix scenes
+    perm = np.random.default_rng(5).permutation(allr.shape[1])
+    res = store.intersect(torch.from_numpy(allr[:, perm]).cuda(), group=torch.from_numpy(grp[perm].view(np.int32)))
+    res = {k: v.cpu().numpy() for k, v in res.items()}
+    inv = np.argsort(perm)
+    res = {k: v[inv] for k, v in res.items()}
+    start = 0
+    for g in range(2):
+        n = rays[g].shape[1]
+        one = {k: v.cpu().numpy() for k, v in alone[g].intersect(torch.from_numpy(rays[g]).cuda()).items()}
+        part = {k: v[start:start + n] for k, v in res.items()}
+        off = sum(len(p.objects) for p in pair[:g])
+        for k in ("t", "u", "v", "patch"):
+            assert np.array_equal(part[k], one[k]), (g, k)
+        hit = one["object"] >= 0
+        assert np.array_equal(part["object"][hit], one["object"][hit] + off)
+        o = oracles[g].intersect(rays[g])
+        assert np.array_equal(part["patch"] >= 0, o["patch"] >= 0)
+        start += n
+    # host entry point with per-ray groups gives the same
+    h = store.intersect(allr[:, perm], group=grp[perm])
+    h = {k: v[inv] for k, v in h.items()}
+    for k in res:
+        assert np.array_equal(h[k], res[k]), k
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_request_same_alone_and_in_mix(rt, store, torch, schedule):
+    specs = [(1, S.camera_c2(), 96, 54, 1, 1), (0, S.camera_c1(), 64, 64, 1, 0), (1, S.camera_c2(), 40, 30, 2, 2),
+             (0, S.camera_c1(), 33, 17, 3, 1), (1, S.camera_c2(), 128, 72, 1, 0)]
+    mix = [rt.Request.alloc(g, c, w, h, spp=s, recursion_depth=d, linear=True) for g, c, w, h, s, d in specs]
+    tracer = rt.RayTracer(rt.Options(schedule=schedule))
+    tracer.render_batch(mix, store)
+    torch.cuda.synchronize()
+    assert store.counters()["device_errors"] == 0
+    for (g, c, w, h, s, d), q in zip(specs, mix):
+        one = rt.Request.alloc(g, c, w, h, spp=s, recursion_depth=d, linear=True)
+        tracer.render_batch([one], store)
+        torch.cuda.synchronize()
+        assert torch.equal(one.linear, q.linear), (g, w, h, s, d)
+        assert torch.equal(one.framebuffer, q.framebuffer)
+
+
+def test_batch_groups_match_single_scene_renders(rt, store, alone, torch):
+    for g, cam in enumerate(CAMS):
+        q = rt.Request.alloc(g, cam(), 80, 48, recursion_depth=1, linear=True)
+        rt.RayTracer(rt.Options()).render_batch([q], store)
+        torch.cuda.synchronize()
+        fb, lin = rt.RayTracer(rt.Options(recursion_depth=1)).render_host(cam(), alone[g], 80, 48)
+        assert np.array_equal(q.linear.cpu().numpy(), lin)
+
+
+def test_schedules_agree_on_batches(rt, store, torch):
+    specs = [(1, S.camera_c2(), 64, 36, 2, 1), (0, S.camera_c1(), 48, 48, 1, 1)]
+    out = []
+    for schedule in (0, 1):
+        reqs = [rt.Request.alloc(g, c, w, h, spp=s, recursion_depth=d, linear=True) for g, c, w, h, s, d in specs]
+        rt.RayTracer(rt.Options(schedule=schedule)).render_batch(reqs, store)
+        torch.cuda.synchronize()
+        out.append([r.linear.cpu().numpy() for r in reqs])
+    for a, b in zip(*out):
+        assert np.abs(a - b).max() < 1e-5
+
+
+def test_spp_matches_oracle(rt, store, oracles, torch):
+    q = rt.Request.alloc(1, S.camera_c2(), 96, 54, spp=4, recursion_depth=1, linear=True)
+    rt.RayTracer(rt.Options()).render_batch([q], store)
+    torch.cuda.synchronize()
+    ro = oracles[1].render_spp(S.camera_c2(), 96, 54, 4, depth=1)
+    err = np.abs(q.linear.cpu().numpy() - ro["rgb"])
+    assert float(np.sqrt((err ** 2).mean())) < 5e-3
+    assert (err.max(axis=-1) > 0.05).mean() < 2e-3
+
+
+def test_invalid_batches_raise(rt, store, torch):
+    from cgspline_gb300._capi import CgsError
+    tracer = rt.RayTracer(rt.Options())
+    bad_group = rt.Request.alloc(7, S.camera_c1(), 8, 8)
+    with pytest.raises(CgsError) as e:
+        tracer.render_batch([bad_group], store)
+    assert e.value.status == 1
+    zero_spp = rt.Request.alloc(0, S.camera_c1(), 8, 8)
+    zero_spp.spp = 0
+    with pytest.raises(CgsError):
+        tracer.render_batch([zero_spp], store)
+    with pytest.raises(CgsError):
+        tracer.render_batch([], store)
+    # per-ray groups live on the device: a ray of an unknown group is a miss and sets error bit 8
+    rays = torch.zeros((7, 4), device="cuda")
+    rays[3] = 1.0
+    rays[6] = float("inf")
+    res = store.intersect(rays, group=torch.tensor([0, 9, 1, 2], dtype=torch.int32))
+    assert res["patch"].cpu().tolist()[1] == -1 and res["patch"].cpu().tolist()[3] == -1
+    assert store.counters()["device_errors"] == 8
