@@ -1,19 +1,25 @@
 """Benchmark of the ray--bicubic-patch path on GB300.
 
-Workload (one step = one frame): the seeded displaced torus (R=4, r=1,
-128x128 = 16,384 bicubic patches, radial displacement sigma 0.05 on interior
-control points), 1920x1080 primary rays plus one mirror bounce, Cook-Torrance
-PBR with two point lights and their shadow rays, Bezier clipping at the
-reference tolerance 2^-12 in FP32 followed by the FP64 Newton polish of every
-hit (so the metric's <= 1e-5 relative t error holds; it is verified on a seeded
-1% pixel subset against the FP64 oracle outside the timed region).
+Headline workload (one step = one frame): the seeded displaced torus (R=4,
+r=1, 128x128 = 16,384 bicubic patches, radial displacement sigma 0.05 on
+interior control points), 1920x1080 primary rays plus one mirror bounce,
+Cook-Torrance PBR with two point lights and their shadow rays, Bezier clipping
+at the reference tolerance 2^-12 in FP32 followed by the FP64 Newton polish
+of every hit, on the reference's BVH topology (bit-exact build).
 
-value  = total rays (primary + bounce + shadow) / device time of K frames, scene
-         resident in HBM, L2 flushed before every frame.
+value  = total rays (primary + bounce + shadow) / device time of K frames,
+         scene resident in HBM, L2 flushed before every frame.
 e2e    = the same through cgs_render_host (host framebuffer, copies inside the
          timed region).
---impl reference: the reference's CPU path (oracle/_ref if the reference
-         compiled, else the oracle's restatement) on all host cores.
+accuracy = max relative t error and hit/miss disagreement of the primary hits
+         of a seeded 1% pixel subset against the pure-FP64 GPU search (itself
+         held to the FP64 oracle by the test suite).
+Further objects: split_longest (the same frame on the longest-axis BVH
+build), precision (2^20 grazing rays), batching (64 scenes in one batch
+against 64 plain launches), serving (Poisson request streams through the
+continuous-batching server against the plain one-request-per-launch server).
+--impl reference: the reference's CPU path (the oracle's restatement of it)
+         on all host cores.
 """
 from __future__ import annotations
 
@@ -33,6 +39,7 @@ DEPTH = 1
 L2_BYTES = 129 * 1024 * 1024
 FP32_FLOPS_PER_CLK_SM = 256  # 128 FP32 lanes x FMA
 SMS = 152
+METRIC = "Mrays/s at <=1e-5 rel-t err vs FP64 (C2 torus 1080p + 1 bounce, PBR)"
 
 
 def parse():
@@ -43,9 +50,14 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--schedule", default="wavefront", choices=["wavefront", "plain"])
     ap.add_argument("--precision", default="polish64", choices=["fp32", "polish64"])
+    ap.add_argument("--split", default="reference", choices=["reference", "longest"],
+                    help="BVH split axis of the headline frame")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--quick", action="store_true", help="no plain-path comparison, no FP64 check")
+    ap.add_argument("--quick", action="store_true", help="headline frame only")
     ap.add_argument("--size", default=None, help="WxH of a smaller frame (profiling cases); default 1920x1080")
+    ap.add_argument("--no-batching", action="store_true", help="skip the 64-scene batching comparison")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson stream) comparison")
+    ap.add_argument("--no-precision", action="store_true", help="skip the grazing-ray precision comparison")
     return ap.parse_args()
 
 
@@ -121,7 +133,10 @@ def traffic_summary():
         return None
 
 
+# ----------------------------------------------------------- CPU legs --
 def cpu_leg(scene, camera, sample_rows=1):
+    """The oracle's restatement of the reference's CPU tracer on every host
+    core, over every sample_rows-th row of the frame."""
     import oracle
     o = oracle.OracleScene(scene)
     r = o.render_rows(camera, W, H, 0, sample_rows, depth=DEPTH)
@@ -133,45 +148,246 @@ def cpu_leg(scene, camera, sample_rows=1):
             "seconds": r["seconds"], "rays": rays}
 
 
-def reference_cpu_leg(scene, camera, rows):
-    """The reference's own CPU tracer when it compiled here (oracle/_ref), else the restatement."""
-    try:
-        from oracle import ref as R
-        if R.available():
-            res = R.render_rows(scene, camera, W, H, 0, rows, depth=DEPTH)
-            rays = res["primary"] + res["bounce"] + res["shadow"]
-            return {"value": rays / res["seconds"] / 1e6, "unit": "Mrays/s", "cores": res["threads"],
-                    "kind": "reference", "sample": f"every {rows} row(s) of the {W}x{H} frame, reference "
-                                                   f"CPURayTracer compiled from its own sources",
-                    "seconds": res["seconds"], "rays": rays}
-    except Exception:
-        pass
-    return cpu_leg(scene, camera, rows)
-
-
 def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU path on this host's cores (the
+    reference itself does not build here: its Ds dependency is absent), on
+    a bounded sample of rows of the headline frame per step."""
     from cgspline_gb300 import scenes
     if rank != 0:
         return
     scene, cam = scenes.scene_c2(), scenes.camera_c2()
     rows = 2
     for _ in range(args.warmup):
-        reference_cpu_leg(scene, cam, rows * 4)
+        cpu_leg(scene, cam, rows * 4)
     tot_rays, tot_s, leg = 0, 0.0, None
     for _ in range(args.steps):
-        leg = reference_cpu_leg(scene, cam, rows)
+        leg = cpu_leg(scene, cam, rows)
         tot_rays += leg["rays"]
         tot_s += leg["seconds"]
     v = tot_rays / tot_s / 1e6
-    line = {"metric": "Mrays/s at <=1e-5 rel-t err vs FP64 (C2 torus 1080p + 1 bounce, PBR)", "value": v,
-            "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced torus)", "impl": "reference",
+    line = {"metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced torus)",
+            "impl": "reference",
             "config": {"workload": f"torus 16384 patches, {W}x{H} primary + {DEPTH} bounce, PBR, 2 point lights, "
                                    f"CPU sample = every {rows} rows"},
             "cpu_baseline": {k: leg[k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "Mrays/s"},
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------- GPU legs --
+def timed(torch, stream, flush, fn, reps):
+    """Device ms of each of `reps` calls of fn(), L2 flushed before each."""
+    e0 = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    e1 = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    for k in range(reps):
+        flush.fill_(float(k))
+        e0[k].record(stream)
+        fn()
+        e1[k].record(stream)
+        e1[k].synchronize()
+    return [a.elapsed_time(b) for a, b in zip(e0, e1)]
+
+
+def accuracy_vs_fp64(rt, g, rays, prec, group=None):
+    """FP32 (+ polish) hits of `rays` against the pure-FP64 GPU search."""
+    import numpy as np
+    ref = {k: v.cpu().numpy() for k, v in g.intersect(rays, precision=rt.FP64, group=group).items()}
+    a = {k: v.cpu().numpy() for k, v in g.intersect(rays, precision=prec, group=group).items()}
+    hit_a, hit_r = a["patch"] >= 0, ref["patch"] >= 0
+    both = hit_a & hit_r
+    rel = np.abs(a["t"][both] - ref["t"][both]) / ref["t"][both]
+    return {"rays": int(rays.shape[1]), "max_rel_t_err": float(rel.max(initial=0.0)),
+            "rays_over_1e-5": int((rel > 1e-5).sum()), "hit_miss_disagreement": float((hit_a != hit_r).mean()),
+            "patch_disagreement": float((both & (a["patch"] != ref["patch"])).mean()),
+            "reference": "pure-FP64 GPU search"}
+
+
+def frame_leg(rt, torch, g, cam, tracer, frame, stream, flush, steps):
+    for _ in range(3):
+        tracer.render(frame, cam, g, stream)
+        torch.cuda.synchronize()
+    c = g.counters()
+    ms = timed(torch, stream, flush, lambda: tracer.render(frame, cam, g, stream), steps)
+    return c, ms
+
+
+def precision_leg(rt, scenes, torch, dev, g, scene, flush, n=1 << 20):
+    """2^20 seeded grazing rays (within 0.5 degrees of the tangent plane at
+    random points of the torus): FP32, FP32 + FP64 polish, and the full
+    precision form (FP32 + FP64 polish + FP64 fat-line bounds for near-grazing
+    candidates) against the pure-FP64 GPU search, with the throughput of each."""
+    import numpy as np
+    rays = torch.from_numpy(scenes.grazing_rays(scene.surfaces[0], n, seed=3)).to(dev)
+    stream = torch.cuda.current_stream()
+    out = {"rays": n, "workload": "2^20 grazing rays, torus 16384 patches, closest hit"}
+    res = {}
+    for name, prec in (("fp64", rt.FP64), ("fp32", rt.FP32), ("fp32_polish64", rt.FP32_POLISH64),
+                       ("fp32_graze64", rt.FP32_GRAZE64)):
+        g.intersect(rays, precision=prec)
+        torch.cuda.synchronize()
+        reps = 1 if prec == rt.FP64 else 3
+        holder = {}
+        ms = timed(torch, stream, flush, lambda: holder.update(r=g.intersect(rays, precision=prec)), reps)
+        res[name] = {k: v.cpu().numpy() for k, v in holder["r"].items()}
+        out[name] = {"Mrays_s": n / (sum(ms) / reps * 1e-3) / 1e6, "ms": sum(ms) / reps}
+    ref = res["fp64"]
+    for name in ("fp32", "fp32_polish64", "fp32_graze64"):
+        a = res[name]
+        both = (a["patch"] >= 0) & (ref["patch"] >= 0)
+        rel = np.abs(a["t"][both] - ref["t"][both]) / ref["t"][both]
+        out[name].update({"max_rel_t_err": float(rel.max(initial=0.0)),
+                          "rays_over_1e-5": int((rel > 1e-5).sum()),
+                          "hit_miss_disagreement": float(((a["patch"] >= 0) != (ref["patch"] >= 0)).mean()),
+                          "patch_disagreement": float((both & (a["patch"] != ref["patch"])).mean())})
+    out["fp64"]["hits"] = int((ref["patch"] >= 0).sum())
+    return out
+
+
+def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
+    """64 resident scenes (seeded unions of displaced cube-spheres and tori,
+    256..65,536 patches each), one request per scene with 64^2..1024^2 primary
+    rays + 1 bounce + shadow rays.  Batched: every request in one
+    cgs_render_batch wavefront (replayed from a captured CUDA graph).  Plain:
+    one k_render_plain launch per request (the reference's per-frame launch
+    shape), back to back; both on the reference's BVH topology, and the
+    batched path again on the longest-axis build."""
+    t0 = time.perf_counter()
+    scs = [scenes.scene_c4(i) for i in range(64)]
+    cams = [scenes.camera_c4(i) for i in range(64)]
+    gen_s = time.perf_counter() - t0
+    out = {"scenes": 64, "patches": int(sum(s.patch_count for s in scs)),
+           "primary_rays": int(sum(side * side for _, side in cams)), "scene_gen_s": gen_s}
+    for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_LONGEST)):
+        t0 = time.perf_counter()
+        store = rt.GpuScene(scs, device=dev.index or 0, split=split)
+        out[f"store_build_s_{split_name}"] = time.perf_counter() - t0
+        out["footprint_mb"] = store.footprint() / 2 ** 20
+        reqs = [rt.Request.alloc(i, c, side, side, 1, DEPTH, device=dev.index or 0)
+                for i, (c, side) in enumerate(cams)]
+        legs = (("batched", rt.WAVEFRONT), ("plain", rt.PLAIN)) if split == rt.SPLIT_REFERENCE else \
+            (("batched_split_longest", rt.WAVEFRONT),)
+        for name, sched in legs:
+            tr = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=prec, schedule=sched))
+            for _ in range(2):  # the first runs eagerly, the second captures the graph
+                tr.render_batch(reqs, store, stream)
+                torch.cuda.synchronize()
+            c = store.counters()
+            ms = timed(torch, stream, flush, lambda: tr.render_batch(reqs, store, stream), steps)
+            out[name] = {"value": c["rays"] * steps / (sum(ms) * 1e-3) / 1e6, "unit": "Mrays/s",
+                         "ms_per_batch": sum(ms) / steps, "rays": c["rays"], "launches": c["kernel_launches"],
+                         "device_errors": c["device_errors"]}
+        # accuracy: 1% of every scene's primary rays through per-ray groups, against the FP64 GPU search
+        rays, grp = [], []
+        for i, (cam, side) in enumerate(cams):
+            r = rt.camera_rays(cam, side, side, device=dev.index or 0)
+            sub = torch.from_numpy(scenes.random_subset(side * side, 0.01, seed=100 + i)).to(dev)
+            rays.append(r[:, sub])
+            grp.append(torch.full((sub.numel(),), i, dtype=torch.int32, device=dev))
+        acc = accuracy_vs_fp64(rt, store, torch.cat(rays, 1).contiguous(), prec, torch.cat(grp))
+        out["accuracy" if split == rt.SPLIT_REFERENCE else "accuracy_split_longest"] = acc
+        store.close()
+    out["speedup_vs_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    out["speedup_vs_plain_split_longest"] = out["batched_split_longest"]["value"] / out["plain"]["value"]
+    return out
+
+
+SERVE_RES = ((256, 256), (512, 512), (1920, 1080), (3840, 2160))
+
+
+def serving_stream(n, seed=9):
+    """The seeded request mix of the serving workload: scene uniform over the
+    32 resident scenes, resolution uniform over SERVE_RES, renders (1..4 spp,
+    depth 0..3) and closest-hit ray queries (one ray per pixel) half each."""
+    from cgspline_gb300 import scenes
+    rng = scenes.SplitMix64(seed)
+    u = rng.uniform(5 * n).reshape(n, 5)
+    out = []
+    for k in range(n):
+        kind = "render" if u[k, 0] < 0.5 else "query"
+        out.append(dict(kind=kind, scene=int(u[k, 1] * 32) % 32, res=SERVE_RES[int(u[k, 2] * 4) % 4],
+                        spp=1 + int(u[k, 3] * 4) % 4, depth=int(u[k, 4] * 4) % 4))
+    return out
+
+
+def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=40, slots=4, budget_gb=48):
+    """32 resident scenes (1K..1M patches), a Poisson stream of nreq requests
+    per rate through the continuous-batching server (reference and
+    longest-axis BVH builds) and through the plain server (one request per
+    launch, one at a time, reference build); p50 / p99 latency from submit to
+    completion, and rays/s over the stream."""
+    import numpy as np
+    t0 = time.perf_counter()
+    scs = [scenes.scene_c5(i) for i in range(32)]
+    cams = [scenes.camera_c5(i) for i in range(32)]
+    gen_s = time.perf_counter() - t0
+    stream = serving_stream(nreq)
+    out = {"scenes": 32, "patches": int(sum(s.patch_count for s in scs)), "requests_per_rate": nreq,
+           "slots": slots, "memory_budget_gb": budget_gb, "scene_gen_s": gen_s, "rates": []}
+    stores = {}
+    for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_LONGEST)):
+        t0 = time.perf_counter()
+        stores[split_name] = rt.GpuScene(scs, device=dev.index or 0, split=split)
+        out[f"store_build_s_{split_name}"] = time.perf_counter() - t0
+    out["footprint_mb"] = stores["reference"].footprint() / 2 ** 20
+    # inputs and outputs are allocated before the timed streams
+    reqs = []
+    for q in stream:
+        w, h = q["res"]
+        if q["kind"] == "render":
+            reqs.append(rt.Request.alloc(q["scene"], cams[q["scene"]], w, h, spp=q["spp"], recursion_depth=q["depth"],
+                                         device=dev.index or 0))
+        else:
+            rays = rt.camera_rays(cams[q["scene"]], w, h, device=dev.index or 0)
+            res = (torch.empty((3, w * h), dtype=torch.float32, device=dev),
+                   torch.empty((2, w * h), dtype=torch.int32, device=dev))
+            reqs.append((q["scene"], rays, res))
+    torch.cuda.synchronize()
+
+    def play(server, rate, seed):
+        rng = scenes.SplitMix64(seed)
+        gaps = -np.log(1.0 - rng.uniform(nreq)) / rate if rate else np.zeros(nreq)
+        arrivals = np.cumsum(gaps) - gaps[0]
+        r0 = server.stats()["rays_traced"]
+        start = time.perf_counter()
+        tickets = []
+        for k, r in enumerate(reqs):
+            while time.perf_counter() - start < arrivals[k]:
+                pass
+            if isinstance(r, tuple):
+                tickets.append(server.submit_query(r[0], r[1], out=r[2])[0])
+            else:
+                tickets.append(server.submit_render(r))
+        infos = [server.wait(t) for t in tickets]
+        lat = np.array([i["finish_s"] - i["submit_s"] for i in infos]) * 1e3
+        span = max(i["finish_s"] for i in infos) - min(i["submit_s"] for i in infos)
+        rays = server.stats()["rays_traced"] - r0
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "Mrays_s": rays / span / 1e6, "rays": int(rays), "span_s": span}
+
+    opts = rt.Options(recursion_depth=3, precision=prec)
+    servers = {"served": rt.Server(stores["reference"], slots=slots, memory_budget=budget_gb << 30, options=opts),
+               "served_split_longest": rt.Server(stores["longest"], slots=slots, memory_budget=budget_gb << 30,
+                                                 options=opts),
+               "plain": rt.Server(stores["reference"], options=rt.Options(recursion_depth=3, precision=prec,
+                                                                          schedule=rt.PLAIN))}
+    for sv in servers.values():
+        play(sv, 0, 1)  # warm-up: slot buffers grow to their working size, graphs get captured
+    out["max_batch_samples"] = servers["served"].stats()["max_batch_samples"]
+    for k, lam in enumerate(rates):
+        out["rates"].append({"lambda": lam} | {name: play(sv, lam, 100 + k) for name, sv in servers.items()})
+    sat = {name: play(sv, 0, 7) for name, sv in servers.items()}
+    sat["speedup"] = sat["served"]["Mrays_s"] / sat["plain"]["Mrays_s"]
+    sat["speedup_split_longest"] = sat["served_split_longest"]["Mrays_s"] / sat["plain"]["Mrays_s"]
+    out["saturation"] = sat
+    st = servers["served"].stats()
+    out["served_stats"] = {k: st[k] for k in ("batches", "chunks", "peak_slot_bytes", "kernel_launches")}
+    for sv in servers.values():
+        sv.close()
+    for s in stores.values():
+        s.close()
+    return out
 
 
 def main():
@@ -198,7 +414,8 @@ def main():
     dev = torch.device("cuda", local)
 
     scene, cam = scenes.scene_c2(), scenes.camera_c2()
-    g = rt.GpuScene(scene, device=local)
+    split = rt.SPLIT_LONGEST if args.split == "longest" else rt.SPLIT_REFERENCE
+    g = rt.GpuScene(scene, device=local, split=split)
     sched = rt.WAVEFRONT if args.schedule == "wavefront" else rt.PLAIN
     prec = rt.FP32_POLISH64 if args.precision == "polish64" else rt.FP32
     tracer = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=prec, schedule=sched))
@@ -206,31 +423,19 @@ def main():
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
 
-    def step():
-        # a scene refuses a new render while its previous one is in flight
-        # (src/rt/RayTracer.cu:110-116), so frames are issued one at a time;
-        # the events below time each frame on the device.
-        tracer.render(frame, cam, g, stream)
-
+    # a scene refuses a new render while its previous one is in flight
+    # (src/rt/RayTracer.cu:110-116), so frames are issued one at a time and
+    # each is timed on the device
     for _ in range(max(3, args.warmup)):
-        step()
+        tracer.render(frame, cam, g, stream)
         torch.cuda.synchronize()
     counters = g.counters()
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if dist:
         td.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for k in range(args.steps):
-            flush.fill_(float(k))  # L2 flush: 2x L2 bytes written between frames
-            starts[k].record(stream)
-            step()
-            ends[k].record(stream)
-            ends[k].synchronize()
+        ms = timed(torch, stream, flush, lambda: tracer.render(frame, cam, g, stream), args.steps)
         torch.cuda.synchronize()
-    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = float(sum(ms))
     if dist:
         t = torch.tensor([total_ms], device=dev)
@@ -240,20 +445,21 @@ def main():
     value = rays_per_frame * args.steps * world / (total_ms * 1e-3) / 1e6
 
     # e2e: the C-ABI host entry point (framebuffer copied to host inside the timed region)
-    fb_host = None
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        fb_host, _ = tracer.render_host(cam, g, W, H, linear=False)
+        tracer.render_host(cam, g, W, H, linear=False)
     e2e_s = time.perf_counter() - t0
     e2e = {"value": rays_per_frame * args.steps / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 44,
            "d2h_bytes_per_step": W * H * 4}
 
     extra = {}
-    if not args.quick and rank == 0:
-        # dominant-kernel roofline from the kernel's own work counters
+    if rank == 0:
         c = counters
         nrays, nodes, hashes, cand, iters = c["rays"], c["nodes"], c["hash_lookups"], c["candidates"], c["iterations"]
+        # algorithmic bytes: a ray (48 B in + out), a 64 B node per inner-node
+        # visit, an 8 B hash probe per backtrack, a 256 B patch + 64 B of
+        # candidate-list traffic per (ray, patch) search
         alg_bytes = 48 * nrays + 64 * nodes + 8 * hashes + 320 * cand
         alg_flops = 12 * nodes + 296 * cand + 470 * iters + 200 * nrays
         sec_per_frame = total_ms / args.steps / 1e3
@@ -271,48 +477,51 @@ def main():
                                       "peak_source": f"nominal 152 SM x 256 flop/clk at {mhz:.0f} MHz"},
                              "per_ray": {"nodes": nodes / nrays, "hash_lookups": hashes / nrays,
                                          "candidates": cand / nrays, "clip_iterations": iters / nrays}}
-        # plain per-frame GPU path (one thread per pixel megakernel)
+        # accuracy of the primary hits on a seeded 1% pixel subset
+        allr = rt.camera_rays(cam, W, H, device=local)
+        sub = torch.from_numpy(scenes.random_subset(W * H, 0.01, seed=77)).to(dev)
+        subset = allr[:, sub].contiguous()
+        extra["accuracy"] = accuracy_vs_fp64(rt, g, subset, prec)
+    if not args.quick and rank == 0:
+        # plain per-frame GPU path (one thread per pixel, the whole chain inline)
         if sched != rt.PLAIN:
             plain = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=prec, schedule=rt.PLAIN))
-            for _ in range(2):
-                plain.render(frame, cam, g, stream)
-                torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            pm = 0.0
-            for k in range(3):
-                flush.fill_(float(k))
-                e0.record(stream)
-                plain.render(frame, cam, g, stream)
-                e1.record(stream)
-                torch.cuda.synchronize()
-                pm += e0.elapsed_time(e1)
-            extra["plain_path"] = {"value": rays_per_frame * 3 / (pm * 1e-3) / 1e6, "unit": "Mrays/s",
-                                   "ms_per_step": pm / 3}
-        # accuracy vs FP64 on a seeded 1% pixel subset of the primary rays
-        import oracle
-        o = oracle.OracleScene(scene)
-        allr = oracle.camera_rays(cam, W, H)
-        sub = scenes.random_subset(W * H, 0.01, seed=77)
-        rays = np.ascontiguousarray(allr[:, sub])
-        o64 = o.intersect(rays, precision=oracle.FP64)
-        gg = g.intersect(torch.from_numpy(rays).to(dev), precision=prec)
-        gp, gt = gg["patch"].cpu().numpy(), gg["t"].cpu().numpy()
-        hm = float(((gp >= 0) != (o64["patch"] >= 0)).mean())
-        both = (gp >= 0) & (o64["patch"] >= 0)
-        rel = np.abs(gt[both] - o64["t"][both]) / o64["t"][both]
-        extra["accuracy"] = {"subset_rays": int(sub.size), "max_rel_t_err": float(rel.max(initial=0.0)),
-                             "hit_miss_disagreement": hm,
-                             "patch_disagreement": float((both & (gp != o64["patch"])).mean())}
+            _, pms = frame_leg(rt, torch, g, cam, plain, frame, stream, flush, 3)
+            extra["plain_path"] = {"value": rays_per_frame * 3 / (sum(pms) * 1e-3) / 1e6, "unit": "Mrays/s",
+                                   "ms_per_step": sum(pms) / 3}
+        # the same frame on the other BVH build: same hits, different node visits
+        other = rt.SPLIT_LONGEST if split == rt.SPLIT_REFERENCE else rt.SPLIT_REFERENCE
+        g2 = rt.GpuScene(scene, device=local, split=other)
+        c2, ms2 = frame_leg(rt, torch, g2, cam, tracer, frame, stream, flush, args.steps)
+        ga = {k: v.cpu().numpy() for k, v in g.intersect(subset, precision=prec).items()}
+        gb = {k: v.cpu().numpy() for k, v in g2.intersect(subset, precision=prec).items()}
+        hit = ga["patch"] >= 0
+        name = "split_longest" if other == rt.SPLIT_LONGEST else "split_reference"
+        extra[name] = {"value": c2["rays"] * args.steps / (sum(ms2) * 1e-3) / 1e6, "unit": "Mrays/s",
+                       "ms_per_step": sum(ms2) / args.steps, "rays_per_frame": c2["rays"],
+                       "per_ray_nodes": c2["nodes"] / c2["rays"],
+                       "per_ray_hash_lookups": c2["hash_lookups"] / c2["rays"],
+                       "subset_hit_miss_equal": bool(np.array_equal(hit, gb["patch"] >= 0)),
+                       "subset_max_rel_t_diff": float(
+                           (np.abs(ga["t"][hit] - gb["t"][hit]) / ga["t"][hit]).max(initial=0.0)),
+                       "accuracy": accuracy_vs_fp64(rt, g2, subset, prec)}
+        g2.close()
+        if not args.no_precision:
+            extra["precision"] = precision_leg(rt, scenes, torch, dev, g, scene, flush)
+        if not args.no_batching:
+            extra["batching"] = batching_leg(rt, scenes, torch, dev, stream, prec, flush)
+        if not args.no_serving:
+            extra["serving"] = serving_leg(rt, scenes, torch, dev, prec)
     if not args.no_cpu and rank == 0 and world == 1:
         extra["cpu_baseline"] = {k: v for k, v in cpu_leg(scene, cam, 1).items() if k not in ("seconds", "rays")}
     if rank == 0:
-        line = {"metric": "Mrays/s at <=1e-5 rel-t err vs FP64 (C2 torus 1080p + 1 bounce, PBR)", "value": value,
-                "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
-                "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32+f64polish" if prec == rt.FP32_POLISH64 else "f32",
+        line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(3, args.warmup), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32+f64polish" if prec == rt.FP32_POLISH64 else "f32",
                 "data": "synthetic (seeded displaced torus)",
                 "config": {"workload": f"torus 16384 patches, {W}x{H} primary + {DEPTH} bounce, PBR, 2 point lights",
-                           "schedule": args.schedule, "rays_per_frame": rays_per_frame,
+                           "schedule": args.schedule, "bvh_split": args.split, "rays_per_frame": rays_per_frame,
                            "primary_rays": W * H, "l2": "flushed (2x L2 written) before every frame",
                            "parallelism": f"replicas x{world}"},
                 "e2e": e2e, "gpu_launches": counters["kernel_launches"] * args.steps, "clocks": clk.summary()}

@@ -57,6 +57,26 @@ class Hits(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in ("t", "u", "v", "patch", "object")]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("memory_budget", C.c_uint64), ("max_batch_samples", C.c_uint32),
+                ("max_batch_requests", C.c_uint32), ("render", RenderOptions)]
+
+
+class QueryRequest(C.Structure):
+    _fields_ = [("group", C.c_uint32), ("n", C.c_uint32), ("any_hit", C.c_int), ("rays", Rays), ("hits", Hits)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("chunks", C.c_uint32), ("submit_s", C.c_double), ("start_s", C.c_double),
+                ("finish_s", C.c_double), ("samples", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "finished", "rejected", "batches", "chunks", "rays_traced",
+                                          "slot_bytes", "peak_slot_bytes", "kernel_launches")] + \
+        [("busy_s", C.c_double), ("max_batch_samples", C.c_uint32), ("queued", C.c_uint32)]
+
+
 class Counters(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("rays", "primary_rays", "bounce_rays", "shadow_rays", "nodes",
                                           "hash_lookups", "candidates", "iterations", "device_errors",
@@ -78,6 +98,7 @@ SIGNATURES = [
     ("cgs_scene_add_object", C.c_int, [P, U32, P, P, C.POINTER(Material), P, P, U32, C.POINTER(U32)]),
     ("cgs_scene_set_lights", C.c_int, [P, P, U32]),
     ("cgs_scene_set_environment", C.c_int, [P, P, P]),
+    ("cgs_scene_set_bvh_split", C.c_int, [P, C.c_int]),
     ("cgs_bvh_build", C.c_int, [P]),
     ("cgs_hash_build", C.c_int, [P, P]),
     ("cgs_scene_build", C.c_int, [P, P]),
@@ -92,8 +113,16 @@ SIGNATURES = [
     ("cgs_render_host", C.c_int, [P, C.POINTER(Camera), U32, U32, C.POINTER(RenderOptions), P, P, P]),
     ("cgs_render_batch", C.c_int, [P, C.POINTER(RenderRequest), U32, C.POINTER(RenderOptions), P]),
     ("cgs_render_running", C.c_int, [P]),
+    ("cgs_camera_rays", C.c_int, [C.POINTER(Camera), U32, U32, C.c_int, P, P]),
     ("cgs_scene_counters", C.c_int, [P, C.POINTER(Counters)]),
     ("cgs_perfect_hash_build", C.c_int, [P, U32, P, U32, P, U32, P, P]),
+    ("cgs_server_create", C.c_int, [C.POINTER(P), P, C.POINTER(ServerOptions)]),
+    ("cgs_server_destroy", C.c_int, [P]),
+    ("cgs_server_submit_render", C.c_int, [P, C.POINTER(RenderRequest), C.POINTER(C.c_uint64)]),
+    ("cgs_server_submit_query", C.c_int, [P, C.POINTER(QueryRequest), C.POINTER(C.c_uint64)]),
+    ("cgs_server_wait", C.c_int, [P, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]),
+    ("cgs_server_clock", C.c_double, [P]),
+    ("cgs_server_stats_get", C.c_int, [P, C.POINTER(ServerStats)]),
     ("cgs_perfect_hash_build_noalloc", C.c_int, [P, U32, P, U32, P, U32, P, P]),
 ]
 

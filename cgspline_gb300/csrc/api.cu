@@ -42,6 +42,72 @@ int ensure_engine(cgs_scene* sc, uint32_t capacity)
     return CGS_OK;
 }
 
+void GraphCache::release()
+{
+    for (auto& kv : execs) cudaGraphExecDestroy(kv.second.exec);
+    execs.clear();
+    seen.clear();
+    if (capture) cudaStreamDestroy(capture);
+    capture = nullptr;
+}
+
+uint64_t scene_key(const DevScene& S)
+{
+    return key_of({key_of(S.patches), key_of(S.nodes), key_of(S.indices), key_of(S.tables), key_of(S.disps),
+                   key_of(S.bvhs), key_of(S.patchBase), key_of(S.objects), key_of(S.materials),
+                   key_of(S.patchMaterial), key_of(S.lights), key_of(S.groupTop), key_of(S.groupLights),
+                   key_of(S.groupEnv), S.nobjects, S.nsurfaces, S.ngroups});
+}
+
+uint64_t query_key(const Query& q)
+{
+    uint32_t tol;
+    std::memcpy(&tol, &q.tol, 4);
+    return key_of({uint64_t(q.method), uint64_t(q.precision), tol});
+}
+
+cudaError_t run_cached(GraphCache& gc, uint64_t key, cudaStream_t stream, int* launches,
+                       const std::function<cudaError_t(cudaStream_t, int*)>& fn)
+{
+    auto it = gc.execs.find(key);
+    if (it != gc.execs.end())
+    {
+        if (launches) *launches += it->second.launches;
+        gc.replays++;
+        return cudaGraphLaunch(it->second.exec, stream);
+    }
+    if (gc.disabled || gc.seen.insert(key).second) return fn(stream, launches);
+    cudaError_t e = cudaSuccess;
+    if (!gc.capture) e = cudaStreamCreateWithFlags(&gc.capture, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { gc.disabled = true; return fn(stream, launches); }
+    // the captured sequence must follow the work already queued on `stream`
+    // only when it runs, which the graph launch on `stream` provides
+    int nl = 0;
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamBeginCapture(gc.capture, cudaStreamCaptureModeThreadLocal);
+    cudaError_t e1 = e == cudaSuccess ? fn(gc.capture, &nl) : e;
+    cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(gc.capture, &graph) : e;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e3 = (e1 == cudaSuccess && e2 == cudaSuccess) ? cudaGraphInstantiate(&exec, graph, 0) : e2;
+    if (graph) cudaGraphDestroy(graph);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+    {
+        // capture is not available here: run eagerly from now on
+        cudaGetLastError();
+        gc.disabled = true;
+        return fn(stream, launches);
+    }
+    if (gc.execs.size() >= 32)
+    {
+        for (auto& kv : gc.execs) cudaGraphExecDestroy(kv.second.exec);
+        gc.execs.clear();
+    }
+    gc.execs[key] = GraphCache::Entry {exec, nl};
+    gc.captures++;
+    if (launches) *launches += nl;
+    return cudaGraphLaunch(exec, stream);
+}
+
 // Device bytes of a render slot for `samples` primary rays and `lights`
 // lights per group (the sizes RenderSlot::ensure reserves).
 uint64_t RenderSlot::bytes_for(uint32_t samples, uint32_t lights)
@@ -105,14 +171,52 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
     return CGS_OK;
 }
 
+int RenderSlot::ensure_engine(uint32_t rays)
+{
+    if (engineCapacity >= rays && engine.p) return CGS_OK;
+    CGS_TRY(engine.reserve(engine_words(rays, kEnginePasses)));
+    engineCapacity = rays;
+    wb.engine = engine.p;
+    wb.engineCapacity = engineCapacity;
+    return CGS_OK;
+}
+
+uint64_t RenderSlot::bytes() const
+{
+    uint64_t b = ray0.bytes() + ray1.bytes() + shadow.bytes() + contrib.bytes() + base.bytes() + accum.bytes();
+    b += hitF.bytes() + smp0.bytes() + smp1.bytes() + grp0.bytes() + grp1.bytes() + dep0.bytes() + dep1.bytes();
+    b += count.bytes() + shadowSlot.bytes() + shadowGroup.bytes() + engine.bytes() + visible.bytes() + hitI.bytes();
+    b += occluded.bytes() + req.bytes() + counters.bytes() + batch.bytes();
+    return b;
+}
+
 void RenderSlot::release()
 {
     ray0.release(); ray1.release(); shadow.release(); contrib.release(); base.release(); accum.release();
     hitF.release();
     for (auto* b : {&smp0, &smp1, &grp0, &grp1, &dep0, &dep1, &count, &shadowSlot, &shadowGroup, &engine}) b->release();
-    visible.release(); hitI.release(); occluded.release(); req.release(); counters.release();
+    visible.release(); hitI.release(); occluded.release(); req.release(); counters.release(); batch.release();
+    graphs.release();
     wb = WavefrontBuffers {};
     engineCapacity = 0;
+}
+
+cudaError_t launch_wavefront_cached(const DevScene& S, RenderSlot& slot, const RenderBatch& b, cudaStream_t stream,
+                                    int* launches)
+{
+    const WavefrontBuffers& w = slot.wb;
+    uint32_t eps;
+    std::memcpy(&eps, &b.eps, 4);
+    const uint64_t key = key_of({scene_key(S), query_key(b.q), uint64_t(b.maxDepth), eps, key_of(slot.batch.p),
+                                 key_of(slot.counters.p), key_of(w.ray[0]), key_of(w.ray[1]), key_of(w.engine),
+                                 key_of(w.shadow), key_of(w.accum), key_of(w.hit.t), key_of(w.occluded),
+                                 key_of(w.contrib), key_of(w.visible), key_of(w.base), key_of(w.count),
+                                 key_of(w.sample[0]), key_of(w.group[0]), key_of(w.depth[0]), w.capacity,
+                                 w.lightCapacity, w.engineCapacity});
+    RenderSlot* sp = &slot;
+    return run_cached(slot.graphs, key, stream, launches, [&](cudaStream_t st, int* nl) {
+        return launch_render_wavefront(S, b, sp->batch.p, sp->wb, sp->counters.p, st, nl);
+    });
 }
 
 int prepare_batch(cgs_scene* sc, const cgs_render_request* reqs, uint32_t n, const cgs_render_options* opt,
@@ -136,7 +240,7 @@ int prepare_batch(cgs_scene* sc, const cgs_render_request* reqs, uint32_t n, con
         DevRequest& d = host[k];
         camera_setup(r.camera, r.width, r.height, opt->flip_y, d.cam);
         d.group = r.group; d.width = r.width; d.height = r.height; d.spp = r.spp; d.depth = depth;
-        d.sampleBase = uint32_t(samples); d.pixelBase = uint32_t(pixels); d.stride = r.width;
+        d.sampleBase = uint32_t(samples); d.pixelBase = uint32_t(pixels); d.stride = r.width; d.row0 = 0;
         d.fb = r.framebuffer; d.linear = r.linear_rgb;
         samples += uint64_t(r.width) * r.height * r.spp;
         pixels += uint64_t(r.width) * r.height;
@@ -162,10 +266,12 @@ int run_batch(cgs_scene* sc, RenderSlot& slot, const std::vector<DevRequest>& ho
     {
         int r = slot.ensure(b.samples, sc->maxLights(), b.nreq);
         if (r) return r;
+        CGS_TRY(slot.batch.reserve(1));
         CGS_TRY(cudaMemcpyAsync(slot.req.p, host.data(), host.size() * sizeof(DevRequest), cudaMemcpyHostToDevice,
                                 stream));
         b.req = slot.req.p;
-        e = launch_render_wavefront(sc->dev(), b, slot.wb, slot.counters.p, stream, launches);
+        CGS_TRY(cudaMemcpyAsync(slot.batch.p, &b, sizeof b, cudaMemcpyHostToDevice, stream));
+        e = launch_wavefront_cached(sc->dev(), slot, b, stream, launches);
     }
     return cuda_status(e);
 }
@@ -342,6 +448,14 @@ int cgs_render_host(cgs_scene* s, const cgs_camera* cam, uint32_t w, uint32_t h,
     if (linear) CGS_TRY(cudaMemcpyAsync(linear, s->linStage.p, 12ull * w * h, cudaMemcpyDeviceToHost, st));
     CGS_TRY(cudaStreamSynchronize(st));
     return CGS_OK;
+}
+
+int cgs_camera_rays(const cgs_camera* cam, uint32_t w, uint32_t h, int flip_y, float* rays, void* stream)
+{
+    if (!cam || !rays || w == 0 || h == 0 || uint64_t(w) * h >= (1ull << 32)) return CGS_ERR_INVALID_ARGUMENT;
+    CameraSetup c;
+    camera_setup(*cam, w, h, flip_y, c);
+    return cuda_status(launch_camera_rays(c, w, h, rays, (cudaStream_t)stream));
 }
 
 int cgs_render_running(cgs_scene* s)

@@ -360,6 +360,153 @@ __device__ __forceinline__ void project_net(float2* net, const float4* __restric
     }
 }
 
+// ------------------------------------- FP64 fat-line bounds (grazing) --
+// The precision form searches near-grazing candidates (the ray within 30
+// degrees of the plane of the patch's diagonals) on a net projected in FP64
+// (rounded to FP32), with the fat-line bounds of every FP32 sub-net computed
+// in FP64 (distances, hull scan, DBL_EPSILON) and rounded outward, to the
+// tolerance 2^-20: FP32 sub-nets near the ray are small, so FP32 holds them,
+// while the FP32 bounds and the 2^-12 tolerance lose near-tangent roots.
+constexpr float kGrazeTol = 0x1p-20f;
+// A near-grazing search stops after this many iterations and keeps what it
+// found (the 2^-20 tolerance can be out of FP32 reach far from the ray).
+constexpr int kGrazeIterations = 1024;
+
+// Precision levels (enum cgs_precision) of closest-hit searches: 0 FP32;
+// 1 FP32 + FP64 polish; 2 pure FP64; 3 as 1, with the FP64 bounds for
+// candidates within 30 degrees of grazing.  Internal level 5: the search of
+// 3 without the polish (closest-hit passes whose polish runs separately).
+// Any-hit searches run at level 0.
+__host__ __device__ __forceinline__ bool polishes(int precision) { return precision == 1 || precision == 3; }
+__host__ __device__ __forceinline__ float graze_sin(int precision)
+{
+    return (precision == 3 || precision == 5) ? 0.5f : 0.0f;  // sin 30 degrees
+}
+__host__ __device__ __forceinline__ int search_only(int precision)
+{
+    return precision == 3 ? 5 : precision == 5 ? 5 : 0;
+}
+
+__device__ __forceinline__ double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 operator-(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 operator*(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ double len2d(double2 a) { return sqrt(a.x * a.x + a.y * a.y); }
+
+// xAxisIntersection in double with DBL_EPSILON (src/Spline_BezierClipping.cu:127-156)
+__device__ __forceinline__ bool x_axis_d(double& lo, double& hi, double2 A, double2 B)
+{
+    const double eps = 2.220446049250313e-16;
+    const double q = A.y - B.y;
+    if (fabs(q) > eps)
+    {
+        const double t = A.y / q;
+        if (0.0 <= t && t <= 1.0) { lo = hi = (1.0 - t) * A.x + t * B.x; return true; }
+    }
+    else if (fabs(A.y) <= eps)
+    {
+        lo = fmin(A.x, B.x); hi = fmax(A.x, B.x);
+        return true;
+    }
+    return false;
+}
+
+// clip_range in double (src/Spline_BezierClipping.cu:610-701)
+__device__ __forceinline__ void clip_range_d(const double2* p, int cutside, double& lower, double& upper)
+{
+    lower = 1.0; upper = 0.0;
+    double2 L = p[15] - p[0];
+    const double2 D = p[12] - p[3];
+    L = cutside == 0 ? L + D : L - D;
+    {
+        const double l = len2d(L);
+        if (l != 0.0) L = make_double2(L.x / l, L.y / l);
+    }
+    const double2 N = make_double2(-L.y, L.x);
+    double ytop[4], ybot[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        double y[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+        {
+            const double2 q = cutside == 0 ? p[4 * k + i] : p[4 * i + k];
+            y[k] = N.x * q.x + N.y * q.y;
+        }
+        ybot[i] = fmin(fmin(y[0], y[1]), fmin(y[2], y[3]));
+        ytop[i] = fmax(fmax(y[0], y[1]), fmax(y[2], y[3]));
+    }
+    const double o1 = 1.0 / 3.0, o2 = 2.0 / 3.0;
+    const double2 hull[7] = {make_double2(o2, ybot[2]), make_double2(1.0, ybot[3]), make_double2(1.0, ytop[3]),
+                             make_double2(o2, ytop[2]), make_double2(o1, ytop[1]), make_double2(0.0, ytop[0]),
+                             make_double2(0.0, ybot[0])};
+    double2 P1 = make_double2(0.0, ybot[0]), P2 = make_double2(o1, ybot[1]);
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+    {
+        const double2 P3 = hull[k];
+        const double2 a = P2 - P1, b = P3 - P1;
+        if (a.x * b.y - a.y * b.x >= 0.0)
+        {
+            double lo, hi;
+            if (x_axis_d(lo, hi, P1, P2)) { lower = fmin(lower, lo); upper = fmax(upper, hi); }
+            P1 = P2;
+        }
+        P2 = P3;
+    }
+    double lo, hi;
+    if (x_axis_d(lo, hi, P1, P2)) { lower = fmin(lower, lo); upper = fmax(upper, hi); }
+    lower = lower * 0x0FFp-8;
+    upper = upper + (1.0 - upper) * 0x001p-8;
+}
+
+// FP64 bounds of an FP32 sub-net, rounded outward.
+__device__ __forceinline__ void clip_range64(const float2* p, int cutside, float& lower, float& upper)
+{
+    double2 q[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) q[i] = make_double2(p[i].x, p[i].y);
+    double lo, hi;
+    clip_range_d(q, cutside, lo, hi);
+    lower = __double2float_rd(lo);
+    upper = __double2float_ru(hi);
+}
+
+__device__ __forceinline__ double dot_d(double3 a, double3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ double3 cross_d(double3 a, double3 b)
+{
+    return make_double3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double3 unit3d(double3 a)
+{
+    const double l = sqrt(dot_d(a, a));
+    return l != 0.0 ? make_double3(a.x / l, a.y / l, a.z / l) : a;
+}
+
+// project_net with the axes and dot products in double, rounded to float.
+__device__ __forceinline__ void project_net64(float2* net, const float4* __restrict__ P, float3 o, float3 d)
+{
+    const double3 dd = make_double3(d.x, d.y, d.z);
+    const double3 a0 = unit3d(cross_d(dd, make_double3(dd.x, dd.y, dd.z + 8.0)));
+    const double3 a1 = unit3d(cross_d(dd, a0));
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+    {
+        const float4 q = __ldg(P + i);
+        const double3 Q = make_double3(double(q.x) - o.x, double(q.y) - o.y, double(q.z) - o.z);
+        net[i] = make_float2(float(dot_d(a0, Q)), float(dot_d(a1, Q)));
+    }
+}
+
+// The ray within asin(sinmax) of the plane of the patch's diagonals.
+__device__ __forceinline__ bool near_grazing(const float4* __restrict__ P, float3 d, float sinmax)
+{
+    const float3 a = xyz(__ldg(P + 15)) - xyz(__ldg(P)), b = xyz(__ldg(P + 12)) - xyz(__ldg(P + 3));
+    const float3 n = cross(a, b);
+    const float l = len(n);
+    return l > 0.0f && fabsf(dot(n, d)) < sinmax * l;
+}
+
 // doBezierClipping2D_device (src/Spline_BezierClipping.cu:547-828) with the
 // half-precision (mid,len) stack replaced by a full-precision (min,max)
 // stack of the same depth.  Popped sub-nets are re-derived from the
@@ -375,12 +522,18 @@ struct ClipState
     float2 buf[16];
     float2 emin, emax;
     int cutsideStack, sl, it;
-    bool found;
+    float tol;
+    bool found, b64;  // b64: FP64 projection and fat-line bounds (near-grazing)
 };
 
-__device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink)
+// grazeSin > 0: the precision form (candidates within asin(grazeSin) of
+// grazing get the FP64 bounds)
+__device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, float tol, float grazeSin)
 {
-    project_net(c.buf, sink.P, sink.o, sink.d);
+    c.b64 = grazeSin > 0.0f && near_grazing(sink.P, sink.d, grazeSin);
+    c.tol = c.b64 ? kGrazeTol : tol;
+    if (c.b64) project_net64(c.buf, sink.P, sink.o, sink.d);
+    else project_net(c.buf, sink.P, sink.o, sink.d);
     c.emin = make_float2(0.0f, 0.0f);
     c.emax = make_float2(1.0f, 1.0f);
     c.cutsideStack = 0;
@@ -389,17 +542,19 @@ __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink)
     c.found = false;
 }
 
-__device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, float tol, LocalCounters& lc)
+__device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, LocalCounters& lc)
 {
+    if (c.b64 && c.it >= kGrazeIterations) return false;
     if (c.it++ >= kMaxClipIterations) { lc.errors |= kErrClipIterations; return false; }
     lc.iterations++;
     const int cutside = c.cutsideStack & 1;
-    if (len2(c.buf[3] - c.buf[12]) < tol && len2(c.buf[15] - c.buf[0]) < tol)
+    if (len2(c.buf[3] - c.buf[12]) < c.tol && len2(c.buf[15] - c.buf[0]) < c.tol)
         c.found |= approximateIntersection(sink, c.buf, c.emin, c.emax);
     else
     {
         float lower, upper;
-        clip_range(c.buf, cutside, lower, upper);
+        if (c.b64) clip_range64(c.buf, cutside, lower, upper);
+        else clip_range(c.buf, cutside, lower, upper);
         float delta = upper - lower;
         if (delta > 0.8f)
         {
@@ -450,18 +605,19 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
     float4 e = st[c.sl];
     c.emin = make_float2(e.x, e.y);
     c.emax = make_float2(e.z, e.w);
-    project_net(c.buf, sink.P, sink.o, sink.d);
+    if (c.b64) project_net64(c.buf, sink.P, sink.o, sink.d);
+    else project_net(c.buf, sink.P, sink.o, sink.d);
     subpatchU(c.buf, c.emin.x, c.emax.x);
     subpatchV(c.buf, c.emin.y, c.emax.y);
     return true;
 }
 
-static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, LocalCounters& lc)
+static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, float grazeSin, LocalCounters& lc)
 {
     float4 st[kClipStack];
     ClipState c;
-    clip_begin(c, sink);
-    while (clip_step(c, st, sink, tol, lc)) {}
+    clip_begin(c, sink, tol, grazeSin);
+    while (clip_step(c, st, sink, lc)) {}
     return c.found;
 }
 
@@ -539,15 +695,46 @@ __device__ __forceinline__ void dbasis_d(double t, double* w)
     w[0] = -3.0 * s * s; w[1] = 3.0 * s * s - 6.0 * t * s; w[2] = 6.0 * t * s - 3.0 * t * t; w[3] = 3.0 * t * t;
 }
 
-// Newton polish of S(u,v) = o + t d on the winning hit, as mixed-precision
-// iterative refinement: the residual S(u,v) - (o + t d) is evaluated in FP64
-// (Bernstein weights and the tensor sum in double), the 3x3 Jacobian
-// [dS/du dS/dv -d] and its solve stay in FP32, and (u,v,t) accumulate in
-// FP64.  An FP32 Jacobian is accurate to ~1e-7 relative, so each step cuts
-// the error by that factor; at most kPolishSteps steps, stopping once the
-// update is below 1e-13 of t.  The result is kept only if the iteration
-// converges inside the patch domain (1e-6 slack) in front of the origin.
+// Newton polish of S(u,v) = o + t d on the winning hit, first as
+// mixed-precision iterative refinement: the residual S(u,v) - (o + t d) is
+// evaluated in FP64 (Bernstein weights and the tensor sum in double), the 3x3
+// Jacobian [dS/du dS/dv -d] and its solve stay in FP32, and (u,v,t)
+// accumulate in FP64.  An FP32 Jacobian is accurate to ~1e-7 relative, so each
+// step cuts the error by about that factor times the Jacobian's condition
+// number; the iteration stops once the update is below 1e-13 of t.  Hits
+// where kPolishSteps such steps do not converge (ill-conditioned, e.g.
+// grazing) continue with up to kPolishSteps64 full-FP64 Newton steps (FP64
+// Jacobian, as the oracle's polish).  The result is kept if it is finite and
+// lies inside the patch domain (1e-6 slack) in front of the origin.
 constexpr int kPolishSteps = 3;
+constexpr int kPolishSteps64 = 10;
+
+// Projected surface point and partials at (U, V) in FP64.
+__device__ __forceinline__ void surface_d(const float4* __restrict__ P, double U, double V, double3& Sp, double3& Su,
+                                          double3& Sv)
+{
+    double wu[4], wv[4], du[4], dv[4];
+    basis_d(U, wu); basis_d(V, wv); dbasis_d(U, du); dbasis_d(V, dv);
+    double H[4] = {0, 0, 0, 0}, Hu[4] = {0, 0, 0, 0}, Hv[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+    {
+        double r[4] = {0, 0, 0, 0}, ru[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+        {
+            const float4 q = __ldg(P + 4 * j + i);
+            r[0] += wu[i] * q.x; r[1] += wu[i] * q.y; r[2] += wu[i] * q.z; r[3] += wu[i] * q.w;
+            ru[0] += du[i] * q.x; ru[1] += du[i] * q.y; ru[2] += du[i] * q.z; ru[3] += du[i] * q.w;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) { H[k] += wv[j] * r[k]; Hu[k] += wv[j] * ru[k]; Hv[k] += dv[j] * r[k]; }
+    }
+    const double iw = 1.0 / H[3];
+    Sp = make_double3(H[0] * iw, H[1] * iw, H[2] * iw);
+    Su = make_double3((Hu[0] - Hu[3] * Sp.x) * iw, (Hu[1] - Hu[3] * Sp.y) * iw, (Hu[2] - Hu[3] * Sp.z) * iw);
+    Sv = make_double3((Hv[0] - Hv[3] * Sp.x) * iw, (Hv[1] - Hv[3] * Sp.y) * iw, (Hv[2] - Hv[3] * Sp.z) * iw);
+}
 
 static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P, double3 o, double3 d, double& t,
                                                     double& u, double& v)
@@ -587,17 +774,36 @@ static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P
         const float3 c = -df;
         const float3 svxc = cross(Sv, c);
         const float det = dot(Su, svxc);
-        if (!(fabsf(det) > 1e-30f)) return false;
+        if (!(fabsf(det) > 1e-30f)) break;
         const float3 mF = f3(-fx, -fy, -fz);
         const float idet = 1.0f / det;
         const double dU = double(dot(mF, svxc) * idet);
         const double dV = double(dot(Su, cross(mF, c)) * idet);
         const double dT = double(dot(Su, cross(Sv, mF)) * idet);
         U += dU; V += dV; T += dT;
-        if (!isfinite(U + V + T)) return false;
+        if (!isfinite(U + V + T)) { U = u; V = v; T = t; break; }
         if (fabs(dT) <= 1e-13 * fabs(T) && fabs(dU) + fabs(dV) <= 1e-13) { converged = true; break; }
     }
-    (void)converged;
+    if (!converged)
+    {
+        // the oracle's polish: FP64 Jacobian and solve
+        const double3 c = make_double3(-d.x, -d.y, -d.z);
+        for (int it = 0; it < kPolishSteps64; it++)
+        {
+            double3 Sp, Su, Sv;
+            surface_d(P, U, V, Sp, Su, Sv);
+            const double3 mF = make_double3(o.x + T * d.x - Sp.x, o.y + T * d.y - Sp.y, o.z + T * d.z - Sp.z);
+            const double3 svxc = cross_d(Sv, c);
+            const double det = dot_d(Su, svxc);
+            if (!(fabs(det) > 1e-300)) return false;
+            const double dU = dot_d(mF, svxc) / det;
+            const double dV = dot_d(Su, cross_d(mF, c)) / det;
+            const double dT = dot_d(Su, cross_d(Sv, mF)) / det;
+            U += dU; V += dV; T += dT;
+            if (!isfinite(U + V + T)) return false;
+            if (fabs(dU) + fabs(dV) < 1e-15 && fabs(dT) < 1e-15 * fabs(T)) { converged = true; break; }
+        }
+    }
     if (U < -1e-6 || U > 1.0 + 1e-6 || V < -1e-6 || V > 1.0 + 1e-6 || T <= 0.0) return false;
     t = T; u = U; v = V;
     return true;
@@ -723,7 +929,7 @@ __device__ __forceinline__ void to_local(const DevObject& ob, float3 o, float3 d
 __device__ __forceinline__ bool search_patch(HitSink& sink, const Query& q, LocalCounters& lc)
 {
     lc.candidates++;
-    return q.method == 0 ? clip_patch(sink, q.tol, lc) : subdiv_patch(sink, q.tol, lc);
+    return q.method == 0 ? clip_patch(sink, q.tol, graze_sin(q.precision), lc) : subdiv_patch(sink, q.tol, lc);
 }
 
 // FP64 Newton polish of a world-space hit, done in the object's space.
@@ -781,15 +987,16 @@ __device__ __forceinline__ int scene_closest(const DevScene& S, uint32_t group, 
         return false;
     };
     hash_traverse<false>(S, S.bvhs[S.groupTop[group]], o, inv, limit, objfn, lc);
-    if (nearest >= 0 && q.precision == 1) polish_hit(S, o, d, hit);
+    if (nearest >= 0 && polishes(q.precision)) polish_hit(S, o, d, hit);
     return nearest;
 }
 
 // Any hit (Context::intersect(const Ray&), src/rt/RayTracer.cu:351-383;
 // rt::intersect(const BezierSurface&, const Ray&), src/rt/Primitive.cu:250-268).
 __device__ __forceinline__ bool scene_any(const DevScene& S, uint32_t group, float3 o, float3 d, float tmax,
-                                          const Query& q, LocalCounters& lc)
+                                          const Query& qin, LocalCounters& lc)
 {
+    const Query q {qin.method, 0, qin.tol};  // any-hit searches run at level 0
     float limit = tmax;
     const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     auto objfn = [&](uint32_t oi) -> bool {

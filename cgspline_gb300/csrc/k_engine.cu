@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
         if (clipping)
         {
             bool found = false, more = false;
-            if (q.method == 0) { more = clip_step(c, stack, sink, q.tol, lc); found = c.found; }
+            if (q.method == 0) { more = clip_step(c, stack, sink, lc); found = c.found; }
             else found = subdiv_patch(sink, q.tol, lc);
             if (!more)
             {
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                     sink.dist = kAny ? lmax : lt;
                     sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
                     lc.candidates++;
-                    if (q.method == 0) clip_begin(c, sink);
+                    if (q.method == 0) clip_begin(c, sink, q.tol, graze_sin(q.precision));
                     clipping = true;
                 }
             }
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(128) k_rest(DevScene S, RaysSoA rays, uint32_t
         float3 o, d; float tmax;
         load_ray(rays, rid, o, d, tmax);
         Query q32 = q;
-        q32.precision = 0;  // the polish kernel runs afterwards
+        q32.precision = search_only(q.precision);  // the polish kernel runs afterwards
         const uint32_t g = rays.group ? rays.group[rid] : 0u;
         if (g >= S.ngroups) continue;
         if (kAny)
@@ -475,13 +475,12 @@ __global__ void __launch_bounds__(128) k_polish(DevScene S, RaysSoA rays, uint32
 
 int sms()
 {
-    static int v = 0;
-    if (!v)
-    {
-        int dev = 0;
+    static const int v = [] {
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    }
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
     return v;
 }
 
@@ -496,12 +495,9 @@ template<bool kAny>
 void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, HitsSoA hits,
             int32_t* occluded, Eng E, Counters* cnt, cudaStream_t stream, int& nl)
 {
-    static int gCol = 0, gRes = 0;
-    if (!gCol)
-    {
-        gCol = resident((const void*)k_collect<kAny>, kCollectThreads);
-        gRes = resident((const void*)k_resolve<kAny>, kResolveThreads);
-    }
+    // thread-safe one-time initialisation (several host threads may launch)
+    static const int gCol = resident((const void*)k_collect<kAny>, kCollectThreads);
+    static const int gRes = resident((const void*)k_resolve<kAny>, kResolveThreads);
     const uint32_t warps = (n + 31) / 32;
     const int gc = int(std::min<uint32_t>(uint32_t(gCol), warps / (kCollectThreads / 32) + 1));
     const int gr = int(std::min<uint32_t>(uint32_t(gRes), warps / (kResolveThreads / 32) + 1));
@@ -529,6 +525,13 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     if (nDev) n = capacity;  // grid sizing only; kernels read *nDev
     if (n == 0) return cudaSuccess;
     if (n > capacity) return cudaErrorInvalidValue;
+    if (any) q.precision = 0;  // any-hit searches run at level 0
+    if (!any && q.precision == 2)
+    {
+        // the pure-FP64 search has no traversal / clip split
+        if (launches) *launches += 1;
+        return launch_query_fp64(S, rays, n, nDev, kTolFP64, hits, cnt, stream);
+    }
     Eng E = carve(scratch, capacity);
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kPasses + 1), stream);
     const int flat = sms() * 4;
@@ -536,7 +539,7 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     int nl = 1;
     if (any) launch<true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     else launch<false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
-    if (!any && q.precision == 1)
+    if (!any && polishes(q.precision))
     {
         k_polish<<<flat * 2, 128, 0, stream>>>(S, rays, n, nDev, hits);
         nl++;

@@ -12,6 +12,8 @@
 //                shading pass that queues shadow and bounce rays, an any-hit
 //                query over the shadow queue and a resolve pass per bounce
 //                level; queue sizes stay on the device.
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace cgs {
@@ -96,7 +98,7 @@ __device__ __forceinline__ void store_pixel(const DevRequest& r, uint32_t px, fl
 
 __device__ __forceinline__ float2 sample_xy(const DevRequest& r, uint32_t pixel, uint32_t s)
 {
-    const float x = float(pixel % r.width), y = float(pixel / r.width);
+    const float x = float(pixel % r.width), y = float(pixel / r.width + r.row0);
     if (r.spp <= 1) return make_float2(x, y);
     return make_float2(x + float(s) * (1.0f / float(r.spp)), y + vdc(s));
 }
@@ -194,8 +196,9 @@ struct Q  // a ray queue: 9 floats per ray (SoA with stride = capacity) + sample
     }
 };
 
-__global__ void k_wf_camera(RenderBatch b, Q q, float* accum, uint32_t* count)
+__global__ void k_wf_camera(const RenderBatch* __restrict__ bp, Q q, float* accum, uint32_t* count)
 {
+    const RenderBatch b = *bp;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < b.samples; k += gridDim.x * blockDim.x)
     {
         const DevRequest& r = b.req[find_request(b.req, b.nreq, k, false)];
@@ -304,8 +307,9 @@ __global__ void k_wf_resolve(DevScene S, Q q, const uint32_t* count, HitsSoA hit
     }
 }
 
-__global__ void k_wf_finish(RenderBatch b, const float* accum)
+__global__ void k_wf_finish(const RenderBatch* __restrict__ bp, const float* accum)
 {
+    const RenderBatch b = *bp;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < b.pixels; p += gridDim.x * blockDim.x)
     {
         const DevRequest& r = b.req[find_request(b.req, b.nreq, p, true)];
@@ -319,15 +323,26 @@ __global__ void k_wf_finish(RenderBatch b, const float* accum)
     }
 }
 
+// Primary rays of a w x h image, one per pixel centre, SoA (7, w*h).
+__global__ void k_camera_rays(CameraSetup cam, uint32_t w, uint32_t h, float* rays)
+{
+    const size_t n = size_t(w) * h;
+    for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x)
+    {
+        const float3 d = pixel_dir(cam, float(k % w), float(k / w));
+        rays[k] = cam.pos[0]; rays[n + k] = cam.pos[1]; rays[2 * n + k] = cam.pos[2];
+        rays[3 * n + k] = d.x; rays[4 * n + k] = d.y; rays[5 * n + k] = d.z; rays[6 * n + k] = INFINITY;
+    }
+}
+
 int sm_count()
 {
-    static int sms = 0;
-    if (!sms)
-    {
-        int dev = 0;
+    static const int sms = [] {
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
     return sms;
 }
 
@@ -354,11 +369,19 @@ cudaError_t launch_render_plain(const DevScene& S, const RenderBatch& b, const D
     return cudaGetLastError();
 }
 
-cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, const WavefrontBuffers& wb,
-                                    Counters* counters, cudaStream_t stream, int* launches)
+cudaError_t launch_camera_rays(const CameraSetup& cam, uint32_t w, uint32_t h, float* rays, cudaStream_t stream)
 {
-    static int gShade = 0;
-    if (!gShade) gShade = blocks_for((const void*)k_wf_shade, kWfThreads);
+    const size_t n = size_t(w) * h;
+    if (n == 0) return cudaSuccess;
+    const int blocks = int(std::min<size_t>((n + 255) / 256, size_t(sm_count()) * 8));
+    k_camera_rays<<<blocks, 256, 0, stream>>>(cam, w, h, rays);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, const RenderBatch* bDev,
+                                    const WavefrontBuffers& wb, Counters* counters, cudaStream_t stream, int* launches)
+{
+    static const int gShade = blocks_for((const void*)k_wf_shade, kWfThreads);  // thread-safe one-time init
     const int gFlat = sm_count() * 8;
     int nl = 0;
     const uint32_t cap = wb.capacity;
@@ -366,10 +389,10 @@ cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, con
     const uint32_t scap = cap * lcap;
     Q q[2] = {{wb.ray[0], wb.sample[0], wb.group[0], wb.depth[0], cap},
               {wb.ray[1], wb.sample[1], wb.group[1], wb.depth[1], cap}};
-    k_wf_camera<<<gFlat, 256, 0, stream>>>(b, q[0], wb.accum, wb.count);
+    k_wf_camera<<<gFlat, 256, 0, stream>>>(bDev, q[0], wb.accum, wb.count);
     nl++;
     Query qa = b.q;
-    qa.precision = 0;
+    qa.precision = 0;  // shadow rays: any hit at level 0
     const float* sh = wb.shadow;
     const RaysSoA shadowRays {sh, sh + scap, sh + 2ull * scap, sh + 3ull * scap, sh + 4ull * scap, sh + 5ull * scap,
                               sh + 6ull * scap, wb.shadowGroup};
@@ -392,7 +415,7 @@ cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, con
                                                lcap, wb.accum);
         nl += 3;
     }
-    k_wf_finish<<<gFlat, 256, 0, stream>>>(b, wb.accum);
+    k_wf_finish<<<gFlat, 256, 0, stream>>>(bDev, wb.accum);
     nl++;
     if (launches) *launches += nl;
     return cudaGetLastError();

@@ -18,6 +18,33 @@ struct HitsSoA { float *t, *u, *v; int32_t *patch, *object; };
 cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, RaysSoA rays, const uint32_t* patch_ids,
                                uint32_t n, Query q, HitsSoA hits, Counters* counters, cudaStream_t stream);
 
+// One thread per ray with the whole search inline (the plain query path);
+// `group` applies where rays.group is null.  Any hit writes hits.patch only.
+cudaError_t launch_query_plain(const DevScene& S, RaysSoA rays, uint32_t n, uint32_t group, Query q, bool any,
+                               HitsSoA hits, Counters* counters, cudaStream_t stream);
+
+// A query request's slice in a batch: rays [base, base + n) of the batch
+// come from src[0..6] (ox oy oz dx dy dz tmax; tmax nullable) and their hits
+// go to out (any-hit: out.patch only).
+struct QueryChunk
+{
+    const float* src[7];
+    uint32_t group, n, base, pad;
+    HitsSoA out;
+};
+// hdr (device) = (chunks, total rays) of the batch; cap = the staging
+// capacity (SoA stride, grid size).
+cudaError_t launch_gather_rays(const QueryChunk* table, const uint32_t* hdr, uint32_t cap, float* rays,
+                               uint32_t* group, cudaStream_t stream);
+cudaError_t launch_scatter_hits(const QueryChunk* table, const uint32_t* hdr, uint32_t cap, HitsSoA hits, bool any,
+                                cudaStream_t stream);
+
+// The pure-FP64 closest-hit search (precision 2), one thread per ray: n rays
+// (or *nDev, with n bounding the grid), FP64 clip tolerance `tol`.
+constexpr double kTolFP64 = 1e-9;
+cudaError_t launch_query_fp64(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, double tol,
+                              HitsSoA hits, Counters* counters, cudaStream_t stream);
+
 // ---------------------------------------------------------- query engine --
 // Closest / any hit of n rays (n from the host, or *nDev when nDev != null;
 // capacity bounds both) by alternating traversal and clip passes
@@ -37,15 +64,17 @@ struct CameraSetup
     float half_dx, half_dy;
 };
 
-// One render request of a batch.  Its samples are the global sample indices
-// [sampleBase, sampleBase + width*height*spp); its pixels [pixelBase, pixelBase
-// + width*height).
+// One render request of a batch: rows [row0, row0 + height) of an image
+// whose camera set-up is `cam` (a request may be split into row chunks).  Its
+// samples are the global sample indices [sampleBase, sampleBase +
+// width*height*spp); its pixels [pixelBase, pixelBase + width*height).  fb and
+// linear point at the chunk's first row.
 struct DevRequest
 {
     CameraSetup cam;
     uint32_t group, width, height, spp;
     int depth;
-    uint32_t sampleBase, pixelBase, stride;
+    uint32_t sampleBase, pixelBase, stride, row0;
     uint32_t* fb;
     float* linear;
 };
@@ -85,10 +114,16 @@ struct WavefrontBuffers
     uint32_t lightCapacity;
 };
 
+// Primary rays (one per pixel centre) of a w x h image, SoA (7, w*h), tmax = inf.
+cudaError_t launch_camera_rays(const CameraSetup& cam, uint32_t w, uint32_t h, float* rays, cudaStream_t stream);
 cudaError_t launch_render_plain(const DevScene& S, const RenderBatch& b, const DevRequest* hostReq,
                                 Counters* counters, cudaStream_t stream, int* launches);
-cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, const WavefrontBuffers& wb,
-                                    Counters* counters, cudaStream_t stream, int* launches);
+// The wavefront schedule of batch b.  The kernels read the batch from bDev
+// (a device copy of b, uploaded by the caller), so that the launch sequence
+// depends only on the buffers, b.maxDepth, b.eps and b.q and can be replayed
+// from a captured CUDA graph for any batch of that shape.
+cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, const RenderBatch* bDev,
+                                    const WavefrontBuffers& wb, Counters* counters, cudaStream_t stream, int* launches);
 
 // ---------------------------------------------------------- perfect hash --
 struct HashScratch

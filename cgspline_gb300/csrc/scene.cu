@@ -17,7 +17,9 @@ namespace cgs {
 // comes from the size of a box that is never inflated (src/rt/BVH.cpp:46-52),
 // i.e. an empty box whose three extents compare equal, which selects y; the
 // partition is std::nth_element with the same comparator, so the topology
-// matches the reference built with the same standard library.
+// matches the reference built with the same standard library.  With
+// CGS_SPLIT_LONGEST the box is the elements' centroid box (the evident intent
+// of that code): same rule, same partition, the longest axis.
 uint32_t HostBVH::wrap(Element* e, size_t count, uint32_t key)
 {
     if (count == 0) emptyLeaf = true;
@@ -34,8 +36,10 @@ uint32_t HostBVH::wrap(Element* e, size_t count, uint32_t key)
 uint32_t HostBVH::split(Element* e, size_t count, uint32_t key)
 {
     if (count <= perNode || (key & (1u << 31))) return wrap(e, count, key);
-    Box empty;
-    float v[3] = {empty.hi[0] - empty.lo[0], empty.hi[1] - empty.lo[1], empty.hi[2] - empty.lo[2]};
+    Box box;
+    if (split_mode == CGS_SPLIT_LONGEST)
+        for (size_t i = 0; i < count; i++) box.inflate(e[i].centroid);
+    float v[3] = {box.hi[0] - box.lo[0], box.hi[1] - box.lo[1], box.hi[2] - box.lo[2]};
     const int dim = v[2] > v[1] ? (v[0] > v[2] ? 0 : 2) : (v[0] > v[1] ? 0 : 1);
     size_t middle = count / 2;
     std::nth_element(e, e + middle, e + count,
@@ -500,6 +504,15 @@ int cgs_scene_set_environment(cgs_scene* s, const float bg[3], const float amb[3
     return upload_lights(s);
 }
 
+int cgs_scene_set_bvh_split(cgs_scene* s, int mode)
+{
+    if (!s || (mode != CGS_SPLIT_REFERENCE && mode != CGS_SPLIT_LONGEST)) return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->splitMode != mode) s->bvhBuilt = s->uploaded = s->hashed = false;
+    s->splitMode = mode;
+    return CGS_OK;
+}
+
 int cgs_bvh_build(cgs_scene* s)
 {
     if (!s) return CGS_ERR_INVALID_ARGUMENT;
@@ -509,11 +522,13 @@ int cgs_bvh_build(cgs_scene* s)
         if (gr.objects.empty()) return CGS_ERR_EMPTY_LEAF;
     for (auto& sf : s->surfaces)
     {
+        sf.bvh.split_mode = s->splitMode;
         build_surface_bvh(sf);
         if (sf.bvh.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
     }
     for (auto& gr : s->groups)
     {
+        gr.top.split_mode = s->splitMode;
         build_group_bvh(s, gr);
         if (gr.top.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
     }

@@ -6,7 +6,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <initializer_list>
 #include <mutex>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/cgspline.h"
@@ -35,6 +39,7 @@ struct HostBVH
     std::vector<Node> nodes;
     std::vector<uint32_t> keys, indices;
     uint32_t perNode = 1;
+    int split_mode = CGS_SPLIT_REFERENCE;
     bool emptyLeaf = false;
     uint32_t wrap(Element* e, size_t count, uint32_t key);
     uint32_t split(Element* e, size_t count, uint32_t key);
@@ -100,12 +105,45 @@ inline int cuda_status(cudaError_t e)
         if (_e != cudaSuccess) return cuda_status(_e); \
     } while (0)
 
+// Executable CUDA graphs of launch sequences, keyed by a hash of everything a
+// sequence depends on (buffers, sizes, options).  A key runs eagerly the
+// first time (one-time initialisation, occupancy queries), is captured on
+// the second and replayed from then on.
+struct GraphCache
+{
+    struct Entry { cudaGraphExec_t exec; int launches; };
+    std::unordered_map<uint64_t, Entry> execs;
+    std::unordered_set<uint64_t> seen;
+    cudaStream_t capture = nullptr;
+    bool disabled = false;
+    uint64_t replays = 0, captures = 0;
+    void release();
+};
+
+// FNV-1a over 64-bit words.
+inline uint64_t key_of(std::initializer_list<uint64_t> words)
+{
+    uint64_t h = 1469598103934665603ull;
+    for (uint64_t w : words)
+        for (int k = 0; k < 8; k++) { h ^= (w >> (8 * k)) & 0xFF; h *= 1099511628211ull; }
+    return h;
+}
+inline uint64_t key_of(const void* p) { return uint64_t(reinterpret_cast<uintptr_t>(p)); }
+uint64_t scene_key(const DevScene& S);
+uint64_t query_key(const Query& q);
+
+// Runs fn(stream, &launches) -- a launch sequence -- through gc.
+cudaError_t run_cached(GraphCache& gc, uint64_t key, cudaStream_t stream, int* launches,
+                       const std::function<cudaError_t(cudaStream_t, int*)>& fn);
+
 // Device buffers of one in-flight render batch (wavefront queues, engine
 // scratch, request table, counters).  A scene owns one; the server owns one
 // per concurrently running batch.
 struct RenderSlot
 {
     WavefrontBuffers wb {};
+    DBuf<RenderBatch> batch;  // device copy of the batch description
+    GraphCache graphs;
     DBuf<float> ray0, ray1, shadow, contrib, base, accum, hitF;
     DBuf<uint32_t> smp0, smp1, grp0, grp1, dep0, dep1, count, shadowSlot, shadowGroup, engine;
     DBuf<int32_t> visible, hitI, occluded;
@@ -113,7 +151,9 @@ struct RenderSlot
     DBuf<Counters> counters;
     uint32_t engineCapacity = 0;
     int ensure(uint32_t samples, uint32_t lights, uint32_t nreq);
+    int ensure_engine(uint32_t rays);  // query-engine scratch for `rays` rays
     void release();
+    uint64_t bytes() const;
     static uint64_t bytes_for(uint32_t samples, uint32_t lights);
 };
 
@@ -127,6 +167,7 @@ struct cgs_scene
     std::vector<cgs::Object> objects;
     std::vector<cgs::Group> groups;
     uint32_t current = 0;  // group receiving add_object / set_lights / set_environment
+    int splitMode = CGS_SPLIT_REFERENCE;
     bool bvhBuilt = false, uploaded = false, hashed = false;
 
     // device side
@@ -184,7 +225,7 @@ void hash_coefficients(uint32_t n, uint32_t A[16], uint32_t B[16]);
 int ensure_engine(cgs_scene* sc, uint32_t capacity);
 inline bool valid_query(int method, int precision)
 {
-    return (method == 0 || method == 1) && precision >= 0 && precision <= 2;
+    return (method == 0 || method == 1) && precision >= 0 && precision <= 3;
 }
 // Fill `out` (device request table of `slot`) and the batch description for
 // n requests; validates them.  Returns a status.
@@ -192,5 +233,9 @@ int prepare_batch(cgs_scene* sc, const cgs_render_request* reqs, uint32_t n, con
                   std::vector<DevRequest>& host, RenderBatch& b);
 int run_batch(cgs_scene* sc, RenderSlot& slot, const std::vector<DevRequest>& host, RenderBatch& b, int schedule,
               cudaStream_t stream, int* launches);
+// The wavefront sequence of batch b (already uploaded to slot.batch, its
+// request table to slot.req) through the slot's graph cache.
+cudaError_t launch_wavefront_cached(const DevScene& S, RenderSlot& slot, const RenderBatch& b, cudaStream_t stream,
+                                    int* launches);
 
 }  // namespace cgs

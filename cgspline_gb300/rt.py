@@ -23,8 +23,9 @@ from . import _capi
 from ._capi import check
 
 CLIP, SUBDIV = 0, 1
-FP32, FP32_POLISH64, FP64 = 0, 1, 2
+FP32, FP32_POLISH64, FP64, FP32_GRAZE64 = 0, 1, 2, 3
 PLAIN, WAVEFRONT = 0, 1
+SPLIT_REFERENCE, SPLIT_LONGEST = 0, 1
 DEFAULT_TOL = 2.0 ** -12
 
 
@@ -61,7 +62,7 @@ class GpuScene:
     group k of the store (its own object-level BVH, lights and environment,
     sharing the patch and BVH arrays with the others)."""
 
-    def __init__(self, scene, device: int = 0, build: bool = True, stream=None):
+    def __init__(self, scene, device: int = 0, build: bool = True, stream=None, split: int = SPLIT_REFERENCE):
         self.lib = _capi.load()
         self.scenes = list(scene) if isinstance(scene, (list, tuple)) else [scene]
         self.scene = self.scenes[0]
@@ -71,6 +72,7 @@ class GpuScene:
         self.h = h
         self._keep = []
         self.surface_base = []
+        check(self.lib.cgs_scene_set_bvh_split(self.h, split), "cgs_scene_set_bvh_split")
         for g, sc in enumerate(self.scenes):
             if g > 0:
                 gid = C.c_uint32()
@@ -304,6 +306,16 @@ def camera_struct(cam) -> _capi.Camera:
                         cam.fovy)
 
 
+def camera_rays(camera, width: int, height: int, flip_y: bool = False, device: int = 0, stream=None):
+    """Primary rays of a width x height frame (cgs_camera_rays): (7, w*h) float32 CUDA tensor."""
+    torch = _torch()
+    lib = _capi.load()
+    rays = torch.empty((7, width * height), dtype=torch.float32, device=f"cuda:{device}")
+    check(lib.cgs_camera_rays(C.byref(camera_struct(camera)), width, height, int(flip_y), _ptr(rays),
+                              _stream_handle(stream)), "cgs_camera_rays")
+    return rays
+
+
 class RayTracer:
     """rt::RayTracer: asynchronous render of a resident scene into a device frame."""
 
@@ -342,6 +354,75 @@ class RayTracer:
 
     def running(self) -> bool:
         return bool(self._scene is not None and self.lib.cgs_render_running(self._scene.h))
+
+
+class Server:
+    """Continuous-batching request server over a resident GpuScene
+    (cgs_server_*): render and ray-query requests of any groups, cut into
+    chunks that fit a slot's share of `memory_budget`, batched and run on
+    `slots` concurrent streams.  Options.schedule = PLAIN gives the
+    one-request-per-launch baseline (one slot, the plain kernels)."""
+
+    def __init__(self, scene: GpuScene, slots: int = 4, memory_budget: int = 16 << 30, max_batch_samples: int = 0,
+                 max_batch_requests: int = 0, options: Options | None = None):
+        self.lib = _capi.load()
+        self.scene = scene
+        self.options = options or Options()
+        o = _capi.ServerOptions(slots, memory_budget, max_batch_samples, max_batch_requests, self.options.c())
+        h = C.c_void_p()
+        check(self.lib.cgs_server_create(C.byref(h), scene.h, C.byref(o)), "cgs_server_create")
+        self.h = h
+        self._keep = {}
+
+    def submit_render(self, req: "Request") -> int:
+        t = C.c_uint64()
+        check(self.lib.cgs_server_submit_render(self.h, C.byref(req.c()), C.byref(t)), "cgs_server_submit_render")
+        self._keep[t.value] = req
+        return t.value
+
+    def submit_query(self, group: int, rays, any_hit: bool = False, out=None):
+        """rays: (7, n) float32 CUDA tensor.  Returns (ticket, hits dict of device tensors)."""
+        torch = _torch()
+        n = rays.shape[1]
+        if out is None:
+            fo = torch.empty((3, n), dtype=torch.float32, device=rays.device)
+            io = torch.empty((2, n), dtype=torch.int32, device=rays.device)
+        else:
+            fo, io = out
+        r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)], None)
+        h = _capi.Hits(fo[0].data_ptr(), fo[1].data_ptr(), fo[2].data_ptr(), io[0].data_ptr(), io[1].data_ptr())
+        q = _capi.QueryRequest(group, n, int(any_hit), r, h)
+        t = C.c_uint64()
+        check(self.lib.cgs_server_submit_query(self.h, C.byref(q), C.byref(t)), "cgs_server_submit_query")
+        self._keep[t.value] = (rays, fo, io)
+        return t.value, dict(t=fo[0], u=fo[1], v=fo[2], patch=io[0], object=io[1])
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> dict:
+        info = _capi.RequestInfo()
+        st = self.lib.cgs_server_wait(self.h, ticket, timeout, C.byref(info))
+        check(st, "cgs_server_wait")
+        self._keep.pop(ticket, None)
+        return {k: getattr(info, k) for k, _ in _capi.RequestInfo._fields_}
+
+    def clock(self) -> float:
+        return float(self.lib.cgs_server_clock(self.h))
+
+    def stats(self) -> dict:
+        s = _capi.ServerStats()
+        check(self.lib.cgs_server_stats_get(self.h, C.byref(s)), "cgs_server_stats_get")
+        return {k: getattr(s, k) for k, _ in _capi.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cgs_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PerfectHashFunction:

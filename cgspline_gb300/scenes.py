@@ -323,13 +323,12 @@ def cube_sphere_surface(radius: float = 1.0, n: int = 2, sigma: float = 0.02, se
         r[inter] = radius + sigma * rng.normal(int(inter.sum()))
         P = nrm * r[..., None]
         pts.append(np.concatenate([P.reshape(-1, 3), np.ones((g * g, 1))], axis=1))
-        base = f * g * g
-        for pb in range(n):
-            for pa in range(n):
-                for j in range(4):
-                    for i in range(4):
-                        idx.append(base + (3 * pa + i) * g + (3 * pb + j))
-    return Surface(np.concatenate(pts).astype(np.float32), np.asarray(idx, dtype=np.uint32))
+        # patch (pa, pb) of the face, b-major; point (i, j) at 4j + i
+        pb, pa = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        j, i = np.meshgrid(np.arange(4), np.arange(4), indexing="ij")
+        ix = f * g * g + (3 * pa.reshape(-1, 1) + i.reshape(1, -1)) * g + (3 * pb.reshape(-1, 1) + j.reshape(1, -1))
+        idx.append(ix.reshape(-1))
+    return Surface(np.concatenate(pts).astype(np.float32), np.concatenate(idx).astype(np.uint32))
 
 
 def _rotation(q):
@@ -351,6 +350,45 @@ def _transforms(R, scale, t):
     return M.T.reshape(16).astype(np.float32), W.T.reshape(16).astype(np.float32)
 
 
+# The perfect hash of the reference (16 trials, src/rt/PerfectHashFunction.cu:
+# 229-503) finds no injective table for the heap-key sets of some BVH sizes,
+# and the BVH's key set depends only on its leaf count.  These grid sizes of
+# torus_surface (2 nv^2 patches, nv = 3..260) and cube_sphere_surface (6 n^2
+# patches, n = 1..150) are such sizes; the generators below step down to the
+# next size that hashes.  (Listed from the oracle's restatement of the hash;
+# a CPU test re-derives them.)
+TORUS_NV_NO_HASH = frozenset((
+    17, 24, 33, 46, 47, 48, 65, 66, 67, 70, 91, 92, 93, 94, 95, 96, 97, 129, 130, 131, 132, 133, 135, 136, 137,
+    182, 183, 184, 185, 186, 187, 188, 189, 190, 191, 192, 193, 194, 195, 196, 197, 198, 199, 200, 201, 202, 204,
+    205, 206, 207, 208, 211, 212, 213, 216, 224, 228, 229, 230, 237, 254, 256, 257, 258, 259, 260))
+SPHERE_N_NO_HASH = frozenset((
+    19, 27, 37, 38, 39, 53, 54, 55, 75, 76, 77, 78, 105, 106, 107, 108, 109, 110, 111, 112, 113, 114, 115, 116,
+    118, 119, 120, 148, 149, 150))
+
+
+def bvh_keys(leaves: int) -> np.ndarray:
+    """Heap keys, in node order, of the median-split BVH over `leaves`
+    elements with one element per leaf (BVH::split, src/rt/BVH.cpp:40-80):
+    the key set depends only on the leaf count."""
+    out = []
+    stack = [(leaves, 1)]
+    while stack:
+        count, key = stack.pop()
+        out.append(key)
+        if count <= 1:
+            continue
+        m = count // 2
+        stack.append((count - m, (key << 1) ^ 1))
+        stack.append((m, key << 1))
+    return np.asarray(out, dtype=np.uint32)
+
+
+def _hashable(n: int, bad: frozenset, lo: int) -> int:
+    while n > lo and n in bad:
+        n -= 1
+    return n
+
+
 def scene_c4(index: int, seed: int = 4, min_patches: int = 256, max_patches: int = 65536) -> Scene:
     """Scene `index` of the 64-scene batching workload: a seeded random union
     of 8..64 displaced cube-spheres and tori (the torus of scene_c2 on a
@@ -370,10 +408,10 @@ def scene_c4(index: int, seed: int = 4, min_patches: int = 256, max_patches: int
         pos = rng.uniform(3, -4.0, 4.0)
         sseed = int(rng.u64(1)[0] >> np.uint64(12))
         if kind < 0.5:
-            n = max(1, int(np.floor(np.sqrt(per / 6.0) + 0.5)))
+            n = _hashable(max(1, int(np.floor(np.sqrt(per / 6.0) + 0.5))), SPHERE_N_NO_HASH, 1)
             surf = cube_sphere_surface(1.0, n, 0.03, sseed)
         else:
-            nv = max(3, int(np.floor(np.sqrt(per / 2.0) + 0.5)))
+            nv = _hashable(max(3, int(np.floor(np.sqrt(per / 2.0) + 0.5))), TORUS_NV_NO_HASH, 3)
             surf = torus_surface(1.0, 0.35, 2 * nv, nv, 0.02, sseed)
         surfaces.append(surf)
         l2w, w2l = _transforms(_rotation(qv), 0.5 + sc, pos)
@@ -403,6 +441,17 @@ def camera_c4(index: int, seed: int = 4):
     cam = Camera(look_at(d, (0.0, 0.0, 0.0), up), tuple(float(np.float32(c)) for c in d), (1, 1, 1),
                  float(np.float32(math.radians(50.0))))
     return cam, side
+
+
+# ----------------------------------------------------------------- C5 ----
+def scene_c5(index: int, seed: int = 5) -> Scene:
+    """Resident scene `index` of the serving workload: the union generator of
+    scene_c4 with 1,024..1,048,576 patches (log-uniform)."""
+    return scene_c4(index, seed=seed, min_patches=1024, max_patches=1 << 20)
+
+
+def camera_c5(index: int, seed: int = 5) -> Camera:
+    return camera_c4(index, seed=seed)[0]
 
 
 def bernstein(t: np.ndarray):

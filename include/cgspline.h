@@ -39,9 +39,22 @@ int cgs_version(void);
 
 /* ----------------------------------------------------------- options -- */
 enum cgs_method { CGS_METHOD_CLIP = 0, CGS_METHOD_SUBDIV = 1 };
-/* FP32: the reference's arithmetic.  FP32_POLISH64: FP32 search, then an FP64
- * Newton polish of (u,v,t) of the winning hit.  FP64: the whole search in FP64. */
-enum cgs_precision { CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP64 = 2 };
+/* Precision of closest-hit searches.  FP32: the reference's arithmetic.
+ * FP32_POLISH64: FP32 search and traversal, then an FP64 Newton polish of
+ * (u,v,t) of the winning hit.  FP32_GRAZE64 (the full precision form):
+ * FP32_POLISH64, and candidates the ray meets within 30 degrees of grazing
+ * (of the plane of the patch's diagonals) are searched on a net projected in
+ * FP64 with FP64 fat-line bounds to tolerance 2^-20.  FP64: the whole search
+ * in FP64 (traversal, clipping to 1e-9, every root polished), the comparison
+ * run of the precision form.  Any-hit searches (shadow rays, any_hit
+ * queries) always run in FP32. */
+enum cgs_precision { CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP64 = 2, CGS_PREC_FP32_GRAZE64 = 3 };
+/* Split axis of the BVH build.  REFERENCE: BVH::split's axis, taken from a
+ * box that is never inflated (src/rt/BVH.cpp:46-52) and so always y -- the
+ * reference's topology, bit for bit.  LONGEST: the longest axis of the
+ * elements' centroid box, everything else unchanged: the same hits (up to
+ * ties between equally distant candidates) with far fewer node visits. */
+enum cgs_bvh_split { CGS_SPLIT_REFERENCE = 0, CGS_SPLIT_LONGEST = 1 };
 /* PLAIN: one thread per pixel runs the whole bounce chain (the reference's
  * launch shape, src/rt/RayTracer.cu:171-178).  WAVEFRONT: persistent,
  * stage-separated kernels over compacted ray queues. */
@@ -144,6 +157,9 @@ int cgs_scene_set_environment(cgs_scene* scene, const float background[3], const
  * environment calls apply to the current group; surfaces are shared. */
 int cgs_scene_add_group(cgs_scene* scene, uint32_t* group_id);
 
+/* Split axis (enum cgs_bvh_split) of the next cgs_bvh_build; default REFERENCE. */
+int cgs_scene_set_bvh_split(cgs_scene* scene, int mode);
+
 /* BVH::build for every surface (BezierSurface::buildBVH, src/rt/Primitive.cu:199-220)
  * and the object level (Scene::buildBVH, src/rt/Scene.cu:218-232): host median
  * split, one element per leaf (src/rt/BVH.cpp:9-124). */
@@ -228,6 +244,13 @@ typedef struct cgs_render_request {
 int cgs_render_batch(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,
                      const cgs_render_options* options, void* stream);
 
+/* The primary rays of RayTracer::render (src/rt/RayTracer.cu:59-71,152-163):
+ * one ray per pixel centre of a width x height image, written to the device
+ * array rays as SoA (7, width*height) = ox oy oz dx dy dz tmax (= +inf).
+ * Asynchronous on `stream`. */
+int cgs_camera_rays(const cgs_camera* camera, uint32_t width, uint32_t height, int flip_y, float* rays,
+                    void* stream);
+
 /* RayTracer::running (src/rt/RayTracer.h:45-48): 1 while a render is in flight. */
 int cgs_render_running(cgs_scene* scene);
 
@@ -260,6 +283,77 @@ int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uin
 #define CGS_NOALLOC_MAX_KEYS 262144u
 int cgs_perfect_hash_build_noalloc(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t displ_capacity,
                                    uint32_t* table, uint32_t table_capacity, uint32_t params[5], void* stream);
+
+/* ------------------------------------------------------------ serving -- */
+/* A request server over a built scene store.  Render and ray-query requests
+ * of any groups are queued on submit, cut into chunks (row ranges of an image,
+ * ranges of a ray array) that fit one slot's share of the device-memory
+ * budget, and packed into batches that run on `slots` concurrent streams.  A
+ * batch starts as soon as a slot is free, so requests that arrive while
+ * others run are admitted and overlap with them on the device (continuous
+ * batching).  Every sample and ray is computed exactly as by cgs_render_batch
+ * and cgs_intersect, so a request's result does not depend on what it was
+ * batched with.  The reference has no counterpart: its RayTracer renders one
+ * frame at a time on a worker thread (src/rt/RayTracer.cu:107-180); with
+ * schedule CGS_SCHED_PLAIN the server behaves that way (one slot, one request
+ * per launch, the plain kernel, no chunking), which is the per-request
+ * baseline.  The scene store must not change while a server uses it. */
+typedef struct cgs_server cgs_server;
+
+typedef struct cgs_server_options {
+    uint32_t slots;              /* concurrent batches (streams), 1..16 */
+    uint64_t memory_budget;      /* device bytes for all slots' working buffers
+                                    (the resident scenes are not counted) */
+    uint32_t max_batch_samples;  /* primary samples or query rays per batch; 0 = what a slot's share holds */
+    uint32_t max_batch_requests; /* chunks per batch; 0 = 256 */
+    cgs_render_options render;   /* eps, flip_y, method, precision, tol, schedule for every request */
+} cgs_server_options;
+
+/* A ray query: closest or any hit of n rays (device SoA) in one group. */
+typedef struct cgs_query_request {
+    uint32_t group;
+    uint32_t n;
+    int any_hit;
+    cgs_rays rays;   /* device; rays.group is ignored (the request's group applies) */
+    cgs_hits hits;   /* device; any_hit writes only hits.patch (0 occluded, -1 free) */
+} cgs_query_request;
+
+typedef struct cgs_request_info {
+    int status;          /* CGS_OK, or the error that ended the request */
+    uint32_t chunks;     /* chunks the request was cut into */
+    double submit_s;     /* server clock at submit, first launch and completion */
+    double start_s;
+    double finish_s;
+    uint64_t samples;    /* primary samples (renders) or rays (queries) */
+} cgs_request_info;
+
+typedef struct cgs_server_stats {
+    uint64_t submitted, finished, rejected;
+    uint64_t batches, chunks;
+    uint64_t rays_traced;        /* every ray the device traced (primary, bounce, shadow, query) */
+    uint64_t slot_bytes;         /* device bytes held by the slots now */
+    uint64_t peak_slot_bytes;
+    uint64_t kernel_launches;
+    double busy_s;               /* time with at least one batch in flight */
+    uint32_t max_batch_samples;  /* the per-batch limit in force */
+    uint32_t queued;             /* chunks waiting */
+} cgs_server_stats;
+
+int cgs_server_create(cgs_server** server, cgs_scene* scene, const cgs_server_options* options);
+/* Finishes every submitted request, then frees the server. */
+int cgs_server_destroy(cgs_server* server);
+/* Queue a request; *ticket identifies it.  CGS_ERR_ADMISSION when one row
+ * (render) or one ray (query) cannot fit a slot's memory share, or when the
+ * request needs more lights than the slots were sized for. */
+int cgs_server_submit_render(cgs_server* server, const cgs_render_request* request, uint64_t* ticket);
+int cgs_server_submit_query(cgs_server* server, const cgs_query_request* request, uint64_t* ticket);
+/* Wait up to timeout_s seconds (< 0: without limit) for a request.  CGS_OK
+ * with its info once it has finished (the ticket is then released),
+ * CGS_ERR_BUSY on timeout, CGS_ERR_NOT_FOUND for an unknown ticket. */
+int cgs_server_wait(cgs_server* server, uint64_t ticket, double timeout_s, cgs_request_info* info);
+/* Seconds since the server was created (the clock of cgs_request_info). */
+double cgs_server_clock(const cgs_server* server);
+int cgs_server_stats_get(cgs_server* server, cgs_server_stats* stats);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,12 @@ LIB = os.path.join(BUILD, "libcgs_oracle.so")
 SRC = os.path.join(HERE, "cgs_oracle.cpp")
 
 CLIP_HOST, CLIP_DEVICE, SUBDIV = 0, 1, 2
+# the precision form's clip: CLIP_DEVICE, with near-grazing candidates (ray
+# within GRAZE_5 / GRAZE_30 of the plane of the patch diagonals, graze_sin of
+# intersect) searched on an FP64-projected net with FP64 fat-line bounds to
+# tolerance 2^-20
+CLIP_GRAZE64 = 5
+GRAZE_5, GRAZE_30 = 0.0871557427, 0.5
 FP32, FP32_POLISH64, FP64 = 0, 1, 2
 
 
@@ -52,6 +58,8 @@ def lib():
         L.ora_scene_set_lights.argtypes = [P, P, C.c_uint32]
         L.ora_scene_set_env.argtypes = [P, fp, fp]
         L.ora_scene_build.argtypes = [P]
+        L.ora_scene_set_split.argtypes = [P, C.c_int]
+        L.ora_set_graze_sin.argtypes = [C.c_float]
         L.ora_bvh_sizes.argtypes = [P, C.c_int, u32]
         L.ora_bvh_export.argtypes = [P, C.c_int, u32, u32, u32, u32, u32, u32]
         L.ora_hash_build.argtypes = [u32, C.c_uint32, u32, u32, C.c_uint32, u32, C.c_uint32]
@@ -78,10 +86,13 @@ def _ptr(a):
 class OracleScene:
     """A built scene (BVHs + perfect hashes) in the oracle."""
 
-    def __init__(self, scene):
+    def __init__(self, scene, split=0):
+        """split: 0 the reference's BVH split axis (always y), 1 the longest
+        axis of the elements' centroid box."""
         L = lib()
         self.scene = scene
         self.h = L.ora_scene_new()
+        L.ora_scene_set_split(self.h, split)
         for s in scene.surfaces:
             pts = np.ascontiguousarray(s.points, np.float32)
             idx = np.ascontiguousarray(s.indices, np.uint32)
@@ -132,8 +143,11 @@ class OracleScene:
                     A=int(par[0]), B=int(par[1]), N=int(par[2]), mask=int(par[3]))
 
     def intersect(self, rays, method=CLIP_HOST, precision=FP32, tol=2.0 ** -12, tol64=1e-9, any_hit=False,
-                  nthreads=None, counters=False):
+                  nthreads=None, counters=False, graze_sin=GRAZE_30):
+        """graze_sin: the grazing margin of CLIP_GRAZE64 (GRAZE_5 restates the
+        GPU's FP32_POLISH64 level, GRAZE_30 its FP32_GRAZE64 level)."""
         L = lib()
+        L.ora_set_graze_sin(graze_sin)
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[1]
         of = np.zeros((3, n), np.float32)

@@ -438,7 +438,26 @@ template<class R, class F> bool clip2d_host(F& onHit, const V2<R>* patch, R tol,
 // half-precision (mid,len) stack replaced by a full-precision (min,max) stack
 // of the same depth (32).  The CUDA product follows this structure; this copy
 // lets the tests compare against it directly.
-template<class R, class F> bool clip2d_device(F& onHit, const V2<R>* patch, R tol, ClipStats* st)
+// FP64 fat-line bounds of an FP32 sub-net (the precision form's variant for
+// near-grazing candidates): the distances, hull scan and epsilons of
+// clip_range in double, the interval rounded outward to float.
+inline void clip_range_f64(const V2<float>* p, int cutside, float& lower, float& upper)
+{
+    V2<double> q[16];
+    for (int i = 0; i < 16; i++) q[i] = {double(p[i].x), double(p[i].y)};
+    double lo, hi;
+    clip_range<double>(q, cutside, lo, hi);
+    lower = float(lo);
+    if (double(lower) > lo) lower = std::nextafter(lower, -INFINITY);
+    upper = float(hi);
+    if (double(upper) < hi) upper = std::nextafter(upper, INFINITY);
+}
+inline void clip_range_f64(const V2<double>* p, int cutside, double& lower, double& upper)
+{
+    clip_range<double>(p, cutside, lower, upper);
+}
+
+template<class R, class F, bool kBounds64 = false> bool clip2d_device(F& onHit, const V2<R>* patch, R tol, ClipStats* st)
 {
     struct State { V2<R> min, max; };
     bool found = false;
@@ -448,8 +467,11 @@ template<class R, class F> bool clip2d_device(F& onHit, const V2<R>* patch, R to
     State e {{0, 0}, {1, 1}};
     V2<R> buf[16];
     for (int i = 0; i < 16; i++) buf[i] = patch[i];
+    int it = 0;
     do
     {
+        // the near-grazing variant keeps what it found after 1024 iterations
+        if (kBounds64 && it++ >= 1024) return found;
         if (st) st->iterations++;
         const int cutside = cutsideStack & 1;
         R d0 = length(buf[3] - buf[12]);
@@ -459,7 +481,8 @@ template<class R, class F> bool clip2d_device(F& onHit, const V2<R>* patch, R to
         else
         {
             R lower, upper;
-            clip_range(buf, cutside, lower, upper);
+            if constexpr (kBounds64) clip_range_f64(buf, cutside, lower, upper);
+            else clip_range(buf, cutside, lower, upper);
             R delta = upper - lower;
             if (delta > R(0.8f))
             {
@@ -587,7 +610,22 @@ template<class R, class F> bool subdiv2d(F& onHit, const V2<R>* patch, R tol, Cl
 template<class R> struct Ray { V3<R> o, d; R max; };
 struct PatchHit { float t; float u, v; };
 
-enum Method { kClipHost = 0, kClipDevice = 1, kSubdiv = 2 };
+// kClipDeviceB64: kClipDevice with FP64 fat-line bounds; kClipDeviceB64P:
+// the same on a net projected in FP64 (rounded to the search type).
+// kClipGraze: the precision form's clip -- kClipDevice, except that a
+// near-grazing candidate (the ray within asin(g_grazeSin) of the plane of
+// the patch's diagonals: 5 degrees for CGS_PREC_FP32_POLISH64, 30 for
+// CGS_PREC_FP32_GRAZE64) gets kClipDeviceB64P with tolerance 2^-20.
+enum Method { kClipHost = 0, kClipDevice = 1, kSubdiv = 2, kClipDeviceB64 = 3, kClipDeviceB64P = 4, kClipGraze = 5 };
+static float g_grazeSin = 0.5f;
+constexpr float kGrazeTol = 0x1p-20f;
+template<class R> inline bool grazing(const V4<R> P[16], V3<R> d)
+{
+    V3<R> a = xyz(P[15]) - xyz(P[0]), b = xyz(P[12]) - xyz(P[3]);
+    V3<R> n = cross(a, b);
+    R l = length(n);
+    return l > R(0) && std::fabs(dot(n, d)) < R(g_grazeSin) * l;
+}
 
 // spline::doBezierClipping / doSubdivision_device front end,
 // src/Spline_BezierClipping.cu:46-114 and src/Spline_Subdivision.cu:111-165:
@@ -600,11 +638,28 @@ bool intersect_patch(R& distance, V2<R>& uv, const Ray<R>& ray, const V4<R> P[16
     const V3<R> axis0 = versor(cross(d, d + V3<R>{0, 0, 8}));
     const V3<R> axis1 = versor(cross(d, axis0));
     V2<R> net[16];
-    for (int i = 0; i < 16; i++)
+    if (method == kClipGraze)
     {
-        V3<R> Q = xyz(P[i]);
-        net[i] = {dot(axis0, Q - ray.o), dot(axis1, Q - ray.o)};
+        if (grazing(P, d)) { method = kClipDeviceB64P; tol = R(kGrazeTol); }
+        else method = kClipDevice;
     }
+    if (method == kClipDeviceB64P)
+    {
+        const V3<double> dd = cast3<double>(d), oo = cast3<double>(ray.o);
+        const V3<double> a0 = versor(cross(dd, dd + V3<double>{0, 0, 8}));
+        const V3<double> a1 = versor(cross(dd, a0));
+        for (int i = 0; i < 16; i++)
+        {
+            V3<double> Q = cast3<double>(xyz(P[i])) - oo;
+            net[i] = {R(dot(a0, Q)), R(dot(a1, Q))};
+        }
+    }
+    else
+        for (int i = 0; i < 16; i++)
+        {
+            V3<R> Q = xyz(P[i]);
+            net[i] = {dot(axis0, Q - ray.o), dot(axis1, Q - ray.o)};
+        }
     auto onHit = [&](V2<R> e) -> bool {
         V3<R> V = project(interpolate(P, e.x, e.y)) - ray.o;
         R t = length(V);
@@ -615,6 +670,8 @@ bool intersect_patch(R& distance, V2<R>& uv, const Ray<R>& ray, const V4<R> P[16
     {
     case kClipHost: return clip2d_host(onHit, net, tol, st);
     case kClipDevice: return clip2d_device(onHit, net, tol, st);
+    case kClipDeviceB64:
+    case kClipDeviceB64P: return clip2d_device<R, decltype(onHit), true>(onHit, net, tol, st);
     default: return subdiv2d(onHit, net, tol, st);
     }
 }
@@ -669,6 +726,7 @@ struct BVH
     std::vector<uint32_t> keys, indices, table;
     Hash hash;
     uint32_t elementsPerNode = 1;
+    int splitMode = 0;  // 0: the reference's axis (an empty box: y); 1: longest axis of the centroid box
 
     // BVH::wrap, src/rt/BVH.cpp:82-108
     uint32_t wrap(Element* e, size_t count, uint32_t key)
@@ -688,7 +746,9 @@ struct BVH
     uint32_t split(Element* e, size_t count, uint32_t key)
     {
         if (count <= elementsPerNode || (key & (1u << 31))) return wrap(e, count, key);
-        Box box;
+        Box box;  // never inflated in the reference (src/rt/BVH.cpp:46-52)
+        if (splitMode == 1)
+            for (size_t i = 0; i < count; i++) box.inflate(e[i].centroid);
         V3<float> v = box.size();
         int dim = v.z > v.y ? (v.x > v.z ? 0 : 2) : (v.x > v.y ? 0 : 1);
         size_t middle = count / 2;
@@ -1005,15 +1065,18 @@ struct Scene
         }
         top.build(el, 1);
     }
+    int splitMode = 0;
     int build()
     {
         for (auto& s : surfaces)
         {
+            s.bvh.splitMode = splitMode;
             build_surface_bvh(s);
             int e = hash_build(s.bvh.hash, s.bvh.table, s.bvh.keys.data(), uint32_t(s.bvh.keys.size()));
             if (e) return 10 + e;
         }
         if (objects.empty()) return 1;
+        top.splitMode = splitMode;
         build_top();
         int e = hash_build(top.hash, top.table, top.keys.data(), uint32_t(top.keys.size()));
         if (e) return 20 + e;
@@ -1431,6 +1494,9 @@ void ora_scene_set_env(void* s_, const float* bg3, const float* amb3)
 }
 
 int ora_scene_build(void* s_) { return static_cast<Scene*>(s_)->build(); }
+void ora_scene_set_split(void* s_, int mode) { static_cast<Scene*>(s_)->splitMode = mode; }
+// the grazing margin of kClipGraze (process-wide; not thread-safe against running queries)
+void ora_set_graze_sin(float s) { g_grazeSin = s; }
 
 static const BVH* pick_bvh(const Scene* s, int which)
 {

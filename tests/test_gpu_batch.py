@@ -168,3 +168,29 @@ def test_invalid_batches_raise(rt, store, torch):
     res = store.intersect(rays, group=torch.tensor([0, 9, 1, 2], dtype=torch.int32))
     assert res["patch"].cpu().tolist()[1] == -1 and res["patch"].cpu().tolist()[3] == -1
     assert store.counters()["device_errors"] == 8
+
+
+def test_union_scenes_batch_matches_oracle(rt, oracle_mod, torch):
+    """Four seeded unions of cube-spheres and tori (the batching workload's
+    generator, capped at 2,048 patches) in one store, rendered as one batch
+    with one bounce, each against the oracle of its own scene."""
+    scs = [S.scene_c4(i, max_patches=2048) for i in range(4)]
+    store = rt.GpuScene(scs)
+    cams = [S.camera_c4(i)[0] for i in range(4)]
+    reqs = [rt.Request.alloc(i, cams[i], 72, 56, recursion_depth=1, linear=True) for i in range(4)]
+    rt.RayTracer(rt.Options(precision=rt.FP32_POLISH64)).render_batch(reqs, store)
+    torch.cuda.synchronize()
+    assert store.counters()["device_errors"] == 0
+    for i in range(4):
+        ro = oracle_mod.OracleScene(scs[i]).render(cams[i], 72, 56, depth=1)
+        err = np.abs(reqs[i].linear.cpu().numpy() - ro["rgb"])
+        assert float(np.sqrt((err ** 2).mean())) < 5e-3, i
+        assert (err.max(axis=-1) > 0.05).mean() < 5e-3, i
+
+
+def test_camera_rays_match_oracle(rt, oracle_mod, torch):
+    for cam, w, h in ((S.camera_c1(), 37, 23), (S.camera_c2(), 64, 36), (S.camera_c4(5)[0], 16, 16)):
+        g = rt.camera_rays(cam, w, h).cpu().numpy()
+        o = oracle_mod.camera_rays(cam, w, h)
+        assert np.array_equal(g[:3], o[:3]) and np.isinf(g[6]).all()
+        assert np.abs(g[3:6] - o[3:6]).max() < 1e-6  # a few ulps: FMA contraction differs

@@ -229,3 +229,23 @@ def test_long_runs_of_misses_do_not_end_the_query(c1_gpu, c1_oracle, oracle_mod,
     ga = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda(), any_hit=True))
     oa = c1_oracle.intersect(rays, any_hit=True)
     assert np.array_equal(ga["patch"] >= 0, oa["patch"] >= 0)
+
+
+def test_longest_axis_split_bit_exact_and_same_hits(rt, c2_small, c2_small_gpu, oracle_mod, torch):
+    """CGS_SPLIT_LONGEST: the BVHs and hash tables equal the oracle's
+    longest-axis build bit for bit, and the hits equal the reference-split
+    store's (t within 1e-6 relative where the patch differs only by a tie)."""
+    g = rt.GpuScene(c2_small, split=rt.SPLIT_LONGEST)
+    o = oracle_mod.OracleScene(c2_small, split=1)
+    for which in (0, -1):
+        a, b = g.bvh(which), o.bvh(which)
+        for k in ("nodes", "keys", "indices", "table", "disp"):
+            assert np.array_equal(a[k], b[k]), (which, k)
+    rays = torch.from_numpy(oracle_mod.camera_rays(S.camera_c2(), 160, 90)).cuda()
+    r1 = to_host(c2_small_gpu.intersect(rays))
+    r2 = to_host(g.intersect(rays))
+    assert np.array_equal(r1["patch"] >= 0, r2["patch"] >= 0)
+    hit = r1["patch"] >= 0
+    rel = np.abs(r1["t"][hit] - r2["t"][hit]) / r1["t"][hit]
+    assert rel.max(initial=0) <= 1e-6
+    assert (r1["patch"] != r2["patch"])[hit].mean() < 1e-3

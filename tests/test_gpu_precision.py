@@ -1,0 +1,102 @@
+"""GPU tests of the precision form: the pure-FP64 GPU search against the FP64
+oracle, and the FP32 + FP64-polish search against the pure-FP64 GPU search on
+seeded grazing rays (directions within 0.5 degrees of the tangent plane).
+
+Bars: FP64 GPU vs FP64 oracle -- hit/miss identical on camera rays and on
+all but 1e-3 of the grazing rays (the GPU clip re-derives sub-nets where the
+oracle's keeps them, which moves marginal roots by rounding), t within 1e-9
+relative on hits of the same patch.  FP32 + polish vs FP64 GPU -- t within
+1e-5 relative on hits of the same patch.
+"""
+import numpy as np
+import pytest
+
+from cgspline_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    return torch
+
+
+@pytest.fixture(scope="module")
+def rt():
+    from cgspline_gb300 import rt
+    return rt
+
+
+@pytest.fixture(scope="module")
+def torus():
+    return S.scene_c2(nu=32, nv=32)
+
+
+@pytest.fixture(scope="module")
+def torus_gpu(rt, torus):
+    return rt.GpuScene(torus)
+
+
+def host(d):
+    return {k: v.cpu().numpy() for k, v in d.items()}
+
+
+def rel_err(a, b):
+    same = (a["patch"] >= 0) & (a["patch"] == b["patch"]) & (a["object"] == b["object"])
+    return np.abs(a["t"][same] - b["t"][same]) / np.abs(b["t"][same]), same
+
+
+@pytest.mark.parametrize("kind", ["camera", "grazing"])
+def test_fp64_gpu_matches_fp64_oracle(rt, torus, torus_gpu, oracle_mod, torch, kind):
+    if kind == "camera":
+        rays = oracle_mod.camera_rays(S.camera_c2(), 96, 54)
+    else:
+        rays = S.grazing_rays(torus.surfaces[0], 4096, seed=11)
+    o = oracle_mod.OracleScene(torus).intersect(rays, precision=oracle_mod.FP64)
+    g = host(torus_gpu.intersect(torch.from_numpy(rays).cuda(), precision=rt.FP64))
+    hm = int(((g["patch"] >= 0) != (o["patch"] >= 0)).sum())
+    if kind == "camera":
+        assert hm == 0
+    else:
+        assert hm <= rays.shape[1] // 1000, hm
+    rel, same = rel_err(g, o)
+    assert same.sum() > 0.3 * rays.shape[1]
+    assert rel.max(initial=0.0) < 1e-9, rel.max()
+    assert torus_gpu.counters()["device_errors"] == 0
+
+
+def test_precision_form_on_grazing_rays(rt, torus, torus_gpu, oracle_mod, torch):
+    """FP32 + FP64 polish with the FP64 fat-line bounds of near-grazing
+    candidates (FP32_GRAZE64) against the pure-FP64 GPU search on grazing
+    rays: the plain FP32 search (the reference's arithmetic) loses ~1% of
+    these hits, the precision form keeps hit/miss within 1e-3; the oracle's
+    restatement of the same variant agrees on hit/miss."""
+    level = "graze64"
+    prec = rt.FP32_GRAZE64
+    gs = oracle_mod.GRAZE_30
+    host_rays = S.grazing_rays(torus.surfaces[0], 1 << 14, seed=12)
+    rays = torch.from_numpy(host_rays).cuda()
+    ref = host(torus_gpu.intersect(rays, precision=rt.FP64))
+    p = host(torus_gpu.intersect(rays, precision=prec))
+    f = host(torus_gpu.intersect(rays, precision=rt.FP32))
+    hm_p = float(((p["patch"] >= 0) != (ref["patch"] >= 0)).mean())
+    hm_f = float(((f["patch"] >= 0) != (ref["patch"] >= 0)).mean())
+    assert hm_p <= (4e-3 if level == "polish64" else 1e-3) and hm_p < hm_f, (hm_p, hm_f)
+    o = oracle_mod.OracleScene(torus).intersect(host_rays, method=oracle_mod.CLIP_GRAZE64,
+                                                precision=oracle_mod.FP32_POLISH64, graze_sin=gs)
+    assert float(((p["patch"] >= 0) != (o["patch"] >= 0)).mean()) <= 2e-3
+    # clip-iteration limits may end a few of the 2^-20 searches (error bit 2), never the stack
+    assert torus_gpu.counters()["device_errors"] & 1 == 0
+
+
+@pytest.mark.parametrize("prec_name", ["FP32_POLISH64", "FP32_GRAZE64"])
+def test_precision_form_on_camera_rays(rt, torus_gpu, oracle_mod, torch, prec_name):
+    """Camera rays: the precision levels keep every hit of the FP64 search and
+    t within 1e-5 of it."""
+    rays = torch.from_numpy(oracle_mod.camera_rays(S.camera_c2(), 160, 90)).cuda()
+    ref = host(torus_gpu.intersect(rays, precision=rt.FP64))
+    p = host(torus_gpu.intersect(rays, precision=getattr(rt, prec_name)))
+    assert np.array_equal(p["patch"] >= 0, ref["patch"] >= 0)
+    rel, same = rel_err(p, ref)
+    assert rel.max(initial=0.0) <= 1e-5

@@ -192,3 +192,62 @@ def test_scene_generators_deterministic():
     for p in range(nu * nu):
         q = (p // nu) * nu + (p % nu + 1) % nu  # next patch along u
         np.testing.assert_array_equal(nets[p].reshape(4, 4, 4)[:, 3], nets[q].reshape(4, 4, 4)[:, 0])
+
+
+def test_generator_hash_size_lists(oracle_mod):
+    """The grid sizes the scene generators avoid are exactly those whose BVH
+    key sets the reference's hash cannot place in 16 trials (checked on the
+    sizes up to 100 and on every listed size up to 140)."""
+    from cgspline_gb300 import scenes as S
+    for name, bad, patches, lo in (("torus", S.TORUS_NV_NO_HASH, lambda n: 2 * n * n, 3),
+                                   ("sphere", S.SPHERE_N_NO_HASH, lambda n: 6 * n * n, 1)):
+        sizes = set(range(lo, 101)) | {b for b in bad if b <= 140}
+        for n in sorted(sizes):
+            ok = oracle_mod.hash_build(S.bvh_keys(patches(n)))["status"] == 0
+            assert ok == (n not in bad), (name, n)
+
+
+def test_bvh_keys_match_oracle_topology(oracle_mod):
+    from cgspline_gb300 import scenes as S
+    sc = S.scene_c2(nu=8, nv=6)
+    o = oracle_mod.OracleScene(sc)
+    assert np.array_equal(o.bvh(0)["keys"], S.bvh_keys(48))
+
+
+def test_grazing_variant_restatement(oracle_mod):
+    """The oracle's precision-form clip (FP64 projection and fat-line bounds
+    for near-grazing candidates, tolerance 2^-20) against its FP64 search on
+    seeded grazing rays, and unchanged hits on camera rays."""
+    from cgspline_gb300 import scenes as S
+    sc = S.scene_c2(nu=16, nv=16)
+    o = oracle_mod.OracleScene(sc)
+    rays = S.grazing_rays(sc.surfaces[0], 4096, seed=21)
+    ref = o.intersect(rays, precision=oracle_mod.FP64)
+    g = o.intersect(rays, method=oracle_mod.CLIP_GRAZE64, precision=oracle_mod.FP32_POLISH64,
+                    graze_sin=oracle_mod.GRAZE_30)
+    f = o.intersect(rays, method=oracle_mod.CLIP_DEVICE, precision=oracle_mod.FP32_POLISH64)
+    hm_g = ((g["patch"] >= 0) != (ref["patch"] >= 0)).mean()
+    hm_f = ((f["patch"] >= 0) != (ref["patch"] >= 0)).mean()
+    assert hm_g <= 2e-3 and hm_g < hm_f
+    cam = oracle_mod.camera_rays(S.camera_c2(), 64, 36)
+    a = o.intersect(cam, method=oracle_mod.CLIP_GRAZE64, precision=oracle_mod.FP32_POLISH64)
+    b = o.intersect(cam, precision=oracle_mod.FP64)
+    assert np.array_equal(a["patch"] >= 0, b["patch"] >= 0)
+
+
+def test_longest_axis_split_same_hits(oracle_mod):
+    """The longest-axis build changes only the tree: same hits, far fewer
+    node visits than the reference's always-y split."""
+    from cgspline_gb300 import scenes as S
+    sc = S.scene_c2(nu=32, nv=32)
+    a, b = oracle_mod.OracleScene(sc), oracle_mod.OracleScene(sc, split=1)
+    rays = oracle_mod.camera_rays(S.camera_c2(), 96, 54)
+    ra, rb = a.intersect(rays), b.intersect(rays)
+    assert np.array_equal(ra["patch"] >= 0, rb["patch"] >= 0)
+    hit = ra["patch"] >= 0
+    assert np.abs(ra["t"][hit] - rb["t"][hit]).max() <= 1e-6 * ra["t"][hit].max()
+    na = a.intersect_stats(rays)["nodes"].mean()
+    nb = b.intersect_stats(rays)["nodes"].mean()
+    assert nb < 0.3 * na
+    assert not np.array_equal(a.bvh(0)["keys"], b.bvh(0)["keys"]) or a.bvh(0)["nodes"].shape != b.bvh(0)["nodes"].shape \
+        or not np.array_equal(a.bvh(0)["nodes"], b.bvh(0)["nodes"])
