@@ -57,6 +57,11 @@ class Hits(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in ("t", "u", "v", "patch", "object")]
 
 
+class EngineConfig(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("passes", "collect_threads", "resolve_threads", "collect_occupancy",
+                                       "resolve_occupancy")]
+
+
 class ServerOptions(C.Structure):
     _fields_ = [("slots", C.c_uint32), ("memory_budget", C.c_uint64), ("max_batch_samples", C.c_uint32),
                 ("max_batch_requests", C.c_uint32), ("render", RenderOptions)]
@@ -114,6 +119,10 @@ SIGNATURES = [
     ("cgs_render_batch", C.c_int, [P, C.POINTER(RenderRequest), U32, C.POINTER(RenderOptions), P]),
     ("cgs_render_running", C.c_int, [P]),
     ("cgs_camera_rays", C.c_int, [C.POINTER(Camera), U32, U32, C.c_int, P, P]),
+    ("cgs_engine_config_get", C.c_int, [C.POINTER(EngineConfig)]),
+    ("cgs_engine_config_set", C.c_int, [C.POINTER(EngineConfig)]),
+    ("cgs_autotune_render", C.c_int, [P, C.POINTER(RenderRequest), U32, C.POINTER(RenderOptions), C.c_int,
+                                      C.POINTER(EngineConfig), C.POINTER(C.c_double), P]),
     ("cgs_scene_counters", C.c_int, [P, C.POINTER(Counters)]),
     ("cgs_perfect_hash_build", C.c_int, [P, U32, P, U32, P, U32, P, P]),
     ("cgs_server_create", C.c_int, [C.POINTER(P), P, C.POINTER(ServerOptions)]),

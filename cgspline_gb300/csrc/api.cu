@@ -207,7 +207,8 @@ cudaError_t launch_wavefront_cached(const DevScene& S, RenderSlot& slot, const R
     const WavefrontBuffers& w = slot.wb;
     uint32_t eps;
     std::memcpy(&eps, &b.eps, 4);
-    const uint64_t key = key_of({scene_key(S), query_key(b.q), uint64_t(b.maxDepth), eps, key_of(slot.batch.p),
+    const uint64_t key = key_of({scene_key(S), query_key(b.q), uint64_t(b.maxDepth), eps, engine_config_generation(),
+                                 key_of(slot.batch.p),
                                  key_of(slot.counters.p), key_of(w.ray[0]), key_of(w.ray[1]), key_of(w.engine),
                                  key_of(w.shadow), key_of(w.accum), key_of(w.hit.t), key_of(w.occluded),
                                  key_of(w.contrib), key_of(w.visible), key_of(w.base), key_of(w.count),
@@ -456,6 +457,86 @@ int cgs_camera_rays(const cgs_camera* cam, uint32_t w, uint32_t h, int flip_y, f
     CameraSetup c;
     camera_setup(*cam, w, h, flip_y, c);
     return cuda_status(launch_camera_rays(c, w, h, rays, (cudaStream_t)stream));
+}
+
+int cgs_engine_config_get(cgs_engine_config* out)
+{
+    if (!out) return CGS_ERR_INVALID_ARGUMENT;
+    const EngineConfig c = engine_config();
+    *out = cgs_engine_config {c.passes, c.collectThreads, c.resolveThreads, c.collectOccupancy, c.resolveOccupancy};
+    return CGS_OK;
+}
+
+int cgs_engine_config_set(const cgs_engine_config* in)
+{
+    if (!in) return CGS_ERR_INVALID_ARGUMENT;
+    const EngineConfig c {in->passes, in->collect_threads, in->resolve_threads, in->collect_occupancy,
+                          in->resolve_occupancy};
+    return set_engine_config(c) ? CGS_OK : CGS_ERR_INVALID_ARGUMENT;
+}
+
+// The autotuner: renders the batch (wavefront schedule) under every
+// candidate engine setting, times `repeats` replays of each on the device,
+// and keeps the fastest (median) as the process-wide setting.
+int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n, const cgs_render_options* opt,
+                        int repeats, cgs_engine_config* best, double* best_ms, void* stream)
+{
+    if (!s || !opt || repeats < 1 || repeats > 64) return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    std::vector<DevRequest> host;
+    RenderBatch b;
+    int r = prepare_batch(s, reqs, n, opt, host, b);
+    if (r) return r;
+    if (!s->hashed) return CGS_ERR_NOT_BUILT;
+    CGS_TRY(cudaSetDevice(s->device));
+    if (cudaEventQuery(s->finished) == cudaErrorNotReady) return CGS_ERR_BUSY;
+    cudaStream_t st = (cudaStream_t)stream;
+    const EngineConfig saved = engine_config();
+    EngineConfig winner = saved;
+    double winnerMs = 1e300;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CGS_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return CGS_ERR_CUDA; }
+    int status = CGS_OK;
+    for (int passes : {1, 2, 4})
+        for (int ct : {128, 256})
+            for (int rt : {64, 128})
+            {
+                const EngineConfig c {passes, ct, rt, 0, 0};
+                set_engine_config(c);
+                std::vector<float> ms;
+                for (int k = 0; k < repeats + 2 && status == CGS_OK; k++)
+                {
+                    RenderBatch bk = b;
+                    if (k >= 2 && cudaEventRecord(e0, st) != cudaSuccess) status = CGS_ERR_CUDA;
+                    if (status == CGS_OK) status = run_batch(s, s->slot, host, bk, CGS_SCHED_WAVEFRONT, st, &s->launches);
+                    if (status == CGS_OK && k >= 2)
+                    {
+                        float t = 0.0f;
+                        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                            cudaEventElapsedTime(&t, e0, e1) != cudaSuccess)
+                            status = CGS_ERR_CUDA;
+                        ms.push_back(t);
+                    }
+                    else if (status == CGS_OK && cudaStreamSynchronize(st) != cudaSuccess)
+                        status = CGS_ERR_CUDA;
+                }
+                if (status != CGS_OK) break;
+                std::sort(ms.begin(), ms.end());
+                const double med = ms[ms.size() / 2];
+                if (med < winnerMs) { winnerMs = med; winner = c; }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    set_engine_config(status == CGS_OK ? winner : saved);
+    if (status != CGS_OK) return status;
+    if (best)
+        *best = cgs_engine_config {winner.passes, winner.collectThreads, winner.resolveThreads,
+                                   winner.collectOccupancy, winner.resolveOccupancy};
+    if (best_ms) *best_ms = winnerMs;
+    s->lastStream = st;
+    s->lastCounters = s->slot.counters.p;
+    return CGS_OK;
 }
 
 int cgs_render_running(cgs_scene* s)

@@ -701,7 +701,8 @@ __device__ __forceinline__ void dbasis_d(double t, double* w)
 // Jacobian [dS/du dS/dv -d] and its solve stay in FP32, and (u,v,t)
 // accumulate in FP64.  An FP32 Jacobian is accurate to ~1e-7 relative, so each
 // step cuts the error by about that factor times the Jacobian's condition
-// number; the iteration stops once the update is below 1e-13 of t.  Hits
+// number; the iteration stops once the update is below 1e-9 of t (the
+// remaining error is then far below FP32 resolution).  Hits
 // where kPolishSteps such steps do not converge (ill-conditioned, e.g.
 // grazing) continue with up to kPolishSteps64 full-FP64 Newton steps (FP64
 // Jacobian, as the oracle's polish).  The result is kept if it is finite and
@@ -782,7 +783,9 @@ static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P
         const double dT = double(dot(Su, cross(Sv, mF)) * idet);
         U += dU; V += dV; T += dT;
         if (!isfinite(U + V + T)) { U = u; V = v; T = t; break; }
-        if (fabs(dT) <= 1e-13 * fabs(T) && fabs(dU) + fabs(dV) <= 1e-13) { converged = true; break; }
+        // the last step bounds the error of the previous iterate and contracts
+        // by ~1e-7 x the Jacobian's condition: below 1e-9 the result is FP32-exact
+        if (fabs(dT) <= 1e-9 * fabs(T) && fabs(dU) + fabs(dV) <= 1e-9) { converged = true; break; }
     }
     if (!converged)
     {

@@ -29,9 +29,12 @@
 // Both kernels refill lanes one ray (k_collect) or one clip iteration
 // (k_resolve) at a time, so heavy-tailed per-ray work does not idle the other
 // lanes of a warp, and take rays in id order so a warp's rays stay coherent.
-// Rays still unfinished after kPasses passes are completed by k_rest, the
-// inline version of the same search.
+// Rays still unfinished after the configured number of passes are completed
+// by k_rest, the inline version of the same search.  Block sizes, grid
+// occupancy and the pass count are runtime settings (EngineConfig), chosen by
+// the autotuner (cgs_autotune) or set by the caller.
 #include <algorithm>
+#include <mutex>
 
 #include "kernels.h"
 
@@ -39,10 +42,10 @@ namespace cgs {
 
 namespace {
 
-constexpr int kCollectThreads = 256;
-constexpr int kResolveThreads = 128;
-constexpr uint32_t kChunk = 16;   // list entries per ray and pass
-constexpr int kPasses = 4;
+constexpr int kCollectThreads = 256;   // launch bound; runtime block size 128 or 256
+constexpr int kResolveThreads = 128;   // launch bound; runtime block size 64 or 128
+constexpr uint32_t kChunk = 64;        // list entries per ray and pass
+constexpr int kMaxPasses = 8;
 
 // list entry word 0: a patch index, or one of these markers (word 1 = object)
 constexpr uint32_t kLeave = 0xFFFFFFFFu, kEnter = 0xFFFFFFFEu, kCont = 0xFFFFFFFDu;
@@ -74,7 +77,7 @@ Eng carve(uint32_t* base, uint32_t cap)
     e.leafEntry = reinterpret_cast<float*>(take(cap)); e.limit = reinterpret_cast<float*>(take(cap));
     e.lt = reinterpret_cast<float*>(take(cap)); e.lu = reinterpret_cast<float*>(take(cap));
     e.lv = reinterpret_cast<float*>(take(cap));
-    e.ctl = take(4 * (kPasses + 1));
+    e.ctl = take(4 * (kMaxPasses + 1));
     return e;
 }
 
@@ -491,20 +494,33 @@ int resident(const void* fn, int threads)
     return sms() * (per > 0 ? per : 1);
 }
 
+// Resident blocks per SM of kernel fn at `threads` per block (cached: the
+// values depend only on the kernel and the block size).
+template<bool kAny> int per_sm(bool collect, int threads)
+{
+    static const int v[2][2] = {
+        {resident((const void*)k_collect<kAny>, 128) / sms(), resident((const void*)k_collect<kAny>, 256) / sms()},
+        {resident((const void*)k_resolve<kAny>, 64) / sms(), resident((const void*)k_resolve<kAny>, 128) / sms()}};
+    return collect ? v[0][threads == 256] : v[1][threads == 128];
+}
+
 template<bool kAny>
 void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, HitsSoA hits,
             int32_t* occluded, Eng E, Counters* cnt, cudaStream_t stream, int& nl)
 {
-    // thread-safe one-time initialisation (several host threads may launch)
-    static const int gCol = resident((const void*)k_collect<kAny>, kCollectThreads);
-    static const int gRes = resident((const void*)k_resolve<kAny>, kResolveThreads);
+    const EngineConfig c = engine_config();
+    const int ct = c.collectThreads, rt = c.resolveThreads;
+    const int cb = sms() * std::max(1, c.collectOccupancy ? std::min(c.collectOccupancy, per_sm<kAny>(true, ct))
+                                                          : per_sm<kAny>(true, ct));
+    const int rb = sms() * std::max(1, c.resolveOccupancy ? std::min(c.resolveOccupancy, per_sm<kAny>(false, rt))
+                                                          : per_sm<kAny>(false, rt));
     const uint32_t warps = (n + 31) / 32;
-    const int gc = int(std::min<uint32_t>(uint32_t(gCol), warps / (kCollectThreads / 32) + 1));
-    const int gr = int(std::min<uint32_t>(uint32_t(gRes), warps / (kResolveThreads / 32) + 1));
-    for (int p = 0; p < kPasses; p++)
+    const int gc = int(std::min<uint32_t>(uint32_t(cb), warps / (ct / 32) + 1));
+    const int gr = int(std::min<uint32_t>(uint32_t(rb), warps / (rt / 32) + 1));
+    for (int p = 0; p < c.passes; p++)
     {
-        k_collect<kAny><<<gc, kCollectThreads, 0, stream>>>(S, rays, n, nDev, E, p, cnt);
-        k_resolve<kAny><<<gr, kResolveThreads, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
+        k_collect<kAny><<<gc, ct, 0, stream>>>(S, rays, n, nDev, E, p, cnt);
+        k_resolve<kAny><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
         nl += 2;
     }
     k_rest<kAny><<<sms() * 4, 128, 0, stream>>>(S, rays, n, nDev, E, q, hits, occluded, cnt);
@@ -513,9 +529,43 @@ void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Q
 
 }  // namespace
 
+namespace {
+std::mutex gConfigMu;
+EngineConfig gConfig;
+uint64_t gConfigGen = 1;
+}  // namespace
+
+EngineConfig engine_config()
+{
+    std::lock_guard<std::mutex> g(gConfigMu);
+    return gConfig;
+}
+
+uint64_t engine_config_generation()
+{
+    std::lock_guard<std::mutex> g(gConfigMu);
+    return gConfigGen;
+}
+
+bool valid_engine_config(const EngineConfig& c)
+{
+    return c.passes >= 1 && c.passes <= kMaxPasses && (c.collectThreads == 128 || c.collectThreads == 256) &&
+           (c.resolveThreads == 64 || c.resolveThreads == 128) && c.collectOccupancy >= 0 && c.collectOccupancy <= 32 &&
+           c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32;
+}
+
+bool set_engine_config(const EngineConfig& c)
+{
+    if (!valid_engine_config(c)) return false;
+    std::lock_guard<std::mutex> g(gConfigMu);
+    gConfig = c;
+    gConfigGen++;
+    return true;
+}
+
 size_t engine_words(uint32_t capacity, int)
 {
-    return size_t(capacity) * kWordsPerRay + 4 * (kPasses + 1) + 64;
+    return size_t(capacity) * kWordsPerRay + 4 * (kMaxPasses + 1) + 64;
 }
 
 cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, bool any,
@@ -533,7 +583,7 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
         return launch_query_fp64(S, rays, n, nDev, kTolFP64, hits, cnt, stream);
     }
     Eng E = carve(scratch, capacity);
-    cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kPasses + 1), stream);
+    cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const int flat = sms() * 4;
     k_init<<<flat, 256, 0, stream>>>(rays, n, nDev, hits, any ? occluded : nullptr, E);
     int nl = 1;

@@ -15,6 +15,8 @@ namespace {
 
 constexpr int kThreads64 = 128;
 
+struct Interval64 { double x0, y0, x1, y1; };  // a pushed sub-domain (min, max)
+
 __device__ __forceinline__ double3 sub3(double3 a, double3 b) { return make_double3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ double len3d(double3 a) { return sqrt(dot_d(a, a)); }
 
@@ -141,7 +143,7 @@ __device__ __forceinline__ bool approx_d(Sink64& sink, const double2* p, double2
 __device__ __noinline__ bool clip64(Sink64& sink, double tol, LocalCounters& lc)
 {
     double2 buf[16];
-    double4 st[kClipStack];
+    Interval64 st[kClipStack];
     project_d(buf, sink.P, sink.o, sink.d);
     double2 emin = make_double2(0.0, 0.0), emax = make_double2(1.0, 1.0);
     int cutsideStack = 0, sl = 0;
@@ -160,11 +162,11 @@ __device__ __noinline__ bool clip64(Sink64& sink, double tol, LocalCounters& lc)
             const double delta = upper - lower;
             if (delta > 0.8)
             {
-                double4 pushed;
+                Interval64 pushed;
                 if (cutside == 0)
                 {
                     const double hx = 0.5 * (emin.x + emax.x);
-                    pushed = make_double4(emin.x, emin.y, hx, emax.y);
+                    pushed = Interval64 {emin.x, emin.y, hx, emax.y};
                     emin.x = hx;
                     cutsideStack = (cutsideStack << 1) | 3;
                     subU_d(buf, 0.5, 1.0);
@@ -172,7 +174,7 @@ __device__ __noinline__ bool clip64(Sink64& sink, double tol, LocalCounters& lc)
                 else
                 {
                     const double hy = 0.5 * (emin.y + emax.y);
-                    pushed = make_double4(emin.x, emin.y, emax.x, hy);
+                    pushed = Interval64 {emin.x, emin.y, emax.x, hy};
                     emin.y = hy;
                     cutsideStack = (cutsideStack << 1) & ~3;
                     subV_d(buf, 0.5, 1.0);
@@ -203,9 +205,9 @@ __device__ __noinline__ bool clip64(Sink64& sink, double tol, LocalCounters& lc)
         }
         cutsideStack >>= 1;
         if (--sl < 0) break;
-        const double4 e = st[sl];
-        emin = make_double2(e.x, e.y);
-        emax = make_double2(e.z, e.w);
+        const Interval64 e = st[sl];
+        emin = make_double2(e.x0, e.y0);
+        emax = make_double2(e.x1, e.y1);
         project_d(buf, sink.P, sink.o, sink.d);
         subU_d(buf, emin.x, emax.x);
         subV_d(buf, emin.y, emax.y);

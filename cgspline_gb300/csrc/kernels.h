@@ -55,6 +55,23 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
                       Counters* counters, cudaStream_t stream, int* launches);
 constexpr int kEnginePasses = 12;
 
+// Runtime settings of the query engine: collect / resolve passes before the
+// inline fallback, block sizes (collect 128 or 256, resolve 64 or 128) and
+// resident blocks per SM (0 = as many as fit).  Process-wide; a change bumps
+// the generation, which keys the captured CUDA graphs.
+struct EngineConfig
+{
+    int passes = 2;
+    int collectThreads = 256;
+    int resolveThreads = 128;
+    int collectOccupancy = 0;
+    int resolveOccupancy = 0;
+};
+EngineConfig engine_config();
+bool set_engine_config(const EngineConfig& c);
+bool valid_engine_config(const EngineConfig& c);
+uint64_t engine_config_generation();
+
 // --------------------------------------------------------------- render --
 struct CameraSetup
 {

@@ -225,7 +225,8 @@ cudaError_t cgs_server::launch(Slot& s)
             // the sequence reads the batch size from qhdr: one graph per (slot capacity, kind)
             Slot* sp = &s;
             const uint32_t cap = s.qcap;
-            const uint64_t key = key_of({scene_key(S), query_key(q), uint64_t(any), key_of(s.qrays.p),
+            const uint64_t key = key_of({scene_key(S), query_key(q), uint64_t(any), engine_config_generation(),
+                                         key_of(s.qrays.p),
                                          key_of(s.qhitF.p), key_of(s.qhitI.p), key_of(s.qgroup.p), key_of(s.qtab.p),
                                          key_of(s.qhdr.p), key_of(s.rs.engine.p), s.rs.engineCapacity, cap,
                                          key_of(cnt)});

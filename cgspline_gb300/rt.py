@@ -425,6 +425,37 @@ class Server:
             pass
 
 
+def engine_config() -> dict:
+    """The query engine's runtime settings (cgs_engine_config_get)."""
+    lib = _capi.load()
+    c = _capi.EngineConfig()
+    check(lib.cgs_engine_config_get(C.byref(c)), "cgs_engine_config_get")
+    return {k: getattr(c, k) for k, _ in _capi.EngineConfig._fields_}
+
+
+def set_engine_config(**kw):
+    lib = _capi.load()
+    cur = engine_config()
+    cur.update(kw)
+    c = _capi.EngineConfig(**cur)
+    check(lib.cgs_engine_config_set(C.byref(c)), "cgs_engine_config_set")
+
+
+def autotune(scene: GpuScene, requests, options: Options | None = None, repeats: int = 3, stream=None):
+    """cgs_autotune_render: time every candidate engine setting on this batch
+    and keep the fastest.  Returns (settings dict, median ms)."""
+    lib = _capi.load()
+    arr = (_capi.RenderRequest * len(requests))()
+    for k, q in enumerate(requests):
+        arr[k] = q.c()
+    o = (options or Options()).c()
+    best = _capi.EngineConfig()
+    ms = C.c_double()
+    check(lib.cgs_autotune_render(scene.h, arr, len(requests), C.byref(o), repeats, C.byref(best), C.byref(ms),
+                                  _stream_handle(stream)), "cgs_autotune_render")
+    return {k: getattr(best, k) for k, _ in _capi.EngineConfig._fields_}, float(ms.value)
+
+
 class PerfectHashFunction:
     """rt::PerfectHashFunction on the device (deterministic build)."""
 

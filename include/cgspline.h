@@ -251,6 +251,29 @@ int cgs_render_batch(cgs_scene* scene, const cgs_render_request* requests, uint3
 int cgs_camera_rays(const cgs_camera* camera, uint32_t width, uint32_t height, int flip_y, float* rays,
                     void* stream);
 
+/* -------------------------------------------------- engine settings -- */
+/* Runtime settings of the query engine (no counterpart in the reference):
+ * collect / resolve passes before the inline fallback (1..8), block sizes
+ * (collect 128 or 256, resolve 64 or 128) and resident blocks per SM
+ * (0 = as many as fit, else at most 32).  Process-wide. */
+typedef struct cgs_engine_config {
+    int passes;
+    int collect_threads;
+    int resolve_threads;
+    int collect_occupancy;
+    int resolve_occupancy;
+} cgs_engine_config;
+int cgs_engine_config_get(cgs_engine_config* config);
+int cgs_engine_config_set(const cgs_engine_config* config);
+
+/* The autotuner: renders the batch (wavefront schedule) under each candidate
+ * setting (passes 1, 2, 4 x collect 128, 256 x resolve 64, 128 threads), times
+ * `repeats` graph replays of each with CUDA events, and keeps the fastest
+ * (median) as the process-wide setting.  Synchronises `stream`. */
+int cgs_autotune_render(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,
+                        const cgs_render_options* options, int repeats, cgs_engine_config* best,
+                        double* best_ms, void* stream);
+
 /* RayTracer::running (src/rt/RayTracer.h:45-48): 1 while a render is in flight. */
 int cgs_render_running(cgs_scene* scene);
 

@@ -194,3 +194,29 @@ def test_camera_rays_match_oracle(rt, oracle_mod, torch):
         o = oracle_mod.camera_rays(cam, w, h)
         assert np.array_equal(g[:3], o[:3]) and np.isinf(g[6]).all()
         assert np.abs(g[3:6] - o[3:6]).max() < 1e-6  # a few ulps: FMA contraction differs
+
+
+def test_engine_settings_and_autotune(rt, store, torch):
+    """Every engine setting gives the same hits (the pass count only moves rays
+    between the engine and its inline fallback); the autotuner picks one of
+    the candidates and leaves it in force."""
+    base = rt.engine_config()
+    rays = rt.camera_rays(S.camera_c2(), 96, 64)
+    grp = torch.ones(rays.shape[1], dtype=torch.int32, device="cuda")
+    ref = {k: v.cpu().numpy() for k, v in store.intersect(rays, group=grp).items()}
+    try:
+        for passes, ct, rtn in ((1, 128, 64), (4, 256, 128), (8, 128, 128)):
+            rt.set_engine_config(passes=passes, collect_threads=ct, resolve_threads=rtn)
+            got = {k: v.cpu().numpy() for k, v in store.intersect(rays, group=grp).items()}
+            assert np.array_equal(got["patch"] >= 0, ref["patch"] >= 0)
+            hit = ref["patch"] >= 0
+            assert np.abs(got["t"][hit] - ref["t"][hit]).max(initial=0) <= 1e-6 * ref["t"][hit].max(initial=1)
+        from cgspline_gb300._capi import CgsError
+        with pytest.raises(CgsError):
+            rt.set_engine_config(passes=9)
+        reqs = [rt.Request.alloc(1, S.camera_c2(), 64, 36), rt.Request.alloc(0, S.camera_c1(), 32, 32)]
+        cfg, ms = rt.autotune(store, reqs, rt.Options(recursion_depth=1), repeats=1)
+        assert cfg == rt.engine_config() and ms > 0
+        assert cfg["passes"] in (1, 2, 4) and cfg["collect_threads"] in (128, 256)
+    finally:
+        rt.set_engine_config(**base)
