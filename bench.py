@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-batching", action="store_true", help="skip the 64-scene batching comparison")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson stream) comparison")
     ap.add_argument("--no-precision", action="store_true", help="skip the grazing-ray precision comparison")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default engine settings (no autotuner)")
     return ap.parse_args()
 
 
@@ -423,6 +424,13 @@ def main():
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
 
+    # the autotuner picks the engine settings on this frame (outside the timed region)
+    tuned = None
+    if not args.no_tune:
+        req = rt.Request(0, cam, W, H, 1, DEPTH, frame.data, None)
+        if frame.stride == W:
+            cfg, tms = rt.autotune(g, [req], rt.Options(recursion_depth=DEPTH, precision=prec), repeats=3)
+            tuned = {"settings": cfg, "ms": tms}
     # a scene refuses a new render while its previous one is in flight
     # (src/rt/RayTracer.cu:110-116), so frames are issued one at a time and
     # each is timed on the device
@@ -524,7 +532,8 @@ def main():
                            "schedule": args.schedule, "bvh_split": args.split, "rays_per_frame": rays_per_frame,
                            "primary_rays": W * H, "l2": "flushed (2x L2 written) before every frame",
                            "parallelism": f"replicas x{world}"},
-                "e2e": e2e, "gpu_launches": counters["kernel_launches"] * args.steps, "clocks": clk.summary()}
+                "e2e": e2e, "gpu_launches": counters["kernel_launches"] * args.steps, "clocks": clk.summary(),
+                "engine_settings": rt.engine_config(), "autotune": tuned}
         line.update(extra)
         print(json.dumps(line), flush=True)
     if dist:

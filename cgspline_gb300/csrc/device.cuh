@@ -542,73 +542,78 @@ __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, fl
     c.found = false;
 }
 
+// Transposes the 4x4 net in registers where t holds.  A cut along v
+// (subpatchV, fat line of side 1) is a cut along u (subpatchU, side 0) of the
+// transposed net, bit for bit, so one code path serves both sides and the
+// lanes of a warp do not split on the side they cut.
+__device__ __forceinline__ void transpose_if(float2* p, bool t)
+{
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = i + 1; j < 4; j++)
+        {
+            const float2 a = p[4 * i + j], b = p[4 * j + i];
+            p[4 * i + j] = t ? b : a;
+            p[4 * j + i] = t ? a : b;
+        }
+}
+
 __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, LocalCounters& lc)
 {
     if (c.b64 && c.it >= kGrazeIterations) return false;
     if (c.it++ >= kMaxClipIterations) { lc.errors |= kErrClipIterations; return false; }
     lc.iterations++;
-    const int cutside = c.cutsideStack & 1;
+    const bool tr = (c.cutsideStack & 1) != 0;  // this step cuts along v
+    bool pop = true;
+    float a = 0.0f, b = 1.0f;                    // the cut, on the (transposed) net's u axis
     if (len2(c.buf[3] - c.buf[12]) < c.tol && len2(c.buf[15] - c.buf[0]) < c.tol)
         c.found |= approximateIntersection(sink, c.buf, c.emin, c.emax);
     else
     {
+        transpose_if(c.buf, tr);
         float lower, upper;
-        if (c.b64) clip_range64(c.buf, cutside, lower, upper);
-        else clip_range(c.buf, cutside, lower, upper);
-        float delta = upper - lower;
+        if (c.b64) clip_range64(c.buf, 0, lower, upper);
+        else clip_range(c.buf, 0, lower, upper);
+        const float delta = upper - lower;
+        const float lo = tr ? c.emin.y : c.emin.x, hi = tr ? c.emax.y : c.emax.x;
         if (delta > 0.8f)
         {
-            float4 pushed;
-            if (cutside == 0)
-            {
-                float hx = 0.5f * (c.emin.x + c.emax.x);
-                pushed = make_float4(c.emin.x, c.emin.y, hx, c.emax.y);
-                c.emin.x = hx;
-                c.cutsideStack = (c.cutsideStack << 1) | 3;
-                subpatchU(c.buf, 0.5f, 1.0f);
-            }
-            else
-            {
-                float hy = 0.5f * (c.emin.y + c.emax.y);
-                pushed = make_float4(c.emin.x, c.emin.y, c.emax.x, hy);
-                c.emin.y = hy;
-                c.cutsideStack = (c.cutsideStack << 1) & ~3;
-                subpatchV(c.buf, 0.5f, 1.0f);
-            }
+            // split in halves: keep the upper half, push the lower
+            const float h = 0.5f * (lo + hi);
+            const float4 pushed = tr ? make_float4(c.emin.x, c.emin.y, c.emax.x, h)
+                                     : make_float4(c.emin.x, c.emin.y, h, c.emax.y);
+            if (tr) c.emin.y = h; else c.emin.x = h;
+            c.cutsideStack = tr ? ((c.cutsideStack << 1) & ~3) : ((c.cutsideStack << 1) | 3);
             if (c.sl >= kClipStack) { lc.errors |= kErrClipStack; return false; }
             st[c.sl++] = pushed;
-            return true;
+            a = 0.5f; b = 1.0f;
+            pop = false;
         }
         else if (delta > 0.0f)
         {
-            if (cutside == 0)
-            {
-                float sx = c.emax.x - c.emin.x;
-                float u0 = c.emin.x + sx * lower, u1 = c.emax.x - sx * (1.0f - upper);
-                subpatchU(c.buf, lower, upper);
-                c.emin.x = u0; c.emax.x = u1;
-            }
-            else
-            {
-                float sy = c.emax.y - c.emin.y;
-                float v0 = c.emin.y + sy * lower, v1 = c.emax.y - sy * (1.0f - upper);
-                subpatchV(c.buf, lower, upper);
-                c.emin.y = v0; c.emax.y = v1;
-            }
+            const float sz = hi - lo;
+            const float n0 = lo + sz * lower, n1 = hi - sz * (1.0f - upper);
+            if (tr) { c.emin.y = n0; c.emax.y = n1; } else { c.emin.x = n0; c.emax.x = n1; }
             c.cutsideStack ^= 1;
-            return true;
+            a = lower; b = upper;
+            pop = false;
         }
     }
-    // pop
-    c.cutsideStack >>= 1;
-    if (--c.sl < 0) return false;
-    float4 e = st[c.sl];
-    c.emin = make_float2(e.x, e.y);
-    c.emax = make_float2(e.z, e.w);
-    if (c.b64) project_net64(c.buf, sink.P, sink.o, sink.d);
-    else project_net(c.buf, sink.P, sink.o, sink.d);
-    subpatchU(c.buf, c.emin.x, c.emax.x);
-    subpatchV(c.buf, c.emin.y, c.emax.y);
+    if (pop)
+    {
+        c.cutsideStack >>= 1;
+        if (--c.sl < 0) return false;
+        const float4 e = st[c.sl];
+        c.emin = make_float2(e.x, e.y);
+        c.emax = make_float2(e.z, e.w);
+        if (c.b64) project_net64(c.buf, sink.P, sink.o, sink.d);
+        else project_net(c.buf, sink.P, sink.o, sink.d);
+        a = c.emin.x; b = c.emax.x;
+    }
+    subpatchU(c.buf, a, b);  // every lane: the cut, or the u range of the popped sub-net
+    if (pop) subpatchV(c.buf, c.emin.y, c.emax.y);
+    else transpose_if(c.buf, tr);
     return true;
 }
 

@@ -341,26 +341,23 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
         if (!active) continue;
 
         bool finished = false;
-        if (clipping)
+        // A lane without a search in progress walks its list -- object
+        // markers, patches culled by their leaf entry -- until it starts the
+        // next search or its chunk ends, so that the clip steps below run with
+        // as many lanes as possible.
+        while (!clipping && !finished)
         {
-            bool found = false, more = false;
-            if (q.method == 0) { more = clip_step(c, stack, sink, lc); found = c.found; }
-            else found = subdiv_patch(sink, q.tol, lc);
-            if (!more)
+            if (k >= count)
             {
-                clipping = false;
-                if (kAny)
+                // end of this pass's chunk: keep what the next pass needs
+                if (!kAny)
                 {
-                    if (found) { occluded[rid] = 0; E.status[rid] = kFinished; finished = true; }
+                    E.limit[rid] = limit;
+                    if (obj >= 0) { E.lt[rid] = lt; E.lu[rid] = lu; E.lv[rid] = lv; E.lpatch[rid] = lpatch; }
                 }
-                else if (found)
-                {
-                    lt = sink.dist; lu = sink.uv.x; lv = sink.uv.y; lpatch = int32_t(patch);
-                }
+                finished = true;
+                break;
             }
-        }
-        else if (k < count)
-        {
             const uint2 e = list[k++];
             if (e.x == kEnter || e.x == kCont)
             {
@@ -401,15 +398,23 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                 }
             }
         }
-        else
+        if (clipping)
         {
-            // end of this pass's chunk: keep what the next pass needs
-            if (!kAny)
+            bool found = false, more = false;
+            if (q.method == 0) { more = clip_step(c, stack, sink, lc); found = c.found; }
+            else found = subdiv_patch(sink, q.tol, lc);
+            if (!more)
             {
-                E.limit[rid] = limit;
-                if (obj >= 0) { E.lt[rid] = lt; E.lu[rid] = lu; E.lv[rid] = lv; E.lpatch[rid] = lpatch; }
+                clipping = false;
+                if (kAny)
+                {
+                    if (found) { occluded[rid] = 0; E.status[rid] = kFinished; finished = true; }
+                }
+                else if (found)
+                {
+                    lt = sink.dist; lu = sink.uv.x; lv = sink.uv.y; lpatch = int32_t(patch);
+                }
             }
-            finished = true;
         }
         if (finished)
         {

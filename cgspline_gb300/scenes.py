@@ -182,6 +182,52 @@ def look_at(eye, target, up=(0.0, 0.0, 1.0)):
     return tuple(float(np.float32(v)) for v in (x, y, z, w))
 
 
+# ------------------------------------------------------------ .be files --
+def load_be(path_or_text: str) -> Surface:
+    """A Bezier surface file as Surface::load_be reads it (src/Surface.cpp:149-213):
+    the patch count, then 16 one-based point indices per patch, then the point
+    count and x, y, z per point (w = 1); any single non-numeric character
+    separates values.  Accepts a path or the file's text."""
+    import re
+    text = path_or_text
+    if "\n" not in path_or_text and len(path_or_text) < 4096:
+        with open(path_or_text) as f:
+            text = f.read()
+    tok = re.findall(r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?", text)
+    pos = 0
+
+    def take(n):
+        nonlocal pos
+        if pos + n > len(tok):
+            raise ValueError("truncated .be data")
+        out = tok[pos:pos + n]
+        pos += n
+        return out
+
+    npatch = int(take(1)[0])
+    idx = np.asarray([int(v) for v in take(16 * npatch)], dtype=np.int64) - 1
+    npts = int(take(1)[0])
+    xyz = np.asarray([float(v) for v in take(3 * npts)], dtype=np.float32).reshape(npts, 3)
+    if idx.size and (idx.min() < 0 or idx.max() >= npts):
+        raise ValueError("invalid .be data: indices out of range")
+    pts = np.concatenate([xyz, np.ones((npts, 1), np.float32)], axis=1)
+    return Surface(pts, idx.astype(np.uint32))
+
+
+def save_be(surface: Surface, path: str):
+    """Writes a Surface in the .be layout load_be reads (affine points only)."""
+    idx = surface.indices.reshape(-1, 16).astype(np.int64) + 1
+    pts = np.asarray(surface.points, np.float64)
+    with open(path, "w") as f:
+        f.write(f"{idx.shape[0]}\n")
+        for row in idx:
+            f.write(",".join(str(int(v)) for v in row) + "\n")
+        f.write(f"{pts.shape[0]}\n")
+        for p in pts:
+            f.write(f"{float(np.float32(p[0] / p[3])):.9g},{float(np.float32(p[1] / p[3])):.9g},"
+                    f"{float(np.float32(p[2] / p[3])):.9g}\n")
+
+
 # ----------------------------------------------------------------- C1 ----
 def heightfield(seed: int = 1, sigma: float = 0.25, n: int = 4) -> Surface:
     """n x n bicubic patches tiling [0,n]^2 over a shared (3n+1)^2 control grid.
