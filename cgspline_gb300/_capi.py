@@ -40,7 +40,7 @@ class Camera(C.Structure):
 
 class RenderOptions(C.Structure):
     _fields_ = [("recursion_depth", C.c_int), ("eps", C.c_float), ("flip_y", C.c_int), ("method", C.c_int),
-                ("precision", C.c_int), ("tol", C.c_float), ("schedule", C.c_int)]
+                ("precision", C.c_int), ("tol", C.c_float), ("schedule", C.c_int), ("sampling", C.c_int)]
 
 
 class Rays(C.Structure):

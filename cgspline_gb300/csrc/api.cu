@@ -207,7 +207,8 @@ cudaError_t launch_wavefront_cached(const DevScene& S, RenderSlot& slot, const R
     const WavefrontBuffers& w = slot.wb;
     uint32_t eps;
     std::memcpy(&eps, &b.eps, 4);
-    const uint64_t key = key_of({scene_key(S), query_key(b.q), uint64_t(b.maxDepth), eps, engine_config_generation(),
+    const uint64_t key = key_of({scene_key(S), query_key(b.q), uint64_t(b.maxDepth), uint64_t(b.sampling), eps,
+                                 engine_config_generation(),
                                  key_of(slot.batch.p),
                                  key_of(slot.counters.p), key_of(w.ray[0]), key_of(w.ray[1]), key_of(w.engine),
                                  key_of(w.shadow), key_of(w.accum), key_of(w.hit.t), key_of(w.occluded),
@@ -225,7 +226,8 @@ int prepare_batch(cgs_scene* sc, const cgs_render_request* reqs, uint32_t n, con
 {
     if (!reqs || n == 0 || !opt) return CGS_ERR_INVALID_ARGUMENT;
     if (!valid_query(opt->method, opt->precision) || !(opt->tol > 0.0f) ||
-        (opt->schedule != CGS_SCHED_PLAIN && opt->schedule != CGS_SCHED_WAVEFRONT))
+        (opt->schedule != CGS_SCHED_PLAIN && opt->schedule != CGS_SCHED_WAVEFRONT) ||
+        (opt->sampling != CGS_SAMPLING_MIRROR && opt->sampling != CGS_SAMPLING_MONTE_CARLO))
         return CGS_ERR_INVALID_ARGUMENT;
     host.resize(n);
     uint64_t samples = 0, pixels = 0;
@@ -252,6 +254,7 @@ int prepare_batch(cgs_scene* sc, const cgs_render_request* reqs, uint32_t n, con
     b.nreq = n; b.samples = uint32_t(samples); b.pixels = uint32_t(pixels);
     b.maxDepth = maxDepth; b.eps = opt->eps;
     b.q = Query {opt->method, opt->precision, opt->tol};
+    b.sampling = opt->sampling;
     return CGS_OK;
 }
 

@@ -88,6 +88,55 @@ __device__ __forceinline__ bool bounce(const Frame& f, float3 att, float3& R, fl
     return vmax3(a) > kMinRadiance;
 }
 
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011): a counter-based generator, so a ray's random
+// numbers are a function of (image sample, bounce) and do not depend on the
+// batch it runs in.
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++)
+    {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+// 24 random bits to a float in (0, 1)
+__device__ __forceinline__ float u01(uint32_t x) { return float(x >> 8) * 0x1p-24f + 0x1p-25f; }
+
+// Monte-Carlo bounce of the sampled path (src/rt/RayTracer.cu:473-521,
+// microfacet src/rt/PBR.h:165-176): a GGX microfacet normal from two uniform
+// numbers, the reflection about it, and the attenuation
+// mix(diffuse/pi, F * G * (M.V) / ((N.V)(M.N)), metalness).  The numbers
+// come from Philox with counter (image sample, remaining depth, 0, 0) and
+// key (42, 0), in place of the reference's curand state.
+__device__ __forceinline__ bool bounce_mc(const Frame& f, float3 att, uint32_t imageSample, uint32_t dep, float3& R,
+                                          float3& a)
+{
+    const uint4 rnd = philox(make_uint4(imageSample, dep, 0u, 0u), make_uint2(42u, 0u));
+    const float x = u01(rnd.x), y = u01(rnd.y);
+    const float alpha = f.m.roughness * f.m.roughness;
+    const float theta = atan2f(alpha * sqrtf(x), sqrtf(1.0f - x)), phi = 2.0f * kPi * y;
+    const float3 ts = versor(cross(f.N, f.V)), tp = versor(cross(f.N, ts));
+    const float st = sinf(theta), ct = cosf(theta), sp = sinf(phi), cp = cosf(phi);
+    const float3 M = versor((st * cp) * ts + (st * sp) * tp + ct * f.N);
+    const float dotMV = dot(M, f.V);
+    const float3 reflectance = schlick(f3(f.m.specular[0], f.m.specular[1], f.m.specular[2]), dotMV);
+    R = (-f.V) - (2.0f * (-dotMV)) * M;
+    const float dotMN = dot(M, f.N), dotNR = dot(f.N, R);
+    if (dotNR < 1e-14f) return false;
+    const float g = Gsmith(dotNR, f.dotNV, f.m.roughness) * dotMV / (f.dotNV * dotMN);
+    const float3 kd = f3(f.m.diffuse[0], f.m.diffuse[1], f.m.diffuse[2]) * kInvPi;
+    const float3 ks = reflectance * g;
+    const float mt = f.m.metalness;
+    a = att * (kd * (1.0f - mt) + ks * mt);
+    return vmax3(a) > kMinRadiance;
+}
+
 __device__ __forceinline__ void store_pixel(const DevRequest& r, uint32_t px, float3 c)
 {
     c = f3(__saturatef(c.x), __saturatef(c.y), __saturatef(c.z));
@@ -117,7 +166,8 @@ __device__ __forceinline__ uint32_t find_request(const DevRequest* req, uint32_t
 }
 
 // ------------------------------------------------------------- plain --
-__global__ void __launch_bounds__(64) k_render_plain(DevScene S, DevRequest r, float eps, Query q, Counters* cnt)
+__global__ void __launch_bounds__(64) k_render_plain(DevScene S, DevRequest r, float eps, Query q, int sampling,
+                                                     Counters* cnt)
 {
     const uint32_t i = blockIdx.x * 8 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
     LocalCounters lc;
@@ -153,7 +203,8 @@ __global__ void __launch_bounds__(64) k_render_plain(DevScene S, DevRequest r, f
                 color = color + (c * kPi) * att;
                 if (depth <= 0) break;
                 float3 R, a;
-                if (!bounce(f, att, R, a)) break;
+                const uint32_t imageSample = ((j + r.row0) * r.width + i) * r.spp + s;
+                if (!(sampling ? bounce_mc(f, att, imageSample, uint32_t(depth), R, a) : bounce(f, att, R, a))) break;
                 o = f.P + eps * R;
                 d = R;
                 att = a;
@@ -211,7 +262,8 @@ __global__ void k_wf_camera(const RenderBatch* __restrict__ bp, Q q, float* accu
     if (blockIdx.x == 0 && threadIdx.x == 0) { count[0] = b.samples; count[1] = 0; count[2] = 0; }
 }
 
-__global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, float eps, Q q, Q qn, const uint32_t* count,
+__global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, const RenderBatch* __restrict__ bp, float eps,
+                                                         int sampling, Q q, Q qn, const uint32_t* count,
                                                          uint32_t* nextCount, uint32_t* shadowCount, HitsSoA hits,
                                                          float* shadow, uint32_t* shadowGroup, uint32_t* shadowSlot,
                                                          uint32_t shadowCap, uint32_t lcap, float* contrib,
@@ -273,7 +325,20 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DevScene S, float eps, 
             }
         }
         float3 R = f3(0, 0, 0), a = f3(0, 0, 0);
-        const bool more = isHit && dep > 0 && bounce(f, att, R, a);
+        bool more = false;
+        if (isHit && dep > 0)
+        {
+            if (sampling)
+            {
+                // the sample's index within its image: request-local sample + rows above the chunk
+                const RenderBatch* b = bp;
+                const DevRequest& r = b->req[find_request(b->req, b->nreq, smp, false)];
+                const uint32_t imageSample = (smp - r.sampleBase) + r.row0 * r.width * r.spp;
+                more = bounce_mc(f, att, imageSample, dep, R, a);
+            }
+            else
+                more = bounce(f, att, R, a);
+        }
         const uint32_t nk = warp_push(nextCount, more);
         if (more) qn.put(nk, f.P + eps * R, R, a, smp, g, dep - 1);
     }
@@ -363,7 +428,7 @@ cudaError_t launch_render_plain(const DevScene& S, const RenderBatch& b, const D
         const DevRequest& r = hostReq[k];
         dim3 block(8, 8);
         dim3 grid((r.width + 7) / 8, (r.height + 7) / 8);
-        k_render_plain<<<grid, block, 0, stream>>>(S, r, b.eps, b.q, counters);
+        k_render_plain<<<grid, block, 0, stream>>>(S, r, b.eps, b.q, b.sampling, counters);
     }
     if (launches) *launches += int(b.nreq);
     return cudaGetLastError();
@@ -403,7 +468,7 @@ cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, con
         cudaError_t e = run_query(S, q[cur].rays(), 0, wb.count + cur, b.q, false, wb.hit, nullptr, wb.engine,
                                   wb.engineCapacity, kEnginePasses, counters, stream, &nl);
         if (e != cudaSuccess) return e;
-        k_wf_shade<<<gShade, kWfThreads, 0, stream>>>(S, b.eps, q[cur], q[cur ^ 1], wb.count + cur,
+        k_wf_shade<<<gShade, kWfThreads, 0, stream>>>(S, bDev, b.eps, b.sampling, q[cur], q[cur ^ 1], wb.count + cur,
                                                       wb.count + (cur ^ 1), wb.count + 2, wb.hit, wb.shadow,
                                                       wb.shadowGroup, wb.shadowSlot, scap, lcap, wb.contrib,
                                                       wb.visible, wb.base, wb.accum);

@@ -105,6 +105,7 @@ struct RenderBatch
     int maxDepth;
     float eps;
     Query q;
+    int sampling;            // 0: mirror bounce (reference default); 1: Monte-Carlo microfacet bounce
 };
 
 // Work buffers of the wavefront schedule (device memory, sized for `capacity` samples).

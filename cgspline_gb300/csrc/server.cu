@@ -186,6 +186,7 @@ cudaError_t cgs_server::launch(Slot& s)
             s.hostReq[k] = d;
         }
         b.nreq = n; b.samples = sb; b.pixels = pb; b.maxDepth = maxDepth; b.eps = ro.eps; b.q = q;
+        b.sampling = ro.sampling;
         if (plain)
             e = launch_render_plain(S, b, s.hostReq, cnt, s.stream, &s.launches);
         else
@@ -369,7 +370,8 @@ int cgs_server_create(cgs_server** out, cgs_scene* scene, const cgs_server_optio
     *out = nullptr;
     const cgs_render_options& ro = o->render;
     if (o->slots == 0 || o->slots > kMaxSlots || !valid_query(ro.method, ro.precision) || !(ro.tol > 0.0f) ||
-        (ro.schedule != CGS_SCHED_PLAIN && ro.schedule != CGS_SCHED_WAVEFRONT) || ro.recursion_depth < 0 ||
+        (ro.schedule != CGS_SCHED_PLAIN && ro.schedule != CGS_SCHED_WAVEFRONT) ||
+        (ro.sampling != CGS_SAMPLING_MIRROR && ro.sampling != CGS_SAMPLING_MONTE_CARLO) || ro.recursion_depth < 0 ||
         ro.recursion_depth > 64)
         return CGS_ERR_INVALID_ARGUMENT;
     auto* sv = new (std::nothrow) cgs_server();

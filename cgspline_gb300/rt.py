@@ -26,6 +26,7 @@ CLIP, SUBDIV = 0, 1
 FP32, FP32_POLISH64, FP64, FP32_GRAZE64 = 0, 1, 2, 3
 PLAIN, WAVEFRONT = 0, 1
 SPLIT_REFERENCE, SPLIT_LONGEST = 0, 1
+MIRROR, MONTE_CARLO = 0, 1
 DEFAULT_TOL = 2.0 ** -12
 
 
@@ -245,10 +246,11 @@ class Options:
     precision: int = FP32
     tol: float = DEFAULT_TOL
     schedule: int = WAVEFRONT
+    sampling: int = MIRROR
 
     def c(self) -> _capi.RenderOptions:
         return _capi.RenderOptions(self.recursion_depth, self.eps, int(self.flip_y), self.method, self.precision,
-                                   self.tol, self.schedule)
+                                   self.tol, self.schedule, self.sampling)
 
 
 class Frame:

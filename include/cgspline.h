@@ -59,6 +59,14 @@ enum cgs_bvh_split { CGS_SPLIT_REFERENCE = 0, CGS_SPLIT_LONGEST = 1 };
  * launch shape, src/rt/RayTracer.cu:171-178).  WAVEFRONT: persistent,
  * stage-separated kernels over compacted ray queues. */
 enum cgs_schedule { CGS_SCHED_PLAIN = 0, CGS_SCHED_WAVEFRONT = 1 };
+/* MIRROR: the reference's default shading, one mirror bounce per level
+ * weighted by the specular reflectance (src/rt/RayTracer.cu:523-542).
+ * MONTE_CARLO: its sampled path (USE_MONTECARLO_SAMPLING,
+ * src/rt/RayTracer.cu:473-521): a GGX microfacet normal per bounce; the
+ * random numbers come from Philox4x32-10 keyed by (image sample, depth)
+ * instead of the reference's curand states, so they do not depend on the
+ * batch a request runs in. */
+enum cgs_sampling { CGS_SAMPLING_MIRROR = 0, CGS_SAMPLING_MONTE_CARLO = 1 };
 
 /* src/rt/Scene.h:79-95 */
 typedef struct cgs_material {
@@ -95,6 +103,7 @@ typedef struct cgs_render_options {
     int precision;       /* enum cgs_precision */
     float tol;           /* search tolerance on the projected net (reference 2^-12) */
     int schedule;        /* enum cgs_schedule */
+    int sampling;        /* enum cgs_sampling */
 } cgs_render_options;
 
 /* Rays as structure of arrays; direction must be unit length. */

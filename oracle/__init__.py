@@ -60,6 +60,7 @@ def lib():
         L.ora_scene_build.argtypes = [P]
         L.ora_scene_set_split.argtypes = [P, C.c_int]
         L.ora_set_graze_sin.argtypes = [C.c_float]
+        L.ora_philox.argtypes = [u32, C.c_uint32, C.c_uint32]
         L.ora_bvh_sizes.argtypes = [P, C.c_int, u32]
         L.ora_bvh_export.argtypes = [P, C.c_int, u32, u32, u32, u32, u32, u32]
         L.ora_hash_build.argtypes = [u32, C.c_uint32, u32, u32, C.c_uint32, u32, C.c_uint32]
@@ -70,7 +71,7 @@ def lib():
         L.ora_render_rows.argtypes = [P, fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_float,
                                       C.c_int, C.c_float, P, P, P, C.c_int, P]
         L.ora_render_spp.argtypes = [P, fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_int,
-                                     C.c_float, P, P, C.c_int]
+                                     C.c_float, C.c_int, P, P, C.c_int]
         L.ora_intersect_stats.argtypes = [P, fp, C.c_uint64, C.c_int, C.c_float, C.c_int, u32, C.c_int]
         L.ora_camera_rays.argtypes = [fp, C.c_uint32, C.c_uint32, fp]
         L.ora_patch_intersect.argtypes = [fp, u32, fp, C.c_float, C.c_int, P, P, P]
@@ -187,13 +188,16 @@ class OracleScene:
                     shadow=int(counts[2]), seconds=float(secs[0]))
 
 
-    def render_spp(self, camera, w, h, spp, depth=1, eps=1e-4, method=CLIP_HOST, tol=2.0 ** -12, nthreads=None):
-        """spp jittered samples per pixel, averaged (linear rgb and packed sRGB)."""
+    def render_spp(self, camera, w, h, spp, depth=1, eps=1e-4, method=CLIP_HOST, tol=2.0 ** -12, nthreads=None,
+                   mc=False):
+        """spp jittered samples per pixel, averaged (linear rgb and packed sRGB);
+        mc: the Monte-Carlo bounce (Philox keyed by image sample and depth)."""
         L = lib()
         rgb = np.zeros((h, w, 3), np.float32)
         packed = np.zeros((h, w), np.uint32)
         nt = nthreads or os.cpu_count() or 1
-        r = L.ora_render_spp(self.h, camera.packed(), w, h, spp, depth, eps, method, tol, _ptr(rgb), _ptr(packed), nt)
+        r = L.ora_render_spp(self.h, camera.packed(), w, h, spp, depth, eps, method, tol, int(mc), _ptr(rgb),
+                             _ptr(packed), nt)
         if r:
             raise RuntimeError(f"ora_render_spp failed ({r})")
         return dict(rgb=rgb, packed=packed)
@@ -212,6 +216,13 @@ class OracleScene:
             raise RuntimeError(f"ora_render_rows failed ({r})")
         return dict(rgb=rgb, primary=int(counts[0]), bounce=int(counts[1]), shadow=int(counts[2]),
                     seconds=float(secs[0]), threads=nt)
+
+
+def philox(counter, key):
+    """Philox4x32-10 of (counter[4], key[2]) -> 4 x uint32."""
+    c = np.ascontiguousarray(counter, np.uint32).copy()
+    lib().ora_philox(c, int(key[0]), int(key[1]))
+    return c
 
 
 def camera_rays(camera, w, h):

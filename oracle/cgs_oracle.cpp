@@ -1292,7 +1292,23 @@ inline V3<float> BRDF_specular(float dotHL, float dotHN, float dotNV, float dotN
 
 struct Camera { float rot[4]; float pos[3]; float scale[3]; float fovy; };
 
-struct RenderOpts { int depth = 1; float eps = 1e-4f; int method = kClipHost; float tol = 0x1p-12f; };
+struct RenderOpts { int depth = 1; float eps = 1e-4f; int method = kClipHost; float tol = 0x1p-12f; int mc = 0; };
+
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC 2011), the product's
+// counter-based generator for the Monte-Carlo path.
+inline void philox(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; r++)
+    {
+        const uint64_t p0 = uint64_t(0xD2511F53u) * c[0], p1 = uint64_t(0xCD9E8D57u) * c[2];
+        const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0), hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+inline float u01(uint32_t x) { return float(x >> 8) * 0x1p-24f + 0x1p-25f; }
 
 // sRGB encode of a [0,1] value to 8 bits (the reference's pack_sRGB comes
 // from the un-vendored Ds library; IEC 61966-2-1 is used here).
@@ -1348,7 +1364,8 @@ struct Renderer
     }
     // CPURayTracer::trace / closestHit (non Monte-Carlo),
     // src/rt/CPURayTracer.cpp:199-219, 291-440
-    V3<float> trace(const Ray<float>& ray, V3<float> att, int depth, Counters* cn, uint64_t* nrays) const
+    V3<float> trace(const Ray<float>& ray, V3<float> att, int depth, Counters* cn, uint64_t* nrays,
+                    uint32_t imageSample = 0) const
     {
         if (nrays) nrays[depth == op.depth ? 0 : 1]++;
         Hit hit; hit.t = ray.max;
@@ -1383,6 +1400,32 @@ struct Renderer
         }
         color = color * (kPi * att);
         if (depth <= 0) return color;
+        if (op.mc)
+        {
+            // the sampled path, src/rt/RayTracer.cu:473-521; microfacet, src/rt/PBR.h:165-176
+            uint32_t c[4] = {imageSample, uint32_t(depth), 0u, 0u};
+            philox(c, 42u, 0u);
+            const float x = u01(c[0]), y = u01(c[1]);
+            const float alpha = m.roughness * m.roughness;
+            const float theta = std::atan2(alpha * std::sqrt(x), std::sqrt(1.0f - x)), phi = 2.0f * kPi * y;
+            const V3<float> ts = versor(cross(N, V)), tp = versor(cross(N, ts));
+            const float st = std::sin(theta), ct = std::cos(theta), sp = std::sin(phi), cp = std::cos(phi);
+            const V3<float> M = versor((st * cp) * ts + (st * sp) * tp + ct * N);
+            const float dotMV = dot(M, V);
+            const V3<float> reflectance = schlick(m.specular, dotMV);
+            const V3<float> R = (-V) - (2 * (-dotMV)) * M;
+            const float dotMN = dot(M, N), dotNR = dot(N, R);
+            if (dotNR < 1e-14f) return color;
+            const float g = Gsmith(dotNR, dotNV, m.roughness) * dotMV / (dotNV * dotMN);
+            const V3<float> kd = m.diffuse * kInvPi, ks = reflectance * g;
+            const V3<float> a = att * (kd * (1.0f - m.metalness) + ks * m.metalness);
+            if (vmax(a) > 0x1p-8f)
+            {
+                Ray<float> r {P + op.eps * R, R, INFINITY};
+                color = color + trace(r, a, depth - 1, cn, nrays, imageSample);
+            }
+            return color;
+        }
         V3<float> reflectance = schlick(m.specular, dotNV);
         V3<float> R = (-V) - (2 * (-dotNV)) * N;
         float g = Gsmith(dotNV, dotNV, m.roughness);
@@ -1495,6 +1538,8 @@ void ora_scene_set_env(void* s_, const float* bg3, const float* amb3)
 
 int ora_scene_build(void* s_) { return static_cast<Scene*>(s_)->build(); }
 void ora_scene_set_split(void* s_, int mode) { static_cast<Scene*>(s_)->splitMode = mode; }
+// Philox4x32-10 of the Monte-Carlo path, exposed for known-answer tests.
+void ora_philox(uint32_t* ctr4, uint32_t k0, uint32_t k1) { philox(ctr4, k0, k1); }
 // the grazing margin of kClipGraze (process-wide; not thread-safe against running queries)
 void ora_set_graze_sin(float s) { g_grazeSin = s; }
 
@@ -1714,12 +1759,13 @@ static float vdc(uint32_t i)
     return float(i) * 0x1p-32f;
 }
 
-// spp jittered samples per pixel, averaged: sample s of pixel (i, j) traces
+// spp jittered samples per pixel, averaged (mc: the Monte-Carlo bounce with
+// the Philox counter (image sample px*spp + s, remaining depth)): sample s of pixel (i, j) traces
 // the primary ray through (i + s/spp, j + vdc(s)) (the sampled path's jitter,
 // src/rt/RayTracer.cu:226-236); spp = 1 is the unjittered pixel of ora_render.
 // The sum runs over s in order and is scaled by 1/spp before clamping.
 int ora_render_spp(void* s_, const float* camera11, uint32_t w, uint32_t h, uint32_t spp, int depth, float eps,
-                   int method, float tol, float* out_rgb, uint32_t* out_packed, int nthreads)
+                   int method, float tol, int mc, float* out_rgb, uint32_t* out_packed, int nthreads)
 {
     if (spp == 0) return -2;
     auto* s = static_cast<Scene*>(s_);
@@ -1729,7 +1775,7 @@ int ora_render_spp(void* s_, const float* camera11, uint32_t w, uint32_t h, uint
     std::memcpy(cam.pos, camera11 + 4, 3 * sizeof(float));
     std::memcpy(cam.scale, camera11 + 7, 3 * sizeof(float));
     cam.fovy = camera11[10];
-    RenderOpts op; op.depth = depth; op.eps = eps; op.method = method; op.tol = tol;
+    RenderOpts op; op.depth = depth; op.eps = eps; op.method = method; op.tol = tol; op.mc = mc;
     Renderer R(*s, cam, w, h, op);
     parallel_for(uint64_t(w) * h, std::max(1, nthreads), [&](uint64_t px, int) {
         const uint32_t i = uint32_t(px % w), j = uint32_t(px / w);
@@ -1739,7 +1785,7 @@ int ora_render_spp(void* s_, const float* camera11, uint32_t w, uint32_t h, uint
             float x = float(i), y = float(j);
             if (spp > 1) { x = x + float(k) * (1.0f / float(spp)); y = y + vdc(k); }
             Ray<float> pr {R.camPos, R.pixelRayDirection(x, y), INFINITY};
-            V3<float> ck = R.trace(pr, V3<float>{1, 1, 1}, depth, nullptr, nullptr);
+            V3<float> ck = R.trace(pr, V3<float>{1, 1, 1}, depth, nullptr, nullptr, uint32_t(px * spp + k));
             c = {c.x + ck.x, c.y + ck.y, c.z + ck.z};
         }
         if (spp > 1)

@@ -220,3 +220,35 @@ def test_engine_settings_and_autotune(rt, store, torch):
         assert cfg["passes"] in (1, 2, 4) and cfg["collect_threads"] in (128, 256)
     finally:
         rt.set_engine_config(**base)
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_monte_carlo_matches_oracle(rt, store, oracles, torch, schedule):
+    """The sampled path (GGX microfacet bounces, Philox keyed by image sample
+    and depth) against the oracle's restatement with the same random numbers:
+    paths only part where FP32 sin/cos or a clip result round differently."""
+    q = rt.Request.alloc(1, S.camera_c2(), 96, 54, spp=2, recursion_depth=2, linear=True)
+    rt.RayTracer(rt.Options(schedule=schedule, sampling=rt.MONTE_CARLO)).render_batch([q], store)
+    torch.cuda.synchronize()
+    ro = oracles[1].render_spp(S.camera_c2(), 96, 54, 2, depth=2, mc=True)
+    err = np.abs(q.linear.cpu().numpy() - ro["rgb"])
+    assert float(np.sqrt((err ** 2).mean())) < 1e-2
+    assert (err.max(axis=-1) > 0.05).mean() < 2e-2
+
+
+def test_monte_carlo_same_alone_and_in_mix(rt, store, torch):
+    specs = [(1, S.camera_c2(), 64, 36, 3, 2), (0, S.camera_c1(), 40, 40, 2, 1), (1, S.camera_c2(), 33, 20, 1, 3)]
+    tracer = rt.RayTracer(rt.Options(sampling=rt.MONTE_CARLO))
+    mix = [rt.Request.alloc(g, c, w, h, spp=s, recursion_depth=d, linear=True) for g, c, w, h, s, d in specs]
+    tracer.render_batch(mix, store)
+    torch.cuda.synchronize()
+    for (g, c, w, h, s, d), q in zip(specs, mix):
+        one = rt.Request.alloc(g, c, w, h, spp=s, recursion_depth=d, linear=True)
+        tracer.render_batch([one], store)
+        torch.cuda.synchronize()
+        assert torch.equal(one.linear, q.linear)
+    plain = [rt.Request.alloc(g, c, w, h, spp=s, recursion_depth=d, linear=True) for g, c, w, h, s, d in specs]
+    rt.RayTracer(rt.Options(sampling=rt.MONTE_CARLO, schedule=rt.PLAIN)).render_batch(plain, store)
+    torch.cuda.synchronize()
+    for a, b in zip(plain, mix):
+        assert (a.linear - b.linear).abs().max().item() < 1e-5

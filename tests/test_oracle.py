@@ -251,3 +251,27 @@ def test_longest_axis_split_same_hits(oracle_mod):
     assert nb < 0.3 * na
     assert not np.array_equal(a.bvh(0)["keys"], b.bvh(0)["keys"]) or a.bvh(0)["nodes"].shape != b.bvh(0)["nodes"].shape \
         or not np.array_equal(a.bvh(0)["nodes"], b.bvh(0)["nodes"])
+
+
+def test_philox_known_answers(oracle_mod):
+    """Philox4x32-10 of the Monte-Carlo path against the published
+    known-answer vectors of the generator (Salmon et al., SC 2011)."""
+    cases = [([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+             ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+             ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+              [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1])]
+    for ctr, key, want in cases:
+        assert [int(x) for x in oracle_mod.philox(ctr, key)] == want
+
+
+def test_monte_carlo_render_restatement(oracle_mod):
+    """The sampled path converges to a brightness near the mirror path's on a
+    rough, mostly diffuse scene, and is a pure function of its inputs."""
+    from cgspline_gb300 import scenes as S
+    sc = S.scene_c2(nu=16, nv=16)
+    o = oracle_mod.OracleScene(sc)
+    a = o.render_spp(S.camera_c2(), 48, 27, 4, depth=2, mc=True)["rgb"]
+    b = o.render_spp(S.camera_c2(), 48, 27, 4, depth=2, mc=True)["rgb"]
+    m = o.render_spp(S.camera_c2(), 48, 27, 4, depth=2)["rgb"]
+    assert np.array_equal(a, b)
+    assert abs(float(a.mean()) - float(m.mean())) < 0.05
