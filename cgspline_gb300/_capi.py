@@ -108,6 +108,8 @@ SIGNATURES = [
     ("cgs_hash_build", C.c_int, [P, P]),
     ("cgs_scene_build", C.c_int, [P, P]),
     ("cgs_scene_footprint", C.c_int, [P, C.POINTER(C.c_uint64)]),
+    ("cgs_scene_save", C.c_int, [P, C.c_char_p]),
+    ("cgs_scene_load", C.c_int, [C.POINTER(P), C.c_char_p, C.c_int]),
     ("cgs_bvh_sizes", C.c_int, [P, C.c_int32, P]),
     ("cgs_bvh_export", C.c_int, [P, C.c_int32, P, P, P, P, P, P]),
     ("cgs_intersect", C.c_int, [P, C.POINTER(Rays), U32, C.c_int, C.c_int, C.c_float, C.c_int, C.POINTER(Hits), P]),

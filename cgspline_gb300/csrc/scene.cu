@@ -207,7 +207,10 @@ int upload_lights(cgs_scene* sc)
     return CGS_OK;
 }
 
-int upload(cgs_scene* sc)
+}  // namespace
+
+// Device copy of the store's host state (everything but the hash tables).
+int cgs::upload_store(cgs_scene* sc)
 {
     const uint32_t nb = sc->nbvh();
     std::vector<float4> hp, hn;
@@ -292,6 +295,10 @@ int upload(cgs_scene* sc)
     sc->uploaded = true;
     return CGS_OK;
 }
+
+namespace {
+
+int upload(cgs_scene* sc) { return upload_store(sc); }
 
 // BVH::buildHashTable (src/rt/BVH.cpp:24-39) for every BVH of the store.
 int hash_all(cgs_scene* sc, cudaStream_t stream)

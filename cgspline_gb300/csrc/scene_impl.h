@@ -219,6 +219,7 @@ struct cgs_scene
 namespace cgs {
 
 void camera_setup(const cgs_camera& c, uint32_t w, uint32_t h, int flip, CameraSetup& s);
+int upload_store(cgs_scene* sc);
 uint32_t table_capacity(uint32_t n);
 uint32_t displ_size(uint32_t n);
 void hash_coefficients(uint32_t n, uint32_t A[16], uint32_t B[16]);

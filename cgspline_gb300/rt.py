@@ -144,6 +144,20 @@ class GpuScene:
         except Exception:
             pass
 
+    def save(self, path: str):
+        """Writes the built store to a scene blob (cgs_scene_save)."""
+        check(self.lib.cgs_scene_save(self.h, str(path).encode()), "cgs_scene_save")
+
+    @classmethod
+    def load(cls, path: str, device: int = 0) -> "GpuScene":
+        """A store read back from a scene blob (cgs_scene_load): no BVH or hash build."""
+        obj = cls.__new__(cls)
+        obj.lib = _capi.load()
+        h = C.c_void_p()
+        check(obj.lib.cgs_scene_load(C.byref(h), str(path).encode(), device), "cgs_scene_load")
+        obj.h, obj.scenes, obj.scene, obj.device, obj._keep, obj.surface_base = h, [], None, device, [], []
+        return obj
+
     def footprint(self) -> int:
         b = C.c_uint64()
         check(self.lib.cgs_scene_footprint(self.h, C.byref(b)), "cgs_scene_footprint")

@@ -186,6 +186,16 @@ int cgs_scene_build(cgs_scene* scene, void* stream);
 /* Device bytes held by a built scene. */
 int cgs_scene_footprint(const cgs_scene* scene, uint64_t* bytes);
 
+/* Scene blobs (no counterpart in the reference): cgs_scene_save writes a built
+ * store -- surfaces, objects, groups, BVHs and their perfect-hash tables -- to
+ * a file; cgs_scene_load reads it back onto `device` without the BVH and hash
+ * builds.  The loader checks every count, index and link against the data,
+ * and every key's hash slot, before anything reaches the device:
+ * CGS_ERR_INVALID_ARGUMENT for a damaged file, CGS_ERR_NOT_FOUND for a
+ * missing one. */
+int cgs_scene_save(cgs_scene* scene, const char* path);
+int cgs_scene_load(cgs_scene** scene, const char* path, int device);
+
 /* which = surface id, or -1 - g for the object-level BVH of group g.
  * sizes = nodes, indices, table size, displacement size, keys. */
 int cgs_bvh_sizes(const cgs_scene* scene, int32_t which, uint32_t sizes[5]);

@@ -252,3 +252,48 @@ def test_monte_carlo_same_alone_and_in_mix(rt, store, torch):
     torch.cuda.synchronize()
     for a, b in zip(plain, mix):
         assert (a.linear - b.linear).abs().max().item() < 1e-5
+
+
+def test_scene_blob_round_trip(rt, pair, torch, tmp_path):
+    """A saved and reloaded store has the same BVHs and hash tables bit for bit
+    and gives the same hits and images; damaged or missing files are refused."""
+    from cgspline_gb300._capi import CgsError
+    scs = pair + [S.scene_c4(7, max_patches=2048)]
+    a = rt.GpuScene(scs, split=rt.SPLIT_LONGEST)
+    path = tmp_path / "store.cgsb"
+    a.save(path)
+    b = rt.GpuScene.load(path)
+    nsurf = sum(len(s.surfaces) for s in scs)
+    for which in list(range(nsurf)) + [-1, -2, -3]:
+        x, y = a.bvh(which), b.bvh(which)
+        for k in ("nodes", "keys", "indices", "table", "disp"):
+            assert np.array_equal(x[k], y[k]), (which, k)
+        assert (x["A"], x["B"], x["N"], x["mask"]) == (y["A"], y["B"], y["N"], y["mask"])
+    rays = rt.camera_rays(S.camera_c4(7)[0], 64, 64)
+    grp = torch.full((rays.shape[1],), 2, dtype=torch.int32, device="cuda")
+    ra, rb = a.intersect(rays, group=grp), b.intersect(rays, group=grp)
+    for k in ra:
+        assert torch.equal(ra[k], rb[k]), k
+    qa = rt.Request.alloc(1, S.camera_c2(), 48, 32, recursion_depth=1, linear=True)
+    qb = rt.Request.alloc(1, S.camera_c2(), 48, 32, recursion_depth=1, linear=True)
+    rt.RayTracer(rt.Options()).render_batch([qa], a)
+    rt.RayTracer(rt.Options()).render_batch([qb], b)
+    torch.cuda.synchronize()
+    assert torch.equal(qa.linear, qb.linear)
+    data = path.read_bytes()
+    bad = tmp_path / "bad.cgsb"
+    bad.write_bytes(data[: len(data) // 2])
+    with pytest.raises(CgsError) as e:
+        rt.GpuScene.load(bad)
+    assert e.value.status == 1
+    flipped = bytearray(data)
+    flipped[4] ^= 0x5A  # the format version
+    bad.write_bytes(bytes(flipped))
+    with pytest.raises(CgsError) as e:
+        rt.GpuScene.load(bad)
+    assert e.value.status == 1
+    with pytest.raises(CgsError) as e:
+        rt.GpuScene.load(tmp_path / "missing.cgsb")
+    assert e.value.status == 11
+    a.close()
+    b.close()
