@@ -66,7 +66,8 @@ bool bvh_sane(const HostBVH& b, uint32_t elements)
     {
         if (n.left == EMPTY)
         {
-            if (n.right >= b.indices.size()) return false;
+            // a leaf lists at least one element (the build refuses empty leaves)
+            if (n.right + 1 >= b.indices.size() || b.indices[n.right] == EMPTY) return false;
             for (size_t i = n.right; ; i++)
             {
                 if (i >= b.indices.size()) return false;

@@ -229,7 +229,6 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
             const float3 ro = top ? o : lo, ri = top ? inv : linv;
             if (left == EMPTY)
             {
-                leaf = right;
                 if (jumped)
                 {
                     // reached through the hash: its entry is the slab test of its own box
@@ -238,6 +237,41 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     leafEntry = L0;
                 }
                 jumped = false;
+                // the leaf's first element and the one after it in the same step: a
+                // one-element leaf (the build's element count per leaf) is done here
+                const uint32_t e0 = __ldg(S.indices + B.indexBase + right);
+                const uint32_t e1 = __ldg(S.indices + B.indexBase + right + 1);
+                leaf = right + 1;
+                if (e0 == EMPTY)
+                {
+                    leaf = EMPTY;
+                    ascend = true;
+                }
+                else if (obj < 0)
+                {
+                    // descend into object e0 (Context::intersect's callback)
+                    tnode = node; tkey = key; tpost = post; tleaf = leaf;
+                    obj = int32_t(e0);
+                    const DevObject& O = S.objects[e0];
+                    const float3 d = f3(rays.dx[rid], rays.dy[rid], rays.dz[rid]);
+                    float3 ld; float sinv;
+                    to_local(O, o, d, tmax, lo, ld, lmax, sinv);
+                    linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
+                    lt = lmax;
+                    B = S.bvhs[O.surface];
+                    node = 0; key = 1; post = 0; leaf = EMPTY; jumped = false;
+                    leafEntry = -INFINITY;
+                    list[ncand++] = make_uint2(kEnter, e0);
+                }
+                else
+                {
+                    list[ncand++] = make_uint2(e0, __float_as_uint(leafEntry));
+                    if (e1 == EMPTY)
+                    {
+                        leaf = EMPTY;
+                        ascend = true;
+                    }
+                }
             }
             else
             {
