@@ -253,7 +253,9 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
     cgs_render_batch wavefront (replayed from a captured CUDA graph).  Plain:
     one k_render_plain launch per request (the reference's per-frame launch
     shape), back to back; both on the reference's BVH topology, and the
-    batched path again on the longest-axis build."""
+    batched path again on the longest-axis build, with the FP32 + FP64-polish
+    form and with the full precision form (FP64 fat-line bounds for
+    near-grazing candidates added)."""
     t0 = time.perf_counter()
     scs = [scenes.scene_c4(i) for i in range(64)]
     cams = [scenes.camera_c4(i) for i in range(64)]
@@ -267,10 +269,11 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
         out["footprint_mb"] = store.footprint() / 2 ** 20
         reqs = [rt.Request.alloc(i, c, side, side, 1, DEPTH, device=dev.index or 0)
                 for i, (c, side) in enumerate(cams)]
-        legs = (("batched", rt.WAVEFRONT), ("plain", rt.PLAIN)) if split == rt.SPLIT_REFERENCE else \
-            (("batched_split_longest", rt.WAVEFRONT),)
-        for name, sched in legs:
-            tr = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=prec, schedule=sched))
+        legs = (("batched", rt.WAVEFRONT, prec), ("plain", rt.PLAIN, prec)) if split == rt.SPLIT_REFERENCE else \
+            (("batched_split_longest", rt.WAVEFRONT, prec),
+             ("batched_split_longest_graze64", rt.WAVEFRONT, rt.FP32_GRAZE64))
+        for name, sched, p in legs:
+            tr = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=p, schedule=sched))
             for _ in range(2):  # the first runs eagerly, the second captures the graph
                 tr.render_batch(reqs, store, stream)
                 torch.cuda.synchronize()
@@ -286,11 +289,17 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
             sub = torch.from_numpy(scenes.random_subset(side * side, 0.01, seed=100 + i)).to(dev)
             rays.append(r[:, sub])
             grp.append(torch.full((sub.numel(),), i, dtype=torch.int32, device=dev))
-        acc = accuracy_vs_fp64(rt, store, torch.cat(rays, 1).contiguous(), prec, torch.cat(grp))
-        out["accuracy" if split == rt.SPLIT_REFERENCE else "accuracy_split_longest"] = acc
+        rays, grp = torch.cat(rays, 1).contiguous(), torch.cat(grp)
+        if split == rt.SPLIT_REFERENCE:
+            out["accuracy"] = accuracy_vs_fp64(rt, store, rays, prec, grp)
+        else:
+            out["accuracy_split_longest"] = accuracy_vs_fp64(rt, store, rays, prec, grp)
+            out["accuracy_split_longest_graze64"] = accuracy_vs_fp64(rt, store, rays, rt.FP32_GRAZE64, grp)
         store.close()
     out["speedup_vs_plain"] = out["batched"]["value"] / out["plain"]["value"]
     out["speedup_vs_plain_split_longest"] = out["batched_split_longest"]["value"] / out["plain"]["value"]
+    out["speedup_vs_plain_split_longest_graze64"] = \
+        out["batched_split_longest_graze64"]["value"] / out["plain"]["value"]
     return out
 
 
@@ -312,7 +321,7 @@ def serving_stream(n, seed=9):
     return out
 
 
-def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=40, slots=4, budget_gb=48):
+def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=40, slots=2, budget_gb=96):
     """32 resident scenes (1K..1M patches), a Poisson stream of nreq requests
     per rate through the continuous-batching server (reference and
     longest-axis BVH builds) and through the plain server (one request per
