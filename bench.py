@@ -493,6 +493,7 @@ def main():
                                       "unit": "TFLOP/s", "frac": alg_flops / sec_per_frame / 1e12 / fp32_peak,
                                       "peak_source": f"nominal 152 SM x 256 flop/clk at {mhz:.0f} MHz"},
                              "per_ray": {"nodes": nodes / nrays, "hash_lookups": hashes / nrays,
+                                         "hash_table_reads": c["hash_table_reads"] / nrays,
                                          "candidates": cand / nrays, "clip_iterations": iters / nrays}}
         # accuracy of the primary hits on a seeded 1% pixel subset
         allr = rt.camera_rays(cam, W, H, device=local)
@@ -518,6 +519,7 @@ def main():
                        "ms_per_step": sum(ms2) / args.steps, "rays_per_frame": c2["rays"],
                        "per_ray_nodes": c2["nodes"] / c2["rays"],
                        "per_ray_hash_lookups": c2["hash_lookups"] / c2["rays"],
+                       "per_ray_hash_table_reads": c2["hash_table_reads"] / c2["rays"],
                        "subset_hit_miss_equal": bool(np.array_equal(hit, gb["patch"] >= 0)),
                        "subset_max_rel_t_diff": float(
                            (np.abs(ga["t"][hit] - gb["t"][hit]) / ga["t"][hit]).max(initial=0.0)),

@@ -59,7 +59,7 @@ class Hits(C.Structure):
 
 class EngineConfig(C.Structure):
     _fields_ = [(k, C.c_int) for k in ("passes", "collect_threads", "resolve_threads", "collect_occupancy",
-                                       "resolve_occupancy")]
+                                       "resolve_occupancy", "backtrack_cache")]
 
 
 class ServerOptions(C.Structure):
@@ -85,7 +85,7 @@ class ServerStats(C.Structure):
 class Counters(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("rays", "primary_rays", "bounce_rays", "shadow_rays", "nodes",
                                           "hash_lookups", "candidates", "iterations", "device_errors",
-                                          "kernel_launches")]
+                                          "kernel_launches", "hash_table_reads")]
 
 
 _lib = None

@@ -466,7 +466,8 @@ int cgs_engine_config_get(cgs_engine_config* out)
 {
     if (!out) return CGS_ERR_INVALID_ARGUMENT;
     const EngineConfig c = engine_config();
-    *out = cgs_engine_config {c.passes, c.collectThreads, c.resolveThreads, c.collectOccupancy, c.resolveOccupancy};
+    *out = cgs_engine_config {c.passes, c.collectThreads, c.resolveThreads, c.collectOccupancy, c.resolveOccupancy,
+                              c.backtrackCache};
     return CGS_OK;
 }
 
@@ -474,7 +475,7 @@ int cgs_engine_config_set(const cgs_engine_config* in)
 {
     if (!in) return CGS_ERR_INVALID_ARGUMENT;
     const EngineConfig c {in->passes, in->collect_threads, in->resolve_threads, in->collect_occupancy,
-                          in->resolve_occupancy};
+                          in->resolve_occupancy, in->backtrack_cache};
     return set_engine_config(c) ? CGS_OK : CGS_ERR_INVALID_ARGUMENT;
 }
 
@@ -505,7 +506,7 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
         for (int ct : {128, 256})
             for (int rt : {64, 128})
             {
-                const EngineConfig c {passes, ct, rt, 0, 0};
+                const EngineConfig c {passes, ct, rt, 0, 0, saved.backtrackCache};
                 set_engine_config(c);
                 std::vector<float> ms;
                 for (int k = 0; k < repeats + 2 && status == CGS_OK; k++)
@@ -535,7 +536,7 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
     if (status != CGS_OK) return status;
     if (best)
         *best = cgs_engine_config {winner.passes, winner.collectThreads, winner.resolveThreads,
-                                   winner.collectOccupancy, winner.resolveOccupancy};
+                                   winner.collectOccupancy, winner.resolveOccupancy, winner.backtrackCache};
     if (best_ms) *best_ms = winnerMs;
     s->lastStream = st;
     s->lastCounters = s->slot.counters.p;

@@ -96,13 +96,13 @@ __device__ __forceinline__ float3 group_ambient(const DevScene& S, uint32_t g)
 
 struct Counters
 {
-    unsigned long long nodes, hashLookups, candidates, iterations, rays, errors;
+    unsigned long long nodes, hashLookups, candidates, iterations, rays, errors, tableReads;
 };
 
 struct LocalCounters
 {
     uint32_t nodes = 0, hashLookups = 0, candidates = 0, iterations = 0;
-    uint32_t errors = 0;
+    uint32_t errors = 0, tableReads = 0;
 };
 
 // ------------------------------------------------------------ float math --
@@ -911,6 +911,7 @@ __device__ __forceinline__ bool hash_traverse(const DevScene& S, const DevBVH& b
         key = (key >> levels) ^ 1u;
         postponed ^= 1u;
         lc.hashLookups++;
+        lc.tableReads++;
         node = __ldg(table + hash_slot(S, b, key));
     }
     return kAny ? false : result;
@@ -1110,19 +1111,19 @@ __device__ __forceinline__ void flush_counters(Counters* c, const LocalCounters&
 {
     if (!c) return;
     unsigned mask = __activemask();
-    unsigned long long v[5] = {lc.nodes, lc.hashLookups, lc.candidates, lc.iterations, rays};
+    unsigned long long v[6] = {lc.nodes, lc.hashLookups, lc.candidates, lc.iterations, rays, lc.tableReads};
     uint32_t err = lc.errors;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1)
     {
 #pragma unroll
-        for (int k = 0; k < 5; k++) v[k] += __shfl_down_sync(mask, v[k], off);
+        for (int k = 0; k < 6; k++) v[k] += __shfl_down_sync(mask, v[k], off);
         err |= __shfl_down_sync(mask, err, off);
     }
     if (lane_id() == (unsigned)(__ffs(mask) - 1))
     {
         atomicAdd(&c->nodes, v[0]); atomicAdd(&c->hashLookups, v[1]); atomicAdd(&c->candidates, v[2]);
-        atomicAdd(&c->iterations, v[3]); atomicAdd(&c->rays, v[4]);
+        atomicAdd(&c->iterations, v[3]); atomicAdd(&c->rays, v[4]); atomicAdd(&c->tableReads, v[5]);
         if (err) atomicOr(&c->errors, (unsigned long long)err);
     }
 }

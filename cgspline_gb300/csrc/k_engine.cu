@@ -45,6 +45,13 @@ namespace {
 constexpr int kCollectThreads = 256;   // launch bound; runtime block size 128 or 256
 constexpr int kResolveThreads = 128;   // launch bound; runtime block size 64 or 128
 constexpr uint32_t kChunk = 64;        // list entries per ray and pass
+// One collect step appends at most two entries: a leaf's first patch and,
+// when that patch ends the leaf and nothing is postponed inside the object,
+// the marker that leaves the object.
+constexpr uint32_t kMaxAppendsPerStep = 2;
+// Backtrack cache: the node indices of the last kRing postponed siblings of
+// each lane's ray, in a ring in shared memory.
+constexpr uint32_t kRing = 8;
 constexpr int kMaxPasses = 8;
 
 // list entry word 0: a patch index, or one of these markers (word 1 = object)
@@ -81,6 +88,15 @@ Eng carve(uint32_t* base, uint32_t cap)
     return e;
 }
 
+// The BVH a lane walks: its index in the scene's BVH table and the two bases
+// every step uses.
+struct BvhRef { uint32_t idx, nodeBase, indexBase; };
+
+__device__ __forceinline__ BvhRef bvh_ref(const DevScene& S, uint32_t idx)
+{
+    return BvhRef {idx, __ldg(&S.bvhs[idx].nodeBase), __ldg(&S.bvhs[idx].indexBase)};
+}
+
 // Warp-wide refill: every lane in `need` gets the next index from *fetch.
 __device__ __forceinline__ uint32_t warp_fetch(uint32_t* fetch, bool need)
 {
@@ -102,10 +118,25 @@ __device__ __forceinline__ void load_ray(const RaysSoA& r, uint32_t i, float3& o
 }
 
 // ------------------------------------------------------------ collect --
+//
+// A backtrack goes to the sibling postponed deepest on the current path: the
+// one postponed last.  With the backtrack cache on, a step that postpones a
+// sibling also pushes its node index on the lane's ring, and a backtrack pops
+// it from there while it is still in the ring; otherwise (the ring held more
+// than kRing postponed siblings, or the ray was parked since) it looks the
+// sibling's key up in the perfect hash as BVH::hashIntersect does.  Both give
+// the same node.  `rvalid` counts the entries at the top of the ring that are
+// still intact; an object's traversal nests inside the object level's on the
+// same ring, since it leaves the object only with nothing postponed.
 template<bool kAny>
 __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, RaysSoA rays, uint32_t n0,
-                                                                const uint32_t* nDev, Eng E, int pass, Counters* cnt)
+                                                                const uint32_t* nDev, Eng E, int pass, int cache,
+                                                                Counters* cnt)
 {
+    // entry s of this lane's ring at ring[s * blockDim.x + threadIdx.x]; the
+    // ring's state packs its top slot (bits 0-2) with `rvalid` (bits 3-6)
+    __shared__ uint32_t ring[kRing * kCollectThreads];
+    uint32_t rstate = 0;
     const uint32_t n = nDev ? *nDev : n0;
     LocalCounters lc;
     bool active = false, exhausted = false, jumped = false;
@@ -116,7 +147,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
     float leafEntry = -INFINITY;
     int32_t obj = -1;
     uint32_t topIdx = 0;  // the ray's object-level BVH (its group's)
-    DevBVH B {};
+    BvhRef B {};  // the BVH walked now; its hash parameters are read at a table lookup
     uint32_t nrays = 0;
     uint2* list = nullptr;
     for (;;)
@@ -144,12 +175,13 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
                 list = E.list + size_t(rid) * kChunk;
                 ncand = 0;
+                rstate = 0;
                 topIdx = __ldg(S.groupTop + g);
                 if (pass == 0)
                 {
                     node = 0; key = 1; post = 0; leaf = EMPTY; obj = -1; jumped = false;
                     leafEntry = -INFINITY; limit = tmax;
-                    B = S.bvhs[topIdx];
+                    B = bvh_ref(S, topIdx);
                     nrays++;
                 }
                 else
@@ -157,7 +189,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     node = E.node[rid]; key = E.key[rid]; post = E.post[rid]; leaf = E.leaf[rid];
                     jumped = E.jumped[rid] != 0; leafEntry = E.leafEntry[rid]; obj = E.obj[rid];
                     limit = kAny ? tmax : E.limit[rid];
-                    B = S.bvhs[topIdx];
+                    B = bvh_ref(S, topIdx);
                     if (obj >= 0)
                     {
                         tnode = E.tnode[rid]; tkey = E.tkey[rid]; tpost = E.tpost[rid]; tleaf = E.tleaf[rid];
@@ -166,7 +198,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                         to_local(O, o, d, tmax, lo, ld, lmax, sinv);
                         linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
                         lt = kAny ? lmax : E.lt[rid];
-                        B = S.bvhs[O.surface];
+                        B = bvh_ref(S, O.surface);
                         list[ncand++] = make_uint2(kCont, uint32_t(obj));
                     }
                 }
@@ -175,9 +207,9 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         if (__ballot_sync(0xFFFFFFFFu, active || !exhausted) == 0) break;
         if (!active) continue;
 
-        if (ncand >= kChunk)
+        if (ncand + kMaxAppendsPerStep > kChunk)
         {
-            // chunk full: park before this step
+            // no room for what one step may append: park before this step
             E.node[rid] = node; E.key[rid] = key; E.post[rid] = post; E.leaf[rid] = leaf;
             E.jumped[rid] = jumped; E.leafEntry[rid] = leafEntry; E.obj[rid] = obj;
             E.tnode[rid] = tnode; E.tkey[rid] = tkey; E.tpost[rid] = tpost; E.tleaf[rid] = tleaf;
@@ -205,7 +237,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     to_local(O, o, d, tmax, lo, ld, lmax, sinv);
                     linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
                     lt = lmax;
-                    B = S.bvhs[O.surface];
+                    B = bvh_ref(S, O.surface);
                     node = 0; key = 1; post = 0; leaf = EMPTY; jumped = false;
                     leafEntry = -INFINITY;
                     list[ncand++] = make_uint2(kEnter, e);
@@ -258,7 +290,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     to_local(O, o, d, tmax, lo, ld, lmax, sinv);
                     linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
                     lt = lmax;
-                    B = S.bvhs[O.surface];
+                    B = bvh_ref(S, O.surface);
                     node = 0; key = 1; post = 0; leaf = EMPTY; jumped = false;
                     leafEntry = -INFINITY;
                     list[ncand++] = make_uint2(kEnter, e0);
@@ -285,8 +317,15 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 if (iL && iR)
                 {
                     post |= 1u;
-                    if (L0 < R0) { key = key << 1; node = left; leafEntry = L0; }
-                    else { key = (key << 1) ^ 1u; node = right; leafEntry = R0; }
+                    uint32_t other;
+                    if (L0 < R0) { key = key << 1; node = left; leafEntry = L0; other = right; }
+                    else { key = (key << 1) ^ 1u; node = right; leafEntry = R0; other = left; }
+                    if (cache)
+                    {
+                        const uint32_t top = (rstate + 1u) & (kRing - 1u);
+                        ring[top * blockDim.x + threadIdx.x] = other;
+                        rstate = top | (min((rstate >> 3) + 1u, kRing) << 3);
+                    }
                 }
                 else if (iL) { key = key << 1; node = left; leafEntry = L0; }
                 else if (iR) { key = (key << 1) ^ 1u; node = right; leafEntry = R0; }
@@ -303,7 +342,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 {
                     list[ncand++] = make_uint2(kLeave, uint32_t(obj));
                     obj = -1;
-                    B = S.bvhs[topIdx];
+                    B = bvh_ref(S, topIdx);
                     node = tnode; key = tkey; post = tpost; leaf = tleaf;
                     leafEntry = -INFINITY;
                 }
@@ -315,7 +354,18 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 key = (key >> levels) ^ 1u;
                 post ^= 1u;
                 lc.hashLookups++;
-                node = __ldg(S.tables + B.tableBase + hash_slot(S, B, key));
+                if (rstate >= kRing)
+                {
+                    const uint32_t top = rstate & (kRing - 1u);
+                    node = ring[top * blockDim.x + threadIdx.x];
+                    rstate = ((top - 1u) & (kRing - 1u)) | (rstate - kRing) >> 3 << 3;
+                }
+                else
+                {
+                    lc.tableReads++;
+                    const DevBVH H = S.bvhs[B.idx];
+                    node = __ldg(S.tables + H.tableBase + hash_slot(S, H, key));
+                }
                 jumped = true;
             }
         }
@@ -558,7 +608,7 @@ void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Q
     const int gr = int(std::min<uint32_t>(uint32_t(rb), warps / (rt / 32) + 1));
     for (int p = 0; p < c.passes; p++)
     {
-        k_collect<kAny><<<gc, ct, 0, stream>>>(S, rays, n, nDev, E, p, cnt);
+        k_collect<kAny><<<gc, ct, 0, stream>>>(S, rays, n, nDev, E, p, c.backtrackCache, cnt);
         k_resolve<kAny><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
         nl += 2;
     }
@@ -590,7 +640,7 @@ bool valid_engine_config(const EngineConfig& c)
 {
     return c.passes >= 1 && c.passes <= kMaxPasses && (c.collectThreads == 128 || c.collectThreads == 256) &&
            (c.resolveThreads == 64 || c.resolveThreads == 128) && c.collectOccupancy >= 0 && c.collectOccupancy <= 32 &&
-           c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32;
+           c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1);
 }
 
 bool set_engine_config(const EngineConfig& c)

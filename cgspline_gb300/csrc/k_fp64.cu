@@ -286,6 +286,7 @@ __device__ __forceinline__ bool traverse_d(const DevScene& S, const DevBVH& b, d
         key = (key >> levels) ^ 1u;
         postponed ^= 1u;
         lc.hashLookups++;
+        lc.tableReads++;
         node = __ldg(table + hash_slot(S, b, key));
     }
     return result;

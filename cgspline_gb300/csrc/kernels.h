@@ -66,6 +66,7 @@ struct EngineConfig
     int resolveThreads = 128;
     int collectOccupancy = 0;
     int resolveOccupancy = 0;
+    int backtrackCache = 1;  // 1: backtracks read postponed siblings from a per-lane ring first
 };
 EngineConfig engine_config();
 bool set_engine_config(const EngineConfig& c);

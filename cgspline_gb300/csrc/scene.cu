@@ -638,6 +638,7 @@ int cgs_scene_counters(cgs_scene* s, cgs_counters* out)
     CGS_TRY(cudaMemcpy(&c, s->lastCounters, sizeof c, cudaMemcpyDeviceToHost));
     out->rays = c.rays; out->nodes = c.nodes; out->hash_lookups = c.hashLookups; out->candidates = c.candidates;
     out->iterations = c.iterations; out->device_errors = c.errors; out->kernel_launches = uint64_t(s->launches);
+    out->hash_table_reads = c.tableReads;
     return CGS_OK;
 }
 

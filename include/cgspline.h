@@ -126,12 +126,15 @@ typedef struct cgs_counters {
     uint64_t rays;            /* rays traced by the last call (all kinds) */
     uint64_t primary_rays, bounce_rays, shadow_rays;
     uint64_t nodes;           /* inner BVH nodes visited */
-    uint64_t hash_lookups;    /* stackless backtracks through the perfect hash */
+    uint64_t hash_lookups;    /* stackless backtracks (each one a perfect-hash lookup in
+                                 BVH::hashIntersect) */
     uint64_t candidates;      /* (ray, patch) pairs searched */
     uint64_t iterations;      /* clip / subdivision iterations */
     uint64_t device_errors;   /* bit mask: 1 clip stack full, 2 clip iteration limit,
                                  4 traversal step limit, 8 ray of an unknown group */
     uint64_t kernel_launches;
+    uint64_t hash_table_reads; /* backtracks answered through the perfect hash; the rest
+                                  came from the traversal's backtrack cache */
 } cgs_counters;
 
 /* -------------------------------------------------------------- scene -- */
@@ -281,6 +284,12 @@ typedef struct cgs_engine_config {
     int resolve_threads;
     int collect_occupancy;
     int resolve_occupancy;
+    /* 1 (default): the traversal kernel keeps the node indices of the last 8
+     * postponed siblings of each ray in a ring in shared memory and answers a
+     * backtrack from it when the entry is still there; 0: every backtrack
+     * goes through the perfect hash, as in BVH::hashIntersect.  Both visit
+     * the same nodes in the same order and give the same hits. */
+    int backtrack_cache;
 } cgs_engine_config;
 int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
