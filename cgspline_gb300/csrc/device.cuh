@@ -105,6 +105,17 @@ struct LocalCounters
     uint32_t errors = 0, tableReads = 0;
 };
 
+// One 32-byte load through the read-only path (a 256-bit vector load, sm_100
+// and later): p must be 32-byte aligned and the data unchanged while the
+// kernel runs.  A warp's divergent lanes then touch each 32-byte sector of a
+// BVH node with one request instead of two.
+__device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b)
+{
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 // ------------------------------------------------------------ float math --
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
 __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
@@ -872,7 +883,9 @@ __device__ __forceinline__ bool hash_traverse(const DevScene& S, const DevBVH& b
     {
         if (step >= kMaxTraversalSteps) { lc.errors |= kErrTraversal; break; }
         const float4* q = nodes + 4ull * node;
-        const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+        float4 q0, q1, q2, q3;
+        ldg256(q, q0, q1);
+        ldg256(q + 2, q2, q3);
         uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
         if (left != EMPTY)
         {

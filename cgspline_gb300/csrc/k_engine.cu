@@ -255,7 +255,9 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         {
             const float4* q = S.nodes + 4ull * (B.nodeBase + node);
             // one round trip for the whole 64-byte node
-            const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+            float4 q0, q1, q2, q3;
+            ldg256(q, q0, q1);
+            ldg256(q + 2, q2, q3);
             const uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
             const bool top = obj < 0;
             const float3 ro = top ? o : lo, ri = top ? inv : linv;

@@ -247,7 +247,9 @@ __device__ __forceinline__ bool traverse_d(const DevScene& S, const DevBVH& b, d
     {
         if (step >= kMaxTraversalSteps) { lc.errors |= kErrTraversal; break; }
         const float4* q = nodes + 4ull * node;
-        const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+        float4 q0, q1, q2, q3;
+        ldg256(q, q0, q1);
+        ldg256(q + 2, q2, q3);
         const uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
         if (left != EMPTY)
         {
