@@ -838,27 +838,27 @@ __device__ __forceinline__ uint32_t hash_slot(const DevScene& S, const DevBVH& b
 // _node_intersect, src/rt/BVH.h:147-176
 __device__ __forceinline__ bool slab(float& tMin, float3 lo, float3 hi, float3 o, float3 inv)
 {
+    // `if (a > tm) tm = a` and `if (b < tM) tM = b` as one max / min each:
+    // tm and tM start at -inf / +inf and never become NaN, and fmaxf / fminf
+    // skip a NaN argument just as the comparison does.
     float tm = -INFINITY, tM = INFINITY;
     {
         float t0 = (lo.x - o.x) * inv.x, t1 = (hi.x - o.x) * inv.x;
         bool s = signbit(inv.x);
-        float a = s ? t1 : t0, b = s ? t0 : t1;
-        if (a > tm) tm = a;
-        if (b < tM) tM = b;
+        tm = fmaxf(tm, s ? t1 : t0);
+        tM = fminf(tM, s ? t0 : t1);
     }
     {
         float t0 = (lo.y - o.y) * inv.y, t1 = (hi.y - o.y) * inv.y;
         bool s = signbit(inv.y);
-        float a = s ? t1 : t0, b = s ? t0 : t1;
-        if (a > tm) tm = a;
-        if (b < tM) tM = b;
+        tm = fmaxf(tm, s ? t1 : t0);
+        tM = fminf(tM, s ? t0 : t1);
     }
     {
         float t0 = (lo.z - o.z) * inv.z, t1 = (hi.z - o.z) * inv.z;
         bool s = signbit(inv.z);
-        float a = s ? t1 : t0, b = s ? t0 : t1;
-        if (a > tm) tm = a;
-        if (b < tM) tM = b;
+        tm = fmaxf(tm, s ? t1 : t0);
+        tM = fminf(tM, s ? t0 : t1);
     }
     tMin = tm;
     return tm < tM && tM > 0.0001f;
