@@ -538,10 +538,13 @@ struct ClipState
 };
 
 // grazeSin > 0: the precision form (candidates within asin(grazeSin) of
-// grazing get the FP64 bounds)
+// grazing get the FP64 bounds).  kG64 = false compiles the FP64 path out
+// (searches that never take it: a smaller loop body for the instruction
+// cache).
+template<bool kG64 = true>
 __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, float tol, float grazeSin)
 {
-    c.b64 = grazeSin > 0.0f && near_grazing(sink.P, sink.d, grazeSin);
+    c.b64 = kG64 && grazeSin > 0.0f && near_grazing(sink.P, sink.d, grazeSin);
     c.tol = c.b64 ? kGrazeTol : tol;
     if (c.b64) project_net64(c.buf, sink.P, sink.o, sink.d);
     else project_net(c.buf, sink.P, sink.o, sink.d);
@@ -570,9 +573,11 @@ __device__ __forceinline__ void transpose_if(float2* p, bool t)
         }
 }
 
+template<bool kG64 = true>
 __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, LocalCounters& lc)
 {
-    if (c.b64 && c.it >= kGrazeIterations) return false;
+    const bool b64 = kG64 && c.b64;
+    if (b64 && c.it >= kGrazeIterations) return false;
     if (c.it++ >= kMaxClipIterations) { lc.errors |= kErrClipIterations; return false; }
     lc.iterations++;
     const bool tr = (c.cutsideStack & 1) != 0;  // this step cuts along v
@@ -584,7 +589,7 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
     {
         transpose_if(c.buf, tr);
         float lower, upper;
-        if (c.b64) clip_range64(c.buf, 0, lower, upper);
+        if (b64) clip_range64(c.buf, 0, lower, upper);
         else clip_range(c.buf, 0, lower, upper);
         const float delta = upper - lower;
         const float lo = tr ? c.emin.y : c.emin.x, hi = tr ? c.emax.y : c.emax.x;
@@ -618,7 +623,7 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
         const float4 e = st[c.sl];
         c.emin = make_float2(e.x, e.y);
         c.emax = make_float2(e.z, e.w);
-        if (c.b64) project_net64(c.buf, sink.P, sink.o, sink.d);
+        if (b64) project_net64(c.buf, sink.P, sink.o, sink.d);
         else project_net(c.buf, sink.P, sink.o, sink.d);
         a = c.emin.x; b = c.emax.x;
     }

@@ -382,7 +382,9 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
 }
 
 // ------------------------------------------------------------ resolve --
-template<bool kAny>
+// kG64: the search may take the FP64 grazing path (precision levels 3 and 5);
+// the other levels run an instance without that code.
+template<bool kAny, bool kG64>
 __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA rays, uint32_t n0,
                                                              const uint32_t* nDev, Eng E, int pass, Query q,
                                                              HitsSoA hits, int32_t* occluded, Counters* cnt)
@@ -479,7 +481,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                     sink.dist = kAny ? lmax : lt;
                     sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
                     lc.candidates++;
-                    if (q.method == 0) clip_begin(c, sink, q.tol, graze_sin(q.precision));
+                    if (q.method == 0) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision));
                     clipping = true;
                 }
             }
@@ -487,7 +489,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
         if (clipping)
         {
             bool found = false, more = false;
-            if (q.method == 0) { more = clip_step(c, stack, sink, lc); found = c.found; }
+            if (q.method == 0) { more = clip_step<kG64>(c, stack, sink, lc); found = c.found; }
             else found = subdiv_patch(sink, q.tol, lc);
             if (!more)
             {
@@ -587,31 +589,31 @@ int resident(const void* fn, int threads)
 
 // Resident blocks per SM of kernel fn at `threads` per block (cached: the
 // values depend only on the kernel and the block size).
-template<bool kAny> int per_sm(bool collect, int threads)
+template<bool kAny, bool kG64> int per_sm(bool collect, int threads)
 {
     static const int v[2][2] = {
         {resident((const void*)k_collect<kAny>, 128) / sms(), resident((const void*)k_collect<kAny>, 256) / sms()},
-        {resident((const void*)k_resolve<kAny>, 64) / sms(), resident((const void*)k_resolve<kAny>, 128) / sms()}};
+        {resident((const void*)k_resolve<kAny, kG64>, 64) / sms(),
+         resident((const void*)k_resolve<kAny, kG64>, 128) / sms()}};
     return collect ? v[0][threads == 256] : v[1][threads == 128];
 }
 
-template<bool kAny>
+template<bool kAny, bool kG64>
 void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, HitsSoA hits,
             int32_t* occluded, Eng E, Counters* cnt, cudaStream_t stream, int& nl)
 {
     const EngineConfig c = engine_config();
     const int ct = c.collectThreads, rt = c.resolveThreads;
-    const int cb = sms() * std::max(1, c.collectOccupancy ? std::min(c.collectOccupancy, per_sm<kAny>(true, ct))
-                                                          : per_sm<kAny>(true, ct));
-    const int rb = sms() * std::max(1, c.resolveOccupancy ? std::min(c.resolveOccupancy, per_sm<kAny>(false, rt))
-                                                          : per_sm<kAny>(false, rt));
+    const int pc = per_sm<kAny, kG64>(true, ct), pr = per_sm<kAny, kG64>(false, rt);
+    const int cb = sms() * std::max(1, c.collectOccupancy ? std::min(c.collectOccupancy, pc) : pc);
+    const int rb = sms() * std::max(1, c.resolveOccupancy ? std::min(c.resolveOccupancy, pr) : pr);
     const uint32_t warps = (n + 31) / 32;
     const int gc = int(std::min<uint32_t>(uint32_t(cb), warps / (ct / 32) + 1));
     const int gr = int(std::min<uint32_t>(uint32_t(rb), warps / (rt / 32) + 1));
     for (int p = 0; p < c.passes; p++)
     {
         k_collect<kAny><<<gc, ct, 0, stream>>>(S, rays, n, nDev, E, p, c.backtrackCache, cnt);
-        k_resolve<kAny><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
+        k_resolve<kAny, kG64><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
         nl += 2;
     }
     k_rest<kAny><<<sms() * 4, 128, 0, stream>>>(S, rays, n, nDev, E, q, hits, occluded, cnt);
@@ -678,8 +680,9 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     const int flat = sms() * 4;
     k_init<<<flat, 256, 0, stream>>>(rays, n, nDev, hits, any ? occluded : nullptr, E);
     int nl = 1;
-    if (any) launch<true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
-    else launch<false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    if (any) launch<true, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    else if (graze_sin(q.precision) > 0.0f) launch<false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    else launch<false, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     if (!any && polishes(q.precision))
     {
         k_polish<<<flat * 2, 128, 0, stream>>>(S, rays, n, nDev, hits);
