@@ -126,7 +126,8 @@ def measured_peaks():
 
 
 def traffic_summary():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    """DRAM bytes per launch of the dominant kernel (k_collect, first pass over
+    the frame's primary rays) from the committed ncu capture summary."""
     try:
         with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
             return json.load(f)
@@ -474,27 +475,52 @@ def main():
     if rank == 0:
         c = counters
         nrays, nodes, hashes, cand, iters = c["rays"], c["nodes"], c["hash_lookups"], c["candidates"], c["iterations"]
-        # algorithmic bytes: a ray (48 B in + out), a 64 B node per inner-node
-        # visit, an 8 B hash probe per backtrack, a 256 B patch + 64 B of
-        # candidate-list traffic per (ray, patch) search
-        alg_bytes = 48 * nrays + 64 * nodes + 8 * hashes + 320 * cand
-        alg_flops = 12 * nodes + 296 * cand + 470 * iters + 200 * nrays
-        sec_per_frame = total_ms / args.steps / 1e3
         peaks, pk = measured_peaks()
         clocks_now = clk.summary()
         mhz = clocks_now["sm_mhz"] or 2070.0
         fp32_peak = SMS * FP32_FLOPS_PER_CLK_SM * mhz * 1e6 / 1e12
-        achieved = alg_bytes / sec_per_frame / 1e9
+        # the dominant kernel, k_collect (the traversal), timed alone through
+        # cgs_traverse on the frame's primary rays: the same launch as the
+        # frame's first traversal pass.  Algorithmic bytes per ray: 28 in,
+        # 64 per inner-node visit, 8 per backtrack (table + displacement).
+        prim = rt.camera_rays(cam, W, H, device=local)
+        for _ in range(3):
+            g.traverse(prim, stream=stream, copy_lengths=False)
+        torch.cuda.synchronize()
+        kc = g.counters()
+        kms = timed(torch, stream, flush, lambda: g.traverse(prim, stream=stream, copy_lengths=False),
+                    max(3, args.steps))
+        launch_s = sum(kms) / len(kms) / 1e3
+        nprim = int(prim.shape[1])
+        k_bytes = 28 * nprim + 64 * kc["nodes"] + 8 * kc["hash_lookups"]
+        k_flops = 12 * kc["nodes"]
+        achieved = k_bytes / launch_s / 1e9
         tr = traffic_summary()
+        # the frame as a whole: a ray (48 B in + out), a 64 B node per
+        # inner-node visit, an 8 B hash probe per backtrack, a 256 B patch +
+        # 64 B of candidate-list traffic per (ray, patch) search
+        alg_bytes = 48 * nrays + 64 * nodes + 8 * hashes + 320 * cand
+        alg_flops = 12 * nodes + 296 * cand + 470 * iters + 200 * nrays
+        sec_per_frame = total_ms / args.steps / 1e3
         extra["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                             "frac": achieved / peaks["hbm_gbs"], "traffic": tr.get("bytes_per_frame") if tr else None,
-                             "peak_source": pk, "kernel": "whole frame (closest + shade + shadow + resolve)",
-                             "fp32": {"achieved": alg_flops / sec_per_frame / 1e12, "peak": fp32_peak,
-                                      "unit": "TFLOP/s", "frac": alg_flops / sec_per_frame / 1e12 / fp32_peak,
+                             "frac": achieved / peaks["hbm_gbs"],
+                             "traffic": tr.get("bytes_per_launch") if tr else None,
+                             "peak_source": pk,
+                             "kernel": f"k_collect: traversal, first pass over the frame's {nprim} primary rays",
+                             "launch_ms": launch_s * 1e3, "algorithmic_bytes_per_launch": k_bytes,
+                             "per_ray": {"nodes": kc["nodes"] / nprim, "hash_lookups": kc["hash_lookups"] / nprim,
+                                         "hash_table_reads": kc["hash_table_reads"] / nprim},
+                             "note": "the 6.6 MB scene is L2-resident: node reads are served by L1/L2, so the "
+                                     "algorithmic bytes exceed the DRAM traffic; the kernel is bound by the L1 "
+                                     "data pipe and instruction issue",
+                             "fp32": {"achieved": k_flops / launch_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                                      "frac": k_flops / launch_s / 1e12 / fp32_peak,
                                       "peak_source": f"nominal 152 SM x 256 flop/clk at {mhz:.0f} MHz"},
-                             "per_ray": {"nodes": nodes / nrays, "hash_lookups": hashes / nrays,
-                                         "hash_table_reads": c["hash_table_reads"] / nrays,
-                                         "candidates": cand / nrays, "clip_iterations": iters / nrays}}
+                             "frame": {"algorithmic_GB_s": alg_bytes / sec_per_frame / 1e9,
+                                       "fp32_TFLOP_s": alg_flops / sec_per_frame / 1e12,
+                                       "per_ray": {"nodes": nodes / nrays, "hash_lookups": hashes / nrays,
+                                                   "hash_table_reads": c["hash_table_reads"] / nrays,
+                                                   "candidates": cand / nrays, "clip_iterations": iters / nrays}}}
         # accuracy of the primary hits on a seeded 1% pixel subset
         allr = rt.camera_rays(cam, W, H, device=local)
         sub = torch.from_numpy(scenes.random_subset(W * H, 0.01, seed=77)).to(dev)

@@ -313,6 +313,30 @@ int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, in
     return cuda_status(e);
 }
 
+int cgs_traverse(cgs_scene* s, const cgs_rays* rays, uint32_t n, int any_hit, uint32_t* list_lengths, void* stream)
+{
+    if (!s || !rays) return CGS_ERR_INVALID_ARGUMENT;
+    if (n && (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz))
+        return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (!s->hashed) return CGS_ERR_NOT_BUILT;
+    if (n == 0) return CGS_OK;
+    CGS_TRY(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
+    RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, rays->group};
+    s->launches = 0;
+    {
+        int er = ensure_engine(s, n);
+        if (er) return er;
+    }
+    cudaError_t e = run_traverse(s->dev(), r, n, any_hit != 0, s->engine.p, s->engineCapacity, s->counters.p, st,
+                                 list_lengths, &s->launches);
+    s->lastStream = st;
+    s->lastCounters = s->counters.p;
+    return cuda_status(e);
+}
+
 int cgs_intersect_host(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, int precision, float tol,
                        int any_hit, const cgs_hits* hits, void* stream)
 {

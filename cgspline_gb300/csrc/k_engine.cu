@@ -692,4 +692,23 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     return cudaGetLastError();
 }
 
+cudaError_t run_traverse(const DevScene& S, RaysSoA rays, uint32_t n, bool any, uint32_t* scratch, uint32_t capacity,
+                         Counters* cnt, cudaStream_t stream, uint32_t* listLengths, int* launches)
+{
+    if (n == 0) return cudaSuccess;
+    if (n > capacity) return cudaErrorInvalidValue;
+    Eng E = carve(scratch, capacity);
+    cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
+    const EngineConfig c = engine_config();
+    const int ct = c.collectThreads;
+    const int pc = any ? per_sm<true, false>(true, ct) : per_sm<false, false>(true, ct);
+    const int cb = sms() * std::max(1, c.collectOccupancy ? std::min(c.collectOccupancy, pc) : pc);
+    const int gc = int(std::min<uint32_t>(uint32_t(cb), (n + 31) / 32 / (ct / 32) + 1));
+    if (any) k_collect<true><<<gc, ct, 0, stream>>>(S, rays, n, nullptr, E, 0, c.backtrackCache, cnt);
+    else k_collect<false><<<gc, ct, 0, stream>>>(S, rays, n, nullptr, E, 0, c.backtrackCache, cnt);
+    if (launches) *launches += 1;
+    if (listLengths) cudaMemcpyAsync(listLengths, E.count, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, stream);
+    return cudaGetLastError();
+}
+
 }  // namespace cgs

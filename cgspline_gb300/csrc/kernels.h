@@ -53,6 +53,11 @@ size_t engine_words(uint32_t capacity, int passes);
 cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, bool any,
                       HitsSoA hits, int32_t* occluded, uint32_t* scratch, uint32_t capacity, int passes,
                       Counters* counters, cudaStream_t stream, int* launches);
+// The first collect pass of run_query alone (no clipping): each ray's
+// candidate list of that pass, its length copied to listLengths (device, may
+// be null).  For timing and profiling the traversal kernel.
+cudaError_t run_traverse(const DevScene& S, RaysSoA rays, uint32_t n, bool any, uint32_t* scratch, uint32_t capacity,
+                         Counters* cnt, cudaStream_t stream, uint32_t* listLengths, int* launches);
 constexpr int kEnginePasses = 12;
 
 // Runtime settings of the query engine: collect / resolve passes before the

@@ -211,6 +211,27 @@ class GpuScene:
                                      _stream_handle(stream)), "cgs_intersect")
         return dict(t=fo[0], u=fo[1], v=fo[2], patch=io[0], object=io[1])
 
+    def traverse(self, rays, any_hit=False, stream=None, group=None, lengths=None, copy_lengths=True):
+        """cgs_traverse: the traversal kernel alone (the query engine's first
+        collect pass, no clipping) over (7, n) device rays.  Returns the
+        per-ray candidate-list lengths (int32 tensor; patches plus object
+        markers, at most 64), or None with copy_lengths=False."""
+        torch = _torch()
+        assert rays.is_cuda and rays.dtype == torch.float32 and rays.dim() == 2 and rays.shape[0] == 7
+        rays = rays.contiguous()
+        n = rays.shape[1]
+        if lengths is None and copy_lengths:
+            lengths = torch.empty(n, dtype=torch.int32, device=rays.device)
+        gp = None
+        if group is not None:
+            group = group.to(device=rays.device, dtype=torch.int32).contiguous()
+            assert group.numel() == n
+            gp = group.data_ptr()
+        r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)], gp)
+        check(self.lib.cgs_traverse(self.h, C.byref(r), n, int(any_hit), _ptr(lengths) if copy_lengths else None,
+                                    _stream_handle(stream)), "cgs_traverse")
+        return lengths if copy_lengths else None
+
     def _intersect_host(self, rays, method, precision, tol, any_hit, stream, group=None):
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[1]

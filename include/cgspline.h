@@ -220,6 +220,18 @@ int cgs_intersect(cgs_scene* scene, const cgs_rays* rays, uint32_t n, int method
 int cgs_intersect_host(cgs_scene* scene, const cgs_rays* rays, uint32_t n, int method, int precision,
                        float tol, int any_hit, const cgs_hits* hits, void* stream);
 
+/* The traversal kernel alone: the query engine's first collect pass over n
+ * device rays (the stackless hashed walk of BVH::hashIntersect,
+ * src/rt/BVH.h:178-350, nested per object as in Context::intersect,
+ * src/rt/RayTracer.cu:295-383), with no clipping.  list_lengths (device,
+ * may be NULL) receives each ray's candidate-list length for that pass:
+ * patches plus object enter / leave markers, at most 64 (a ray with more is
+ * parked where its list filled).  The counters of the call count its node
+ * visits and backtracks.  Exists so the traversal can be timed and profiled
+ * on its own; hits come from cgs_intersect.  Asynchronous on `stream`. */
+int cgs_traverse(cgs_scene* scene, const cgs_rays* rays, uint32_t n, int any_hit, uint32_t* list_lengths,
+                 void* stream);
+
 /* spline::doBezierClipping / doSubdivision on explicit (ray, patch) pairs
  * (src/Spline.h:488-508): ray k against patch patch_ids[k] of `surface`.
  * hits->t is hit.distance (in: current best, out: closer hit if found);

@@ -289,3 +289,33 @@ def test_union_scene_hits_match_oracle_across_list_chunks(rt, oracle_mod, torch,
     assert ca["nodes"] == cb["nodes"] and ca["hash_lookups"] == cb["hash_lookups"] > 0
     assert cb["hash_table_reads"] == cb["hash_lookups"] and ca["hash_table_reads"] < ca["hash_lookups"] // 2
     g.close()
+
+
+def test_traversal_entry_point(rt, c2_small_gpu, oracle_mod, torch):
+    """cgs_traverse runs the engine's first collect pass alone.  The scene
+    has one object, and BVH::hashIntersect tests no root box, so every ray
+    enters the object: its list holds the enter and leave markers, and a ray
+    that hits a patch at least one patch between them (or its list is full
+    and parked); a ray leaving the scene behind holds only the markers.
+    Closest and any hit collect the same first-pass lists (both cull with
+    the ray's extent only), and a query visits at least the pass's nodes."""
+    cam = oracle_mod.camera_rays(S.camera_c2(), 160, 90)
+    away = np.array([[0], [0], [50], [0], [0], [1], [np.inf]], np.float32)  # leaves the scene's box behind
+    rays = torch.from_numpy(np.ascontiguousarray(np.concatenate([cam, away], axis=1))).cuda()
+    hits = to_host(c2_small_gpu.intersect(rays))
+    lc = c2_small_gpu.traverse(rays).cpu().numpy()
+    nodes = c2_small_gpu.counters()["nodes"]
+    la = c2_small_gpu.traverse(rays, any_hit=True).cpu().numpy()
+    assert np.array_equal(lc, la)
+    assert lc.min() >= 0 and lc.max() <= 64
+    hit = hits["patch"] >= 0
+    assert (lc[hit] >= 3).all()
+    assert lc.min() >= 2 and lc[-1] == 2
+    assert nodes > 0
+    base = rt.engine_config()
+    try:
+        rt.set_engine_config(passes=8)
+        c2_small_gpu.intersect(rays)
+        assert c2_small_gpu.counters()["nodes"] >= nodes
+    finally:
+        rt.set_engine_config(**base)
