@@ -141,8 +141,11 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
     LocalCounters lc;
     bool active = false, exhausted = false, jumped = false;
     uint32_t rid = 0, ncand = 0;
-    float3 o = f3(0, 0, 0), inv = f3(0, 0, 0), lo = f3(0, 0, 0), linv = f3(0, 0, 0);
-    float tmax = 0, lmax = 0, limit = 0, lt = 0;
+    // o, inv, limit: the world ray and its culling bound; co, ci, clim: those
+    // of the level walked now (the world's, or the object's local ray and
+    // best t), switched where the ray enters or leaves an object
+    float3 o = f3(0, 0, 0), inv = f3(0, 0, 0), co = f3(0, 0, 0), ci = f3(0, 0, 0);
+    float tmax = 0, limit = 0, clim = 0;
     uint32_t node = 0, key = 1, post = 0, leaf = EMPTY, tnode = 0, tkey = 1, tpost = 0, tleaf = EMPTY;
     float leafEntry = -INFINITY;
     int32_t obj = -1;
@@ -181,6 +184,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 {
                     node = 0; key = 1; post = 0; leaf = EMPTY; obj = -1; jumped = false;
                     leafEntry = -INFINITY; limit = tmax;
+                    co = o; ci = inv; clim = limit;
                     B = bvh_ref(S, topIdx);
                     nrays++;
                 }
@@ -189,15 +193,16 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     node = E.node[rid]; key = E.key[rid]; post = E.post[rid]; leaf = E.leaf[rid];
                     jumped = E.jumped[rid] != 0; leafEntry = E.leafEntry[rid]; obj = E.obj[rid];
                     limit = kAny ? tmax : E.limit[rid];
+                    co = o; ci = inv; clim = limit;
                     B = bvh_ref(S, topIdx);
                     if (obj >= 0)
                     {
                         tnode = E.tnode[rid]; tkey = E.tkey[rid]; tpost = E.tpost[rid]; tleaf = E.tleaf[rid];
                         const DevObject& O = S.objects[obj];
-                        float3 ld; float sinv;
-                        to_local(O, o, d, tmax, lo, ld, lmax, sinv);
-                        linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
-                        lt = kAny ? lmax : E.lt[rid];
+                        float3 ld; float sinv, lmax;
+                        to_local(O, o, d, tmax, co, ld, lmax, sinv);
+                        ci = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
+                        clim = kAny ? lmax : E.lt[rid];
                         B = bvh_ref(S, O.surface);
                         list[ncand++] = make_uint2(kCont, uint32_t(obj));
                     }
@@ -234,9 +239,8 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     const DevObject& O = S.objects[e];
                     const float3 d = f3(rays.dx[rid], rays.dy[rid], rays.dz[rid]);
                     float3 ld; float sinv;
-                    to_local(O, o, d, tmax, lo, ld, lmax, sinv);
-                    linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
-                    lt = lmax;
+                    to_local(O, o, d, tmax, co, ld, clim, sinv);
+                    ci = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
                     B = bvh_ref(S, O.surface);
                     node = 0; key = 1; post = 0; leaf = EMPTY; jumped = false;
                     leafEntry = -INFINITY;
@@ -259,8 +263,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
             ldg256(q, q0, q1);
             ldg256(q + 2, q2, q3);
             const uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
-            const bool top = obj < 0;
-            const float3 ro = top ? o : lo, ri = top ? inv : linv;
+            const float3 ro = co, ri = ci;
             if (left == EMPTY)
             {
                 if (jumped)
@@ -289,9 +292,8 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                     const DevObject& O = S.objects[e0];
                     const float3 d = f3(rays.dx[rid], rays.dy[rid], rays.dz[rid]);
                     float3 ld; float sinv;
-                    to_local(O, o, d, tmax, lo, ld, lmax, sinv);
-                    linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
-                    lt = lmax;
+                    to_local(O, o, d, tmax, co, ld, clim, sinv);
+                    ci = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
                     B = bvh_ref(S, O.surface);
                     node = 0; key = 1; post = 0; leaf = EMPTY; jumped = false;
                     leafEntry = -INFINITY;
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
             {
                 lc.nodes++;
                 jumped = false;
-                const float lim = top ? limit : lt;
+                const float lim = clim;
                 float L0, R0;
                 const bool iL = slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), ro, ri) && L0 < lim;
                 const bool iR = slab(R0, f3(q1.z, q1.w, q2.x), f3(q2.y, q2.z, q2.w), ro, ri) && R0 < lim;
@@ -344,6 +346,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 {
                     list[ncand++] = make_uint2(kLeave, uint32_t(obj));
                     obj = -1;
+                    co = o; ci = inv; clim = limit;
                     B = bvh_ref(S, topIdx);
                     node = tnode; key = tkey; post = tpost; leaf = tleaf;
                     leafEntry = -INFINITY;
