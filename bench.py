@@ -135,6 +135,25 @@ def traffic_summary():
         return None
 
 
+# ------------------------------------------------------- replicas (N>1) --
+def max_over_ranks(ms: float, td=None, device=None) -> float:
+    """The timed region's length as the slowest replica saw it: every rank
+    renders its own frames (rays are independent, so the path runs as
+    replicas with no data-path collective) and the job lasts as long as its
+    slowest rank."""
+    if td is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mrays(rays_per_frame: int, steps: int, world: int, total_ms: float) -> float:
+    """Whole-job throughput: the rays of all ranks' frames over the slowest rank's time."""
+    return rays_per_frame * steps * world / (total_ms * 1e-3) / 1e6
+
+
 # ----------------------------------------------------------- CPU legs --
 def cpu_leg(scene, camera, sample_rows=1):
     """The oracle's restatement of the reference's CPU tracer on every host
@@ -454,13 +473,9 @@ def main():
     with ClockSampler(local) as clk:
         ms = timed(torch, stream, flush, lambda: tracer.render(frame, cam, g, stream), args.steps)
         torch.cuda.synchronize()
-    total_ms = float(sum(ms))
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(sum(ms)), td if dist else None, dev)
     rays_per_frame = counters["rays"]
-    value = rays_per_frame * args.steps * world / (total_ms * 1e-3) / 1e6
+    value = whole_job_mrays(rays_per_frame, args.steps, world, total_ms)
 
     # e2e: the C-ABI host entry point (framebuffer copied to host inside the timed region)
     torch.cuda.synchronize()
