@@ -535,6 +535,7 @@ struct ClipState
     int cutsideStack, sl, it;
     float tol;
     bool found, b64;  // b64: FP64 projection and fat-line bounds (near-grazing)
+    bool fresh;       // the net is still to be projected (the search's first step)
 };
 
 // grazeSin > 0: the precision form (candidates within asin(grazeSin) of
@@ -546,8 +547,7 @@ __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, fl
 {
     c.b64 = kG64 && grazeSin > 0.0f && near_grazing(sink.P, sink.d, grazeSin);
     c.tol = c.b64 ? kGrazeTol : tol;
-    if (c.b64) project_net64(c.buf, sink.P, sink.o, sink.d);
-    else project_net(c.buf, sink.P, sink.o, sink.d);
+    c.fresh = true;  // the first clip_step projects the net
     c.emin = make_float2(0.0f, 0.0f);
     c.emax = make_float2(1.0f, 1.0f);
     c.cutsideStack = 0;
@@ -573,59 +573,76 @@ __device__ __forceinline__ void transpose_if(float2* p, bool t)
         }
 }
 
+// One step of the search.  The first step of a search only projects the net
+// (clip_begin leaves that to it), at the same place in the code as the
+// re-projection after a pop, so lanes starting a search and lanes popping a
+// sub-net share those instructions; it is not counted as an iteration.
 template<bool kG64 = true>
 __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, LocalCounters& lc)
 {
     const bool b64 = kG64 && c.b64;
-    if (b64 && c.it >= kGrazeIterations) return false;
-    if (c.it++ >= kMaxClipIterations) { lc.errors |= kErrClipIterations; return false; }
-    lc.iterations++;
-    const bool tr = (c.cutsideStack & 1) != 0;  // this step cuts along v
-    bool pop = true;
-    float a = 0.0f, b = 1.0f;                    // the cut, on the (transposed) net's u axis
-    if (len2(c.buf[3] - c.buf[12]) < c.tol && len2(c.buf[15] - c.buf[0]) < c.tol)
-        c.found |= approximateIntersection(sink, c.buf, c.emin, c.emax);
-    else
+    const bool fresh = c.fresh;
+    bool pop = false, tr = false;
+    float a = 0.0f, b = 1.0f;  // the cut, on the (transposed) net's u axis
+    if (!fresh)
     {
-        transpose_if(c.buf, tr);
-        float lower, upper;
-        if (b64) clip_range64(c.buf, 0, lower, upper);
-        else clip_range(c.buf, 0, lower, upper);
-        const float delta = upper - lower;
-        const float lo = tr ? c.emin.y : c.emin.x, hi = tr ? c.emax.y : c.emax.x;
-        if (delta > 0.8f)
+        if (b64 && c.it >= kGrazeIterations) return false;
+        if (c.it++ >= kMaxClipIterations) { lc.errors |= kErrClipIterations; return false; }
+        lc.iterations++;
+        tr = (c.cutsideStack & 1) != 0;  // this step cuts along v
+        pop = true;
+        if (len2(c.buf[3] - c.buf[12]) < c.tol && len2(c.buf[15] - c.buf[0]) < c.tol)
+            c.found |= approximateIntersection(sink, c.buf, c.emin, c.emax);
+        else
         {
-            // split in halves: keep the upper half, push the lower
-            const float h = 0.5f * (lo + hi);
-            const float4 pushed = tr ? make_float4(c.emin.x, c.emin.y, c.emax.x, h)
-                                     : make_float4(c.emin.x, c.emin.y, h, c.emax.y);
-            if (tr) c.emin.y = h; else c.emin.x = h;
-            c.cutsideStack = tr ? ((c.cutsideStack << 1) & ~3) : ((c.cutsideStack << 1) | 3);
-            if (c.sl >= kClipStack) { lc.errors |= kErrClipStack; return false; }
-            st[c.sl++] = pushed;
-            a = 0.5f; b = 1.0f;
-            pop = false;
+            transpose_if(c.buf, tr);
+            float lower, upper;
+            if (b64) clip_range64(c.buf, 0, lower, upper);
+            else clip_range(c.buf, 0, lower, upper);
+            const float delta = upper - lower;
+            const float lo = tr ? c.emin.y : c.emin.x, hi = tr ? c.emax.y : c.emax.x;
+            if (delta > 0.8f)
+            {
+                // split in halves: keep the upper half, push the lower
+                const float h = 0.5f * (lo + hi);
+                const float4 pushed = tr ? make_float4(c.emin.x, c.emin.y, c.emax.x, h)
+                                         : make_float4(c.emin.x, c.emin.y, h, c.emax.y);
+                if (tr) c.emin.y = h; else c.emin.x = h;
+                c.cutsideStack = tr ? ((c.cutsideStack << 1) & ~3) : ((c.cutsideStack << 1) | 3);
+                if (c.sl >= kClipStack) { lc.errors |= kErrClipStack; return false; }
+                st[c.sl++] = pushed;
+                a = 0.5f; b = 1.0f;
+                pop = false;
+            }
+            else if (delta > 0.0f)
+            {
+                const float sz = hi - lo;
+                const float n0 = lo + sz * lower, n1 = hi - sz * (1.0f - upper);
+                if (tr) { c.emin.y = n0; c.emax.y = n1; } else { c.emin.x = n0; c.emax.x = n1; }
+                c.cutsideStack ^= 1;
+                a = lower; b = upper;
+                pop = false;
+            }
         }
-        else if (delta > 0.0f)
+        if (pop)
         {
-            const float sz = hi - lo;
-            const float n0 = lo + sz * lower, n1 = hi - sz * (1.0f - upper);
-            if (tr) { c.emin.y = n0; c.emax.y = n1; } else { c.emin.x = n0; c.emax.x = n1; }
-            c.cutsideStack ^= 1;
-            a = lower; b = upper;
-            pop = false;
+            c.cutsideStack >>= 1;
+            if (--c.sl < 0) return false;
+            const float4 e = st[c.sl];
+            c.emin = make_float2(e.x, e.y);
+            c.emax = make_float2(e.z, e.w);
+            a = c.emin.x; b = c.emax.x;
         }
     }
-    if (pop)
+    if (fresh || pop)
     {
-        c.cutsideStack >>= 1;
-        if (--c.sl < 0) return false;
-        const float4 e = st[c.sl];
-        c.emin = make_float2(e.x, e.y);
-        c.emax = make_float2(e.z, e.w);
         if (b64) project_net64(c.buf, sink.P, sink.o, sink.d);
         else project_net(c.buf, sink.P, sink.o, sink.d);
-        a = c.emin.x; b = c.emax.x;
+    }
+    if (fresh)
+    {
+        c.fresh = false;
+        return true;
     }
     subpatchU(c.buf, a, b);  // every lane: the cut, or the u range of the popped sub-net
     if (pop) subpatchV(c.buf, c.emin.y, c.emax.y);
