@@ -288,7 +288,7 @@ int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, in
                   const cgs_hits* hits, void* stream)
 {
     if (!s || !rays || !hits || !valid_query(method, precision) || !(tol > 0.0f)) return CGS_ERR_INVALID_ARGUMENT;
-    if (!hits->patch || (!any_hit && (!hits->t || !hits->u || !hits->v || !hits->object)))
+    if (n && (!hits->patch || (!any_hit && (!hits->t || !hits->u || !hits->v || !hits->object))))
         return CGS_ERR_INVALID_ARGUMENT;
     if (n && (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz))
         return CGS_ERR_INVALID_ARGUMENT;

@@ -319,3 +319,56 @@ def test_traversal_entry_point(rt, c2_small_gpu, oracle_mod, torch):
         assert c2_small_gpu.counters()["nodes"] >= nodes
     finally:
         rt.set_engine_config(**base)
+
+
+def _edge_rays():
+    """Rays at the edges of the slab test and the search: directions with
+    exact zero components (infinite inverse) from origins exactly on patch
+    and box planes (x or y = 0, 1, 2, 3, 4: 0 x inf = NaN inside the slab
+    test), short and zero extents, rays along z (the reference's projection
+    axes are degenerate for them: they miss), and rays cast sideways and from
+    inside the field's box.  No ray lies in the surface: the field is 0 along
+    its patch boundaries, so a ray along one of them at z = 0 meets a
+    continuum of roots, of which the FP32 search may report any."""
+    rays = []
+    for x in (0.0, 0.5, 1.0, 2.0, 2.5, 3.0, 4.0):
+        for y in (0.0, 1.0, 1.5, 3.0, 4.0):
+            for d in ((0, 0.6, -0.8), (0, -0.6, -0.8), (0.6, 0, -0.8), (-0.6, 0, -0.8), (0, 0, -1)):
+                for tmax in (np.inf, 2.0, 0.0):
+                    rays.append((x, y, 2.0, *d, tmax))
+    for z in (-0.2, 0.1, 0.3):
+        for y in (0.0, 1.0, 2.2, 4.0):
+            rays.append((-1.0, y, z, 1, 0, 0, np.inf))    # along +x
+            rays.append((2.0, y, z, 0, 1, 0, np.inf))     # from inside the box along +y
+            rays.append((2.0, 2.0, z, -1, 0, 0, np.inf))  # from inside along -x
+    return np.ascontiguousarray(np.array(rays, np.float32).T)
+
+
+def test_edge_rays_match_oracle(rt, c1_gpu, c1_oracle, torch):
+    rays = _edge_rays()
+    g = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda()))
+    o = c1_oracle.intersect(rays)
+    compare_hits(g, o)
+    assert (g["patch"] >= 0).sum() > 50 and (g["patch"] < 0).sum() > 100
+    zero = rays[6] == 0.0
+    assert (g["patch"][zero] < 0).all()  # a zero extent hits nothing
+    ga = to_host(c1_gpu.intersect(torch.from_numpy(rays).cuda(), any_hit=True))
+    oa = c1_oracle.intersect(rays, any_hit=True)
+    assert np.array_equal(ga["patch"] >= 0, oa["patch"] >= 0)
+    assert c1_gpu.counters()["device_errors"] == 0
+
+
+def test_empty_inputs(rt, c1_gpu, torch):
+    """Zero rays are a no-op on every query entry point (their arrays may be
+    null); an empty render batch is refused as an invalid argument."""
+    from cgspline_gb300._capi import CgsError
+    none = torch.empty((7, 0), dtype=torch.float32, device="cuda")
+    h = c1_gpu.intersect(none)
+    assert all(v.numel() == 0 for v in h.values())
+    assert all(v.numel() == 0 for v in c1_gpu.intersect(none, any_hit=True).values())
+    assert c1_gpu.traverse(none).numel() == 0
+    assert c1_gpu.intersect(np.zeros((7, 0), np.float32))["patch"].size == 0
+    with pytest.raises(CgsError) as e:
+        rt.RayTracer(rt.Options()).render_batch([], c1_gpu)
+    assert e.value.status == 1
+    torch.cuda.synchronize()
