@@ -372,3 +372,58 @@ def test_empty_inputs(rt, c1_gpu, torch):
         rt.RayTracer(rt.Options()).render_batch([], c1_gpu)
     assert e.value.status == 1
     torch.cuda.synchronize()
+
+
+def _rational_surface(seed=11):
+    """Ten patches side by side along x: eight bumpy rational patches
+    (homogeneous control points with weights in [0.5, 2]), one collapsed to a
+    point and one whose control points lie on a line."""
+    rng = np.random.default_rng(seed)
+    nets = []
+    for k in range(10):
+        i, j = np.meshgrid(np.arange(4), np.arange(4), indexing="xy")
+        x, y = k * 1.5 + i / 3.0, j / 3.0
+        z = rng.normal(0.0, 0.3, (4, 4))
+        w = rng.uniform(0.5, 2.0, (4, 4))
+        if k == 8:
+            x, y, z, w = np.full((4, 4), k * 1.5 + 0.5), np.full((4, 4), 0.5), np.zeros((4, 4)), np.ones((4, 4))
+        if k == 9:
+            x, y, z, w = k * 1.5 + i / 3.0 + j / 9.0, np.full((4, 4), 0.5), np.zeros((4, 4)), np.ones((4, 4))
+        # homogeneous points (w x, w y, w z, w): the patch projects to x, y, z where w = 1
+        nets.append(np.stack([x * w, y * w, z * w, w], axis=-1).reshape(16, 4))
+    pts = np.concatenate(nets).astype(np.float32)
+    return S.Surface(pts, np.arange(pts.shape[0], dtype=np.uint32))
+
+
+def test_rational_and_degenerate_patches(rt, oracle_mod, torch):
+    """Rational patches (non-unit weights) and degenerate ones (a point, a
+    line) through the patch-pair entry point and the BVH query, against the
+    oracle's device-structure search: the same found / missed decisions and t
+    within 1e-5."""
+    surf = _rational_surface()
+    sc = S.Scene([surf], [S.Object(0, S.IDENTITY16.copy(), S.IDENTITY16.copy())],
+                 [S.Light((1, 1, 1), 1.0, (0, 0, 5), 0.0, (0, 0, -1), 0.0)])
+    g = rt.GpuScene(sc)
+    rng = np.random.default_rng(5)
+    n = 4000
+    pids = rng.integers(0, 10, n).astype(np.int32)
+    tx = pids * 1.5 + rng.uniform(-0.1, 1.1, n)
+    ty = rng.uniform(-0.1, 1.1, n)
+    d = np.stack([rng.uniform(-0.3, 0.3, n), rng.uniform(-0.3, 0.3, n), -np.ones(n)])
+    d /= np.linalg.norm(d, axis=0)
+    o = np.stack([tx, ty, np.full(n, 0.0)]) - 3.0 * d
+    rays = np.ascontiguousarray(np.concatenate([o, d, np.full((1, n), np.inf)]).astype(np.float32))
+    found, t, u, v = rt.do_bezier_clipping(g, 0, torch.from_numpy(rays).cuda(), torch.from_numpy(pids).cuda())
+    found, t = found.cpu().numpy(), t.cpu().numpy()
+    for k in range(n):
+        hit, to, _, _ = oracle_mod.patch_intersect(surf.points, surf.indices[16 * pids[k]:16 * pids[k] + 16],
+                                                    rays[:, k], method=oracle_mod.CLIP_DEVICE)
+        assert bool(found[k]) == hit, k
+        if hit:
+            assert abs(t[k] - to) <= 1e-5 * to, k
+    assert found[pids < 8].mean() > 0.3 and not found[pids == 8].any()
+    q = to_host(g.intersect(torch.from_numpy(rays).cuda()))
+    oq = oracle_mod.OracleScene(sc).intersect(rays, method=oracle_mod.CLIP_DEVICE)
+    compare_hits(q, oq)
+    assert g.counters()["device_errors"] == 0
+    g.close()
