@@ -94,7 +94,7 @@ typedef struct cgs_camera {
     float fovy;          /* radians */
 } cgs_camera;
 
-/* src/rt/RayTracer.h:26-34 plus this build's choices */
+/* src/rt/RayTracer.h:26-34 plus this library's search, precision, schedule and sampling choices */
 typedef struct cgs_render_options {
     int recursion_depth; /* mirror bounces after the primary hit (reference GPU default 6) */
     float eps;           /* shadow / bounce ray offset (reference 1e-4) */

@@ -1,7 +1,7 @@
 // cgs_oracle.cpp -- TEST INFRASTRUCTURE, NOT PART OF THE PRODUCT.
 //
 // A CPU restatement of the ray--bicubic-patch path of MachSilva/cgspline, used
-// only as the checker for the CUDA implementation in cgspline_gb300/.  Only
+// only to verify the CUDA implementation in cgspline_gb300/.  Only
 // tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may load this
 // library.  Every function cites the reference file:line it restates (paths are
 // relative to the reference project's root).

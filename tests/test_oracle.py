@@ -1,4 +1,4 @@
-"""CPU tests of the oracle (the checker): known-answer patches, BVH and hash
+"""CPU tests of the oracle: known-answer patches, BVH and hash
 invariants of the reference (src/rt/BVH.cpp:9-124, src/rt/PerfectHashFunction.cu:486-503),
 agreement between its FP32 variants and its FP64 truth, and determinism."""
 import math
