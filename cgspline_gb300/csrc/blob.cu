@@ -59,24 +59,32 @@ void get_bvh(Reader& r, HostBVH& b)
 }
 
 // the structure of a BVH read from a file: node links and leaf lists in range
+// Besides the bounds of every index: the layout the traversal relies on to end.
+// Children come after their parent (pre-order), so a descent always moves to a
+// higher node; children carry the heap keys 2k and 2k+1 of their parent and
+// the root key 1, so a backtrack's key names the sibling of an ancestor (the
+// hash check below then maps it to that node).
 bool bvh_sane(const HostBVH& b, uint32_t elements)
 {
-    if (b.nodes.empty() || b.keys.size() != b.nodes.size()) return false;
-    for (const Node& n : b.nodes)
+    if (b.nodes.empty() || b.keys.size() != b.nodes.size() || b.keys[0] != 1u) return false;
+    for (size_t i = 0; i < b.nodes.size(); i++)
     {
+        const Node& n = b.nodes[i];
+        if (n.left != EMPTY && (n.left <= i || n.right <= i || n.left >= b.nodes.size() ||
+                                n.right >= b.nodes.size() || b.keys[n.left] != 2u * b.keys[i] ||
+                                b.keys[n.right] != 2u * b.keys[i] + 1u))
+            return false;
         if (n.left == EMPTY)
         {
             // a leaf lists at least one element (the build refuses empty leaves)
             if (n.right + 1 >= b.indices.size() || b.indices[n.right] == EMPTY) return false;
-            for (size_t i = n.right; ; i++)
+            for (size_t j = n.right; ; j++)
             {
-                if (i >= b.indices.size()) return false;
-                if (b.indices[i] == EMPTY) break;
-                if (b.indices[i] >= elements) return false;
+                if (j >= b.indices.size()) return false;
+                if (b.indices[j] == EMPTY) break;
+                if (b.indices[j] >= elements) return false;
             }
         }
-        else if (n.left >= b.nodes.size() || n.right >= b.nodes.size())
-            return false;
     }
     return true;
 }

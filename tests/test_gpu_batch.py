@@ -295,5 +295,23 @@ def test_scene_blob_round_trip(rt, pair, torch, tmp_path):
     with pytest.raises(CgsError) as e:
         rt.GpuScene.load(tmp_path / "missing.cgsb")
     assert e.value.status == 11
+    # a BVH whose root's children point back up (a cycle the traversal would
+    # walk for ever) or carry the wrong heap keys is refused before upload
+    import struct
+    s0 = scs[0].surfaces[0]
+    nodes_at = 24 + 4 + s0.points.size * 4 + 4 + s0.indices.size * 4  # header, points, indices
+    nnodes = struct.unpack_from("<I", data, nodes_at)[0]
+    assert nnodes > 1
+    root = nodes_at + 4  # 56-byte nodes: two boxes of 6 floats, then left, right
+    left, right = struct.unpack_from("<II", data, root + 48)
+    assert left == 1 and right > 1
+    keys_at = nodes_at + 4 + 56 * nnodes + 4
+    for at, value in ((root + 48, 0), (root + 52, 0), (keys_at + 4 * left, 5)):
+        broken = bytearray(data)
+        struct.pack_into("<I", broken, at, value)
+        bad.write_bytes(bytes(broken))
+        with pytest.raises(CgsError) as e:
+            rt.GpuScene.load(bad)
+        assert e.value.status == 1
     a.close()
     b.close()
