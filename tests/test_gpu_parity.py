@@ -427,3 +427,33 @@ def test_rational_and_degenerate_patches(rt, oracle_mod, torch):
     compare_hits(q, oq)
     assert g.counters()["device_errors"] == 0
     g.close()
+
+
+@pytest.mark.parametrize("index", [2, 9, 21, 33])
+@pytest.mark.parametrize("split", [0, 1])
+def test_union_scenes_closest_and_any_match_oracle(rt, oracle_mod, torch, index, split):
+    """More seeded unions (34-59 objects under random transforms), both BVH
+    builds: closest hits equal the oracle's device-structure search (same
+    object; same patch or an edge tie; t within 1e-5), any-hit decisions are
+    identical, and the polished hits stay within 1e-5 of the FP64 oracle."""
+    sc = S.scene_c4(index, max_patches=6000)
+    g = rt.GpuScene(sc, split=split)
+    o = oracle_mod.OracleScene(sc, split=split)
+    rays = oracle_mod.camera_rays(S.camera_c4(index)[0], 128, 128)
+    tr = torch.from_numpy(rays).cuda()
+    h = to_host(g.intersect(tr))
+    ref = o.intersect(rays, method=oracle_mod.CLIP_DEVICE)
+    compare_hits(h, ref)
+    hit = ref["patch"] >= 0
+    assert np.array_equal(h["object"][hit], ref["object"][hit])
+    ha = to_host(g.intersect(tr, any_hit=True))
+    ra = o.intersect(rays, method=oracle_mod.CLIP_DEVICE, any_hit=True)
+    assert np.array_equal(ha["patch"] >= 0, ra["patch"] >= 0)
+    hp = to_host(g.intersect(tr, precision=rt.FP32_POLISH64))
+    r64 = o.intersect(rays, precision=oracle_mod.FP64)
+    same = (hp["patch"] >= 0) & (hp["patch"] == r64["patch"]) & (hp["object"] == r64["object"])
+    assert same.sum() > 0.9 * (r64["patch"] >= 0).sum()
+    rel = np.abs(hp["t"][same] - r64["t"][same]) / r64["t"][same]
+    assert rel.max(initial=0) <= 1e-5
+    assert g.counters()["device_errors"] == 0
+    g.close()
