@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson stream) comparison")
     ap.add_argument("--no-precision", action="store_true", help="skip the grazing-ray precision comparison")
     ap.add_argument("--no-tune", action="store_true", help="keep the default engine settings (no autotuner)")
+    ap.add_argument("--scene", default="c2",
+                    help="frame scene: c2 (the torus, default) or c4:<i> / c5:<i>, the seeded union scene i of "
+                         "the batching / serving workloads with its camera (profiling cases)")
     return ap.parse_args()
 
 
@@ -420,6 +423,19 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
     return out
 
 
+def frame_scene(scenes, name):
+    """The frame's scene and camera: the C2 torus, or a union scene of the
+    batching (c4:<i>) or serving (c5:<i>) workloads."""
+    if name == "c2":
+        return scenes.scene_c2(), scenes.camera_c2()
+    kind, _, index = name.partition(":")
+    if kind == "c4":
+        return scenes.scene_c4(int(index)), scenes.camera_c4(int(index))[0]
+    if kind == "c5":
+        return scenes.scene_c5(int(index)), scenes.camera_c5(int(index))
+    raise SystemExit(f"unknown scene {name!r}")
+
+
 def main():
     args = parse()
     global W, H
@@ -443,7 +459,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    scene, cam = scenes.scene_c2(), scenes.camera_c2()
+    scene, cam = frame_scene(scenes, args.scene)
     split = rt.SPLIT_LONGEST if args.split == "longest" else rt.SPLIT_REFERENCE
     g = rt.GpuScene(scene, device=local, split=split)
     sched = rt.WAVEFRONT if args.schedule == "wavefront" else rt.PLAIN
@@ -579,8 +595,11 @@ def main():
                 "warmup": max(3, args.warmup), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32+f64polish" if prec == rt.FP32_POLISH64 else "f32",
-                "data": "synthetic (seeded displaced torus)",
-                "config": {"workload": f"torus 16384 patches, {W}x{H} primary + {DEPTH} bounce, PBR, 2 point lights",
+                "data": "synthetic (seeded displaced torus)" if args.scene == "c2" else f"synthetic (union scene {args.scene})",
+                "config": {"workload": (f"torus 16384 patches, {W}x{H} primary + {DEPTH} bounce, PBR, 2 point lights"
+                                        if args.scene == "c2" else
+                                        f"union scene {args.scene} ({scene.patch_count} patches), {W}x{H} primary + "
+                                        f"{DEPTH} bounce, PBR"),
                            "schedule": args.schedule, "bvh_split": args.split, "rays_per_frame": rays_per_frame,
                            "primary_rays": W * H, "l2": "flushed (2x L2 written) before every frame",
                            "parallelism": f"replicas x{world}"},
