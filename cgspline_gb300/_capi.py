@@ -117,6 +117,7 @@ SIGNATURES = [
                                      P]),
     ("cgs_traverse", C.c_int, [P, C.POINTER(Rays), U32, C.c_int, P, P]),
     ("cgs_patch_intersect", C.c_int, [P, U32, C.POINTER(Rays), P, U32, C.c_int, C.c_float, C.POINTER(Hits), P]),
+    ("cgs_patch_normal", C.c_int, [P, U32, P, P, P, U32, P, P]),
     ("cgs_render", C.c_int, [P, C.POINTER(Camera), U32, U32, C.POINTER(RenderOptions), P, U32, P, P]),
     ("cgs_render_host", C.c_int, [P, C.POINTER(Camera), U32, U32, C.POINTER(RenderOptions), P, P, P]),
     ("cgs_render_batch", C.c_int, [P, C.POINTER(RenderRequest), U32, C.POINTER(RenderOptions), P]),

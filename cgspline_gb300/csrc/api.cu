@@ -398,9 +398,27 @@ int cgs_patch_intersect(cgs_scene* s, uint32_t surface, const cgs_rays* rays, co
     s->launches = 1;
     s->lastStream = st;
     s->lastCounters = s->counters.p;
-    return cuda_status(launch_patch_pairs(s->dev(), surface, r, pids, n, q,
+    return cuda_status(launch_patch_pairs(s->dev(), surface, s->surfaces[surface].patchCount(), r, pids, n, q,
                                           HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, s->counters.p,
                                           st));
+}
+
+int cgs_patch_normal(cgs_scene* s, uint32_t surface, const uint32_t* pids, const float* u, const float* v, uint32_t n,
+                     float* normals, void* stream)
+{
+    if (!s || (n && (!pids || !u || !v || !normals))) return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (!s->uploaded) return CGS_ERR_NOT_BUILT;
+    if (surface >= s->surfaces.size()) return CGS_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CGS_OK;
+    CGS_TRY(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
+    s->launches = 1;
+    s->lastStream = st;
+    s->lastCounters = s->counters.p;
+    return cuda_status(launch_patch_normals(s->dev(), surface, s->surfaces[surface].patchCount(), pids, u, v, n,
+                                            normals, s->counters.p, st));
 }
 
 // RayTracer::render (src/rt/RayTracer.cu:107-180) for a batch of requests;

@@ -18,7 +18,7 @@ constexpr float kPi = 3.14159265358979323846f;
 constexpr float kInvPi = 0.318309886183790671538f;
 
 // Error bits reported through Counters::errors.
-enum : uint32_t { kErrClipStack = 1u, kErrClipIterations = 2u, kErrTraversal = 4u, kErrGroup = 8u };
+enum : uint32_t { kErrClipStack = 1u, kErrClipIterations = 2u, kErrTraversal = 4u, kErrGroup = 8u, kErrPatchId = 16u };
 
 // ------------------------------------------------------------ data layout --
 // One BVH (a surface's patch BVH or the object-level BVH).  Node offsets in

@@ -12,13 +12,18 @@ namespace {
 
 constexpr int kPairThreads = 128;
 
-__global__ void __launch_bounds__(kPairThreads) k_patch_pairs(DevScene S, uint32_t surface, RaysSoA rays,
-                                                              const uint32_t* __restrict__ pids, uint32_t n, Query q,
-                                                              HitsSoA hits, Counters* cnt)
+__global__ void __launch_bounds__(kPairThreads) k_patch_pairs(DevScene S, uint32_t surface, uint32_t patches,
+                                                              RaysSoA rays, const uint32_t* __restrict__ pids,
+                                                              uint32_t n, Query q, HitsSoA hits, Counters* cnt)
 {
     LocalCounters lc;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
+    if (i < n && __ldg(pids + i) >= patches)
+    {
+        hits.patch[i] = 0;
+        lc.errors |= kErrPatchId;
+    }
+    else if (i < n)
     {
         const float3 o = f3(__ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i));
         const float3 d = f3(__ldg(rays.dx + i), __ldg(rays.dy + i), __ldg(rays.dz + i));
@@ -137,12 +142,40 @@ cudaError_t launch_scatter_hits(const QueryChunk* table, const uint32_t* hdr, ui
     return cudaGetLastError();
 }
 
-cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, RaysSoA rays, const uint32_t* patch_ids,
-                               uint32_t n, Query q, HitsSoA hits, Counters* counters, cudaStream_t stream)
+cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, uint32_t patches, RaysSoA rays,
+                               const uint32_t* patch_ids, uint32_t n, Query q, HitsSoA hits, Counters* counters,
+                               cudaStream_t stream)
 {
     if (n == 0) return cudaSuccess;
-    k_patch_pairs<<<(n + kPairThreads - 1) / kPairThreads, kPairThreads, 0, stream>>>(S, surface, rays, patch_ids, n,
-                                                                                      q, hits, counters);
+    k_patch_pairs<<<(n + kPairThreads - 1) / kPairThreads, kPairThreads, 0, stream>>>(S, surface, patches, rays,
+                                                                                      patch_ids, n, q, hits, counters);
+    return cudaGetLastError();
+}
+
+__global__ void k_patch_normals(DevScene S, uint32_t surface, uint32_t patches, const uint32_t* __restrict__ pids,
+                                const float* __restrict__ u, const float* __restrict__ v, uint32_t n, float* normals,
+                                Counters* cnt)
+{
+    LocalCounters lc;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const uint32_t p = __ldg(pids + i);
+        float3 N = f3(0.0f, 0.0f, 0.0f);
+        if (p < patches) N = versor(patch_normal(S.patches + 16ull * (__ldg(S.patchBase + surface) + p),
+                                                 __ldg(u + i), __ldg(v + i)));
+        else lc.errors |= kErrPatchId;
+        normals[i] = N.x; normals[n + i] = N.y; normals[2ull * n + i] = N.z;
+    }
+    flush_counters(cnt, lc, 0);
+}
+
+cudaError_t launch_patch_normals(const DevScene& S, uint32_t surface, uint32_t patches, const uint32_t* patch_ids,
+                                 const float* u, const float* v, uint32_t n, float* normals, Counters* counters,
+                                 cudaStream_t stream)
+{
+    if (n == 0) return cudaSuccess;
+    k_patch_normals<<<(n + 255) / 256, 256, 0, stream>>>(S, surface, patches, patch_ids, u, v, n, normals, counters);
     return cudaGetLastError();
 }
 

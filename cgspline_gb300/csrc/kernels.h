@@ -14,9 +14,18 @@ struct RaysSoA { const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax; const uint32_t
 struct HitsSoA { float *t, *u, *v; int32_t *patch, *object; };
 
 // ---------------------------------------------------------- ray queries --
-// spline::doBezierClipping on explicit (ray, patch) pairs, one thread per pair.
-cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, RaysSoA rays, const uint32_t* patch_ids,
-                               uint32_t n, Query q, HitsSoA hits, Counters* counters, cudaStream_t stream);
+// spline::doBezierClipping on explicit (ray, patch) pairs, one thread per pair;
+// a patch id at or past `patches` (the surface's count) is a miss and raises
+// error bit kErrPatchId.
+cudaError_t launch_patch_pairs(const DevScene& S, uint32_t surface, uint32_t patches, RaysSoA rays,
+                               const uint32_t* patch_ids, uint32_t n, Query q, HitsSoA hits, Counters* counters,
+                               cudaStream_t stream);
+// rt::normal (src/rt/Primitive.cu:270-275) at (u[k], v[k]) of patch patch_ids[k]:
+// the unit normal in the surface's space, written as SoA nx | ny | nz (3 n
+// floats); an id past the surface's count gives (0, 0, 0) and kErrPatchId.
+cudaError_t launch_patch_normals(const DevScene& S, uint32_t surface, uint32_t patches, const uint32_t* patch_ids,
+                                 const float* u, const float* v, uint32_t n, float* normals, Counters* counters,
+                                 cudaStream_t stream);
 
 // One thread per ray with the whole search inline (the plain query path);
 // `group` applies where rays.group is null.  Any hit writes hits.patch only.

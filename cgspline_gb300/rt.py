@@ -270,6 +270,20 @@ def do_bezier_clipping(scene: GpuScene, surface: int, rays, patch_ids, t=None, t
     return found, tt, u, v
 
 
+def normal(scene: GpuScene, surface: int, patch_ids, u, v, stream=None):
+    """rt::normal (src/rt/Primitive.cu:270-275) for a batch: the unit normal of
+    patch patch_ids[k] of `surface` at (u[k], v[k]), in the surface's space.
+    Returns a (3, n) float32 tensor (zeros for a patch id past the surface)."""
+    torch = _torch()
+    pid = patch_ids.to(torch.int32).contiguous()
+    uu, vv = u.to(torch.float32).contiguous(), v.to(torch.float32).contiguous()
+    n = pid.numel()
+    out = torch.empty((3, n), dtype=torch.float32, device=pid.device)
+    check(scene.lib.cgs_patch_normal(scene.h, surface, _ptr(pid), _ptr(uu), _ptr(vv), n, _ptr(out),
+                                     _stream_handle(stream)), "cgs_patch_normal")
+    return out
+
+
 @dataclasses.dataclass
 class Options:
     """rt::RayTracer::Options (src/rt/RayTracer.h:26-34) plus the search method,

@@ -131,7 +131,8 @@ typedef struct cgs_counters {
     uint64_t candidates;      /* (ray, patch) pairs searched */
     uint64_t iterations;      /* clip / subdivision iterations */
     uint64_t device_errors;   /* bit mask: 1 clip stack full, 2 clip iteration limit,
-                                 4 traversal step limit, 8 ray of an unknown group */
+                                 4 traversal step limit, 8 ray of an unknown group,
+                                 16 a patch id past its surface's patch count */
     uint64_t kernel_launches;
     uint64_t hash_table_reads; /* backtracks answered through the perfect hash; the rest
                                   came from the traversal's backtrack cache */
@@ -235,10 +236,21 @@ int cgs_traverse(cgs_scene* scene, const cgs_rays* rays, uint32_t n, int any_hit
 /* spline::doBezierClipping / doSubdivision on explicit (ray, patch) pairs
  * (src/Spline.h:488-508): ray k against patch patch_ids[k] of `surface`.
  * hits->t is hit.distance (in: current best, out: closer hit if found);
- * hits->patch is set to 1 when a closer hit was found, else 0.  Device pointers. */
+ * hits->patch is set to 1 when a closer hit was found, else 0; a patch id at or
+ * past the surface's patch count is a miss and sets device_errors bit 16.
+ * Device pointers. */
 int cgs_patch_intersect(cgs_scene* scene, uint32_t surface, const cgs_rays* rays,
                         const uint32_t* patch_ids, uint32_t n, int method, float tol,
                         const cgs_hits* hits, void* stream);
+
+/* rt::normal(const BezierSurface&, const rt::Intersection&) (src/rt/Primitive.cu:270-275):
+ * the unit normal of patch patch_ids[k] of `surface` at (u[k], v[k]), in the
+ * surface's own space (mat::normal normalized, src/SplineMat.h:178-187).
+ * normals receives 3 n floats as nx | ny | nz.  A patch id at or past the
+ * surface's patch count gives (0, 0, 0) and device_errors bit 16.  Device
+ * pointers; asynchronous on `stream`. */
+int cgs_patch_normal(cgs_scene* scene, uint32_t surface, const uint32_t* patch_ids, const float* u, const float* v,
+                     uint32_t n, float* normals, void* stream);
 
 /* ------------------------------------------------------------- render -- */
 /* RayTracer::render (src/rt/RayTracer.cu:107-180): width x height pixels,

@@ -457,3 +457,41 @@ def test_union_scenes_closest_and_any_match_oracle(rt, oracle_mod, torch, index,
     assert rel.max(initial=0) <= 1e-5
     assert g.counters()["device_errors"] == 0
     g.close()
+
+
+def test_patch_normals_match_oracle(rt, torch, oracle_mod):
+    """rt::normal through cgs_patch_normal on the heightfield and on rational
+    patches, against the oracle's normal (src/SplineMat.h:178-187), and patch
+    ids past the surface refused on the device (zero normal, error bit 16),
+    as they are by the patch-pair entry point."""
+    # the rational surface's patches 8 and 9 (a point, a line) have no normal:
+    # their derivatives are parallel and the cross product is rounding noise
+    for surf, regular in ((S.scene_c1().surfaces[0], 16), (_rational_surface(), 8)):
+        sc = S.Scene([surf], [S.Object(0, S.IDENTITY16.copy(), S.IDENTITY16.copy())],
+                     [S.Light((1, 1, 1), 1.0, (0, 0, 5), 0.0, (0, 0, -1), 0.0)])
+        g = rt.GpuScene(sc)
+        rng = np.random.default_rng(3)
+        n = 500
+        pids = rng.integers(0, regular, n).astype(np.int32)
+        u, v = rng.uniform(0, 1, n).astype(np.float32), rng.uniform(0, 1, n).astype(np.float32)
+        got = rt.normal(g, 0, torch.from_numpy(pids).cuda(), torch.from_numpy(u).cuda(),
+                        torch.from_numpy(v).cuda()).cpu().numpy()
+        nets = surf.patches()
+        for k in range(n):
+            _, nk = oracle_mod.patch_eval(nets[pids[k]], float(u[k]), float(v[k]))
+            # FP32 normals of two evaluation orders (power basis without FMA in the
+            # oracle, Bernstein form with FMA here) agree to a few 1e-5 on steep
+            # rational patches
+            assert np.abs(got[:, k] - nk).max() < 2e-4, k
+        assert g.counters()["device_errors"] == 0
+        bad = torch.tensor([0, surf.patch_count, surf.patch_count + 7], dtype=torch.int32, device="cuda")
+        half = torch.full((3,), 0.5, device="cuda")
+        out = rt.normal(g, 0, bad, half, half).cpu().numpy()
+        assert np.abs(out[:, 1:]).max() == 0.0 and np.linalg.norm(out[:, 0]) > 0.5
+        assert g.counters()["device_errors"] == 16
+        rays = torch.zeros((7, 3), device="cuda")
+        rays[5] = -1.0
+        rays[6] = float("inf")
+        found, t, _, _ = rt.do_bezier_clipping(g, 0, rays, bad)
+        assert found.cpu().tolist()[1:] == [0, 0] and g.counters()["device_errors"] == 16
+        g.close()
