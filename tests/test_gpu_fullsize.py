@@ -1,0 +1,86 @@
+"""Size-independent properties at the full headline size: the C2 torus
+(16,384 patches) and all 2,073,600 primary rays of its 1920x1080 frame, the
+size the benchmark runs, where lists park, passes resume and the inline
+fallback takes over.
+
+- Every engine setting (passes, block sizes, backtrack cache) gives the same
+  hits: same hit/miss and patch (or an edge tie), t within 1e-6.
+- A ray has a closest hit exactly when it has any hit (unbounded rays).
+- The backtrack cache changes where a backtrack finds its node, not the walk:
+  node and backtrack counts are equal with it on and off.
+- The polished hits stay within 1e-5 of the FP32 hits they refine (t), on the
+  same patch.
+"""
+import numpy as np
+import pytest
+
+from cgspline_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    import torch
+    from cgspline_gb300 import rt
+    g = rt.GpuScene(S.scene_c2())
+    rays = rt.camera_rays(S.camera_c2(), 1920, 1080)
+    yield rt, torch, g, rays
+    g.close()
+
+
+def host(d):
+    return {k: v.cpu().numpy() for k, v in d.items()}
+
+
+def same_hits(a, b):
+    ha, hb = a["patch"] >= 0, b["patch"] >= 0
+    assert np.array_equal(ha, hb)
+    diff = ha & (a["patch"] != b["patch"])
+    edge = lambda d: np.minimum.reduce([d["u"], 1 - d["u"], d["v"], 1 - d["v"]]) < 1e-5
+    assert (edge(a)[diff] & edge(b)[diff]).all(), int(diff.sum())
+    rel = np.abs(a["t"][ha] - b["t"][ha]) / a["t"][ha]
+    assert rel.max(initial=0) <= 1e-6
+
+
+def test_engine_settings_agree_at_full_size(setup):
+    rt, torch, g, rays = setup
+    base = rt.engine_config()
+    got = {}
+    try:
+        for cfg in ({"passes": 2, "backtrack_cache": 1}, {"passes": 1, "backtrack_cache": 0},
+                    {"passes": 8, "collect_threads": 128, "resolve_threads": 128, "backtrack_cache": 1},
+                    {"passes": 2, "backtrack_cache": 0}):
+            rt.set_engine_config(**cfg)
+            h = host(g.intersect(rays))
+            c = g.counters()
+            assert c["device_errors"] == 0
+            got[tuple(sorted(cfg.items()))] = (h, c)
+    finally:
+        rt.set_engine_config(**base)
+    runs = list(got.values())
+    for h, _ in runs[1:]:
+        same_hits(runs[0][0], h)
+    (h1, c1), (h0, c0) = got[(("backtrack_cache", 1), ("passes", 2))], got[(("backtrack_cache", 0), ("passes", 2))]
+    for k in h1:
+        assert np.array_equal(h1[k], h0[k]), k
+    assert c1["nodes"] == c0["nodes"] and c1["hash_lookups"] == c0["hash_lookups"]
+    assert c0["hash_table_reads"] == c0["hash_lookups"] and c1["hash_table_reads"] < c1["hash_lookups"] // 100
+    assert (runs[0][0]["patch"] >= 0).mean() > 0.2
+
+
+def test_closest_and_any_hit_agree_at_full_size(setup):
+    rt, torch, g, rays = setup
+    c = host(g.intersect(rays))
+    a = host(g.intersect(rays, any_hit=True))
+    assert np.array_equal(c["patch"] >= 0, a["patch"] >= 0)
+
+
+def test_polish_refines_in_place_at_full_size(setup):
+    rt, torch, g, rays = setup
+    f = host(g.intersect(rays, precision=rt.FP32))
+    p = host(g.intersect(rays, precision=rt.FP32_POLISH64))
+    assert np.array_equal(f["patch"], p["patch"]) and np.array_equal(f["object"], p["object"])
+    hit = f["patch"] >= 0
+    rel = np.abs(f["t"][hit] - p["t"][hit]) / p["t"][hit]
+    assert np.quantile(rel, 0.999) < 1e-5 and rel.max() < 1e-3
