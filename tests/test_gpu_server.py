@@ -161,3 +161,22 @@ def test_admission_and_argument_errors(rt, store, torch):
         assert sv.stats()["peak_slot_bytes"] <= 64 << 20
     finally:
         sv.close()
+
+
+def test_monte_carlo_same_alone_and_in_mix(rt, store, torch):
+    """Monte-Carlo renders through the server: a request's random numbers are
+    keyed by its own image sample and depth, so cutting it into row chunks and
+    batching it with others changes no bit."""
+    opts = rt.Options(recursion_depth=2, sampling=rt.MONTE_CARLO)
+    specs = [(1, 96, 54, 3, 2), (2, 80, 60, 2, 1), (0, 64, 48, 4, 2)]
+    c = cams()
+    alone = []
+    for g, w, h, s, d in specs:
+        req = rt.Request.alloc(g, c[g], w, h, spp=s, recursion_depth=d, linear=True)
+        run_server(rt, torch, store, [req], [], slots=1, options=opts)
+        alone.append(req)
+    mix = [rt.Request.alloc(g, c[g], w, h, spp=s, recursion_depth=d, linear=True) for g, w, h, s, d in specs]
+    infos, _, _ = run_server(rt, torch, store, mix, [], slots=2, max_batch_samples=2500, options=opts)
+    assert all(i["status"] == 0 for i in infos) and max(i["chunks"] for i in infos) > 1
+    for a, b in zip(alone, mix):
+        assert torch.equal(a.linear, b.linear) and torch.equal(a.framebuffer, b.framebuffer)
