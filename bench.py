@@ -393,6 +393,9 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
             else:
                 tickets.append(server.submit_render(r))
         infos = [server.wait(t) for t in tickets]
+        failed = [i["status"] for i in infos if i["status"] != 0]
+        if failed:
+            raise RuntimeError(f"serving: {len(failed)} of {len(infos)} requests failed (status {failed[0]})")
         lat = np.array([i["finish_s"] - i["submit_s"] for i in infos]) * 1e3
         span = max(i["finish_s"] for i in infos) - min(i["submit_s"] for i in infos)
         rays = server.stats()["rays_traced"] - r0
