@@ -116,10 +116,10 @@ uint64_t RenderSlot::bytes_for(uint32_t samples, uint32_t lights)
     uint64_t b = 0;
     b += 2 * 9 * c * 4;          // ray queues
     b += 6 * c * 4;              // sample, group, depth of both queues
-    b += 5 * c * 4;              // hits
+    b += 2 * 5 * c * 4;          // hits of even and odd levels
     b += 6 * c * 4;              // base, accum
     b += s * 4 * (1 + 7 + 2 + 3 + 1);  // occluded, shadow rays, slot+group, contrib, visible
-    b += engine_words(uint32_t(std::max<uint64_t>(c, s)), kEnginePasses) * 4;
+    b += 2 * engine_words(uint32_t(std::max<uint64_t>(c, s)), kEnginePasses) * 4;  // closest, shadow
     return b;
 }
 
@@ -128,6 +128,21 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
     const uint32_t nl = std::max<uint32_t>(lights, 1);
     CGS_TRY(req.reserve(std::max<uint32_t>(nreq, 1)));
     CGS_TRY(counters.reserve(1));
+    if (!side)
+    {
+        // the shadow queries run on a stream of their own beside the next
+        // level's closest query; without it everything runs on one stream
+        if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join, cudaEventDisableTiming) != cudaSuccess)
+        {
+            cudaGetLastError();
+            if (side) cudaStreamDestroy(side);
+            if (fork) cudaEventDestroy(fork);
+            side = nullptr; fork = nullptr; join = nullptr;
+        }
+        wb.side = side; wb.fork = fork; wb.join = join;
+    }
     if (wb.capacity >= samples && wb.lightCapacity >= nl && wb.engine) return CGS_OK;
     const size_t cap = std::max<uint32_t>(samples, wb.capacity);
     const uint32_t lc = std::max<uint32_t>(nl, wb.lightCapacity);
@@ -141,12 +156,19 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
     CGS_TRY(count.reserve(8));
     CGS_TRY(hitF.reserve(3 * cap));
     CGS_TRY(hitI.reserve(2 * cap));
+    CGS_TRY(hitF2.reserve(3 * cap));
+    CGS_TRY(hitI2.reserve(2 * cap));
     CGS_TRY(occluded.reserve(sc));
     const uint32_t ecap = uint32_t(std::max(cap, sc));
     if (engineCapacity < ecap)
     {
         CGS_TRY(engine.reserve(engine_words(ecap, kEnginePasses)));
         engineCapacity = ecap;
+    }
+    if (engine2Capacity < ecap)
+    {
+        CGS_TRY(engine2.reserve(engine_words(ecap, kEnginePasses)));
+        engine2Capacity = ecap;
     }
     CGS_TRY(shadow.reserve(7 * sc));
     CGS_TRY(shadowSlot.reserve(sc));
@@ -160,10 +182,13 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
     wb.group[0] = grp0.p; wb.group[1] = grp1.p;
     wb.depth[0] = dep0.p; wb.depth[1] = dep1.p;
     wb.count = count.p;
-    wb.hit = HitsSoA {hitF.p, hitF.p + cap, hitF.p + 2 * cap, hitI.p, hitI.p + cap};
+    wb.hit[0] = HitsSoA {hitF.p, hitF.p + cap, hitF.p + 2 * cap, hitI.p, hitI.p + cap};
+    wb.hit[1] = HitsSoA {hitF2.p, hitF2.p + cap, hitF2.p + 2 * cap, hitI2.p, hitI2.p + cap};
     wb.occluded = occluded.p;
     wb.engine = engine.p;
+    wb.engine2 = engine2.p;
     wb.engineCapacity = engineCapacity;
+    wb.engine2Capacity = engine2Capacity;
     wb.shadow = shadow.p; wb.shadowGroup = shadowGroup.p; wb.shadowSlot = shadowSlot.p;
     wb.contrib = contrib.p; wb.visible = visible.p; wb.base = base.p; wb.accum = accum.p;
     wb.capacity = uint32_t(cap);
@@ -186,6 +211,7 @@ uint64_t RenderSlot::bytes() const
     uint64_t b = ray0.bytes() + ray1.bytes() + shadow.bytes() + contrib.bytes() + base.bytes() + accum.bytes();
     b += hitF.bytes() + smp0.bytes() + smp1.bytes() + grp0.bytes() + grp1.bytes() + dep0.bytes() + dep1.bytes();
     b += count.bytes() + shadowSlot.bytes() + shadowGroup.bytes() + engine.bytes() + visible.bytes() + hitI.bytes();
+    b += hitF2.bytes() + hitI2.bytes() + engine2.bytes();
     b += occluded.bytes() + req.bytes() + counters.bytes() + batch.bytes();
     return b;
 }
@@ -193,12 +219,19 @@ uint64_t RenderSlot::bytes() const
 void RenderSlot::release()
 {
     ray0.release(); ray1.release(); shadow.release(); contrib.release(); base.release(); accum.release();
-    hitF.release();
-    for (auto* b : {&smp0, &smp1, &grp0, &grp1, &dep0, &dep1, &count, &shadowSlot, &shadowGroup, &engine}) b->release();
-    visible.release(); hitI.release(); occluded.release(); req.release(); counters.release(); batch.release();
+    hitF.release(); hitF2.release();
+    for (auto* b : {&smp0, &smp1, &grp0, &grp1, &dep0, &dep1, &count, &shadowSlot, &shadowGroup, &engine, &engine2})
+        b->release();
+    visible.release(); hitI.release(); hitI2.release(); occluded.release(); req.release(); counters.release();
+    batch.release();
     graphs.release();
+    if (side) { cudaStreamSynchronize(side); cudaStreamDestroy(side); }
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    side = nullptr; fork = nullptr; join = nullptr;
     wb = WavefrontBuffers {};
     engineCapacity = 0;
+    engine2Capacity = 0;
 }
 
 cudaError_t launch_wavefront_cached(const DevScene& S, RenderSlot& slot, const RenderBatch& b, cudaStream_t stream,
@@ -211,10 +244,11 @@ cudaError_t launch_wavefront_cached(const DevScene& S, RenderSlot& slot, const R
                                  engine_config_generation(),
                                  key_of(slot.batch.p),
                                  key_of(slot.counters.p), key_of(w.ray[0]), key_of(w.ray[1]), key_of(w.engine),
-                                 key_of(w.shadow), key_of(w.accum), key_of(w.hit.t), key_of(w.occluded),
+                                 key_of(w.shadow), key_of(w.accum), key_of(w.hit[0].t), key_of(w.occluded),
                                  key_of(w.contrib), key_of(w.visible), key_of(w.base), key_of(w.count),
                                  key_of(w.sample[0]), key_of(w.group[0]), key_of(w.depth[0]), w.capacity,
-                                 w.lightCapacity, w.engineCapacity});
+                                 w.lightCapacity, w.engineCapacity, key_of(w.hit[1].t), key_of(w.engine2),
+                                 w.engine2Capacity, key_of(w.side)});
     RenderSlot* sp = &slot;
     return run_cached(slot.graphs, key, stream, launches, [&](cudaStream_t st, int* nl) {
         return launch_render_wavefront(S, b, sp->batch.p, sp->wb, sp->counters.p, st, nl);

@@ -461,25 +461,42 @@ cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, con
     const float* sh = wb.shadow;
     const RaysSoA shadowRays {sh, sh + scap, sh + 2ull * scap, sh + 3ull * scap, sh + 4ull * scap, sh + 5ull * scap,
                               sh + 6ull * scap, wb.shadowGroup};
+    // Level L's shadow query, visibility and resolve run on the side stream
+    // beside level L+1's closest-hit query (they share no buffer: hits and
+    // engine scratch alternate, and the queue counts are reset only after the
+    // join); level L+1's shading waits for them, so every sample accumulates
+    // in the same order as on one stream.
+    const bool two = wb.side != nullptr;
+    cudaStream_t side = two ? wb.side : stream;
     for (int level = 0, cur = 0; level <= b.maxDepth; level++, cur ^= 1)
     {
-        cudaMemsetAsync(wb.count + (cur ^ 1), 0, sizeof(uint32_t), stream);
-        cudaMemsetAsync(wb.count + 2, 0, sizeof(uint32_t), stream);
-        cudaError_t e = run_query(S, q[cur].rays(), 0, wb.count + cur, b.q, false, wb.hit, nullptr, wb.engine,
+        const HitsSoA hit = wb.hit[level & 1];
+        cudaError_t e = run_query(S, q[cur].rays(), 0, wb.count + cur, b.q, false, hit, nullptr, wb.engine,
                                   wb.engineCapacity, kEnginePasses, counters, stream, &nl);
         if (e != cudaSuccess) return e;
+        if (two && level > 0) cudaStreamWaitEvent(stream, wb.join, 0);
+        cudaMemsetAsync(wb.count + (cur ^ 1), 0, sizeof(uint32_t), stream);
+        cudaMemsetAsync(wb.count + 2, 0, sizeof(uint32_t), stream);
         k_wf_shade<<<gShade, kWfThreads, 0, stream>>>(S, bDev, b.eps, b.sampling, q[cur], q[cur ^ 1], wb.count + cur,
-                                                      wb.count + (cur ^ 1), wb.count + 2, wb.hit, wb.shadow,
+                                                      wb.count + (cur ^ 1), wb.count + 2, hit, wb.shadow,
                                                       wb.shadowGroup, wb.shadowSlot, scap, lcap, wb.contrib,
                                                       wb.visible, wb.base, wb.accum);
-        e = run_query(S, shadowRays, 0, wb.count + 2, qa, true, HitsSoA {}, wb.occluded, wb.engine, wb.engineCapacity,
-                      kEnginePasses, counters, stream, &nl);
+        if (two)
+        {
+            cudaEventRecord(wb.fork, stream);
+            cudaStreamWaitEvent(side, wb.fork, 0);
+        }
+        e = run_query(S, shadowRays, 0, wb.count + 2, qa, true, HitsSoA {}, wb.occluded,
+                      two ? wb.engine2 : wb.engine, two ? wb.engine2Capacity : wb.engineCapacity, kEnginePasses,
+                      counters, side, &nl);
         if (e != cudaSuccess) return e;
-        k_wf_visibility<<<gFlat, 256, 0, stream>>>(wb.occluded, wb.shadowSlot, wb.count + 2, scap, wb.visible);
-        k_wf_resolve<<<gFlat, 256, 0, stream>>>(S, q[cur], wb.count + cur, wb.hit, wb.contrib, wb.visible, wb.base,
-                                               lcap, wb.accum);
+        k_wf_visibility<<<gFlat, 256, 0, side>>>(wb.occluded, wb.shadowSlot, wb.count + 2, scap, wb.visible);
+        k_wf_resolve<<<gFlat, 256, 0, side>>>(S, q[cur], wb.count + cur, hit, wb.contrib, wb.visible, wb.base, lcap,
+                                            wb.accum);
         nl += 3;
+        if (two) cudaEventRecord(wb.join, side);
     }
+    if (two) cudaStreamWaitEvent(stream, wb.join, 0);
     k_wf_finish<<<gFlat, 256, 0, stream>>>(bDev, wb.accum);
     nl++;
     if (launches) *launches += nl;

@@ -132,10 +132,13 @@ struct WavefrontBuffers
     uint32_t* group[2];
     uint32_t* depth[2];   // bounces still allowed
     uint32_t* count;      // [0..1] queue sizes, [2] shadow count
-    HitsSoA hit;          // per ray of the current queue
+    HitsSoA hit[2];       // per ray of the queue of an even / odd bounce level
     int32_t* occluded;    // per shadow ray
-    uint32_t* engine;     // query-engine scratch
-    uint32_t engineCapacity;
+    uint32_t* engine;     // query-engine scratch of the closest-hit queries
+    uint32_t* engine2;    // ... of the shadow queries, which run beside the next level's closest query
+    uint32_t engineCapacity, engine2Capacity;
+    cudaStream_t side;    // the shadow queries' stream (null: one stream for everything)
+    cudaEvent_t fork, join;
     float* shadow;        // 7 floats per shadow ray SoA: ox oy oz dx dy dz max
     uint32_t* shadowGroup;
     uint32_t* shadowSlot; // (ray index * lightCapacity + light) of each shadow ray

@@ -144,12 +144,14 @@ struct RenderSlot
     WavefrontBuffers wb {};
     DBuf<RenderBatch> batch;  // device copy of the batch description
     GraphCache graphs;
-    DBuf<float> ray0, ray1, shadow, contrib, base, accum, hitF;
-    DBuf<uint32_t> smp0, smp1, grp0, grp1, dep0, dep1, count, shadowSlot, shadowGroup, engine;
-    DBuf<int32_t> visible, hitI, occluded;
+    DBuf<float> ray0, ray1, shadow, contrib, base, accum, hitF, hitF2;
+    DBuf<uint32_t> smp0, smp1, grp0, grp1, dep0, dep1, count, shadowSlot, shadowGroup, engine, engine2;
+    DBuf<int32_t> visible, hitI, hitI2, occluded;
+    cudaStream_t side = nullptr;  // the shadow queries' stream, forked from and joined to the render's
+    cudaEvent_t fork = nullptr, join = nullptr;
     DBuf<DevRequest> req;
     DBuf<Counters> counters;
-    uint32_t engineCapacity = 0;
+    uint32_t engineCapacity = 0, engine2Capacity = 0;
     int ensure(uint32_t samples, uint32_t lights, uint32_t nreq);
     int ensure_engine(uint32_t rays);  // query-engine scratch for `rays` rays
     void release();
