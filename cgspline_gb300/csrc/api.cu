@@ -119,7 +119,8 @@ uint64_t RenderSlot::bytes_for(uint32_t samples, uint32_t lights)
     b += 2 * 5 * c * 4;          // hits of even and odd levels
     b += 6 * c * 4;              // base, accum
     b += s * 4 * (1 + 7 + 2 + 3 + 1);  // occluded, shadow rays, slot+group, contrib, visible
-    b += 2 * engine_words(uint32_t(std::max<uint64_t>(c, s)), kEnginePasses) * 4;  // closest, shadow
+    // engine scratch: the closest-hit queries' (samples) and the shadow queries' (samples x lights)
+    b += (engine_words(uint32_t(c), kEnginePasses) + engine_words(uint32_t(s), kEnginePasses)) * 4;
     return b;
 }
 
@@ -159,16 +160,18 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
     CGS_TRY(hitF2.reserve(3 * cap));
     CGS_TRY(hitI2.reserve(2 * cap));
     CGS_TRY(occluded.reserve(sc));
-    const uint32_t ecap = uint32_t(std::max(cap, sc));
+    // the closest-hit queries hold `cap` rays, the shadow queries `sc`; with no
+    // side stream both run on the first scratch
+    const uint32_t ecap = uint32_t(side ? cap : std::max(cap, sc)), ecap2 = uint32_t(side ? sc : 0);
     if (engineCapacity < ecap)
     {
         CGS_TRY(engine.reserve(engine_words(ecap, kEnginePasses)));
         engineCapacity = ecap;
     }
-    if (engine2Capacity < ecap)
+    if (ecap2 && engine2Capacity < ecap2)
     {
-        CGS_TRY(engine2.reserve(engine_words(ecap, kEnginePasses)));
-        engine2Capacity = ecap;
+        CGS_TRY(engine2.reserve(engine_words(ecap2, kEnginePasses)));
+        engine2Capacity = ecap2;
     }
     CGS_TRY(shadow.reserve(7 * sc));
     CGS_TRY(shadowSlot.reserve(sc));
