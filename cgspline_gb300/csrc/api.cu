@@ -584,8 +584,11 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
     for (int passes : {1, 2, 4})
         for (int ct : {128, 256})
             for (int rt : {64, 128})
+                for (int full : {1, 0})
             {
-                const EngineConfig c {passes, ct, rt, 0, 0, saved.backtrackCache};
+                // traversal blocks: as many as fit, or three quarters of that (768
+                // threads per SM), which leaves room for the overlapping queries
+                const EngineConfig c {passes, ct, rt, full ? 0 : (ct == 256 ? 3 : 6), 0, saved.backtrackCache};
                 set_engine_config(c);
                 std::vector<float> ms;
                 for (int k = 0; k < repeats + 2 && status == CGS_OK; k++)

@@ -319,7 +319,8 @@ int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
 
 /* The autotuner: renders the batch (wavefront schedule) under each candidate
- * setting (passes 1, 2, 4 x collect 128, 256 x resolve 64, 128 threads), times
+ * setting (passes 1, 2, 4 x collect 128, 256 x resolve 64, 128 threads x
+ * traversal blocks per SM: as many as fit, or 768 threads' worth), times
  * `repeats` graph replays of each with CUDA events, and keeps the fastest
  * (median) as the process-wide setting.  Synchronises `stream`. */
 int cgs_autotune_render(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,
