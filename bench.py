@@ -323,6 +323,7 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
     out["speedup_vs_plain_split_longest"] = out["batched_split_longest"]["value"] / out["plain"]["value"]
     out["speedup_vs_plain_split_longest_graze64"] = \
         out["batched_split_longest_graze64"]["value"] / out["plain"]["value"]
+    out["engine_settings"] = rt.engine_config()
     return out
 
 
@@ -423,6 +424,7 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
         sv.close()
     for s in stores.values():
         s.close()
+    out["engine_settings"] = rt.engine_config()
     return out
 
 
@@ -479,6 +481,7 @@ def main():
         if frame.stride == W:
             cfg, tms = rt.autotune(g, [req], rt.Options(recursion_depth=DEPTH, precision=prec), repeats=3)
             tuned = {"settings": cfg, "ms": tms}
+    frame_settings = rt.engine_config()
     # a scene refuses a new render while its previous one is in flight
     # (src/rt/RayTracer.cu:110-116), so frames are issued one at a time and
     # each is timed on the device
@@ -587,6 +590,10 @@ def main():
         g2.close()
         if not args.no_precision:
             extra["precision"] = precision_leg(rt, scenes, torch, dev, g, scene, flush)
+        # the traversal occupancy cap leaves room for the wavefront's overlapping
+        # shadow query; the batched and served queries have no such overlap and
+        # run the traversal at full occupancy
+        rt.set_engine_config(collect_occupancy=0)
         if not args.no_batching:
             extra["batching"] = batching_leg(rt, scenes, torch, dev, stream, prec, flush)
         if not args.no_serving:
@@ -607,7 +614,7 @@ def main():
                            "primary_rays": W * H, "l2": "flushed (2x L2 written) before every frame",
                            "parallelism": f"replicas x{world}"},
                 "e2e": e2e, "gpu_launches": counters["kernel_launches"] * args.steps, "clocks": clk.summary(),
-                "engine_settings": rt.engine_config(), "autotune": tuned}
+                "engine_settings": frame_settings, "autotune": tuned}
         line.update(extra)
         print(json.dumps(line), flush=True)
     if dist:
