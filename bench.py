@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson stream) comparison")
     ap.add_argument("--no-precision", action="store_true", help="skip the grazing-ray precision comparison")
     ap.add_argument("--no-tune", action="store_true", help="keep the default engine settings (no autotuner)")
+    ap.add_argument("--engine", default=None,
+                    help="fixed engine settings for the frame instead of the autotuner's pick, e.g. "
+                         "passes=2,collect_threads=256,resolve_threads=128,collect_occupancy=3 (profiling runs)")
     ap.add_argument("--scene", default="c2",
                     help="frame scene: c2 (the torus, default) or c4:<i> / c5:<i>, the seeded union scene i of "
                          "the batching / serving workloads with its camera (profiling cases)")
@@ -476,7 +479,9 @@ def main():
 
     # the autotuner picks the engine settings on this frame (outside the timed region)
     tuned = None
-    if not args.no_tune:
+    if args.engine:
+        rt.set_engine_config(**{k.strip(): int(v) for k, v in (kv.split("=") for kv in args.engine.split(","))})
+    elif not args.no_tune:
         req = rt.Request(0, cam, W, H, 1, DEPTH, frame.data, None)
         if frame.stride == W:
             cfg, tms = rt.autotune(g, [req], rt.Options(recursion_depth=DEPTH, precision=prec), repeats=3)
