@@ -319,6 +319,10 @@ void cgs_server::run()
             }
             lk.unlock();
             const cudaError_t e = launch(s);
+            // a batch that failed part-way may have work on the stream: let it
+            // drain before its requests are reported finished, so that callers
+            // may free their buffers
+            if (e != cudaSuccess) cudaStreamSynchronize(s.stream);
             lk.lock();
             uint64_t held = 0;
             for (const Slot& x : slots) held += x.bytes();

@@ -416,7 +416,9 @@ typedef struct cgs_server_stats {
 } cgs_server_stats;
 
 int cgs_server_create(cgs_server** server, cgs_scene* scene, const cgs_server_options* options);
-/* Finishes every submitted request, then frees the server. */
+/* Finishes every submitted request, then frees the server.  No other thread
+ * may be inside, or call, a cgs_server_* function of this server meanwhile or
+ * afterwards. */
 int cgs_server_destroy(cgs_server* server);
 /* Queue a request; *ticket identifies it.  CGS_ERR_ADMISSION when one row
  * (render) or one ray (query) cannot fit a slot's memory share, or when the
@@ -425,7 +427,8 @@ int cgs_server_submit_render(cgs_server* server, const cgs_render_request* reque
 int cgs_server_submit_query(cgs_server* server, const cgs_query_request* request, uint64_t* ticket);
 /* Wait up to timeout_s seconds (< 0: without limit) for a request.  CGS_OK
  * with its info once it has finished (the ticket is then released),
- * CGS_ERR_BUSY on timeout, CGS_ERR_NOT_FOUND for an unknown ticket. */
+ * CGS_ERR_BUSY on timeout, CGS_ERR_NOT_FOUND for an unknown ticket.  The
+ * server keeps a finished request's info until its ticket is waited on. */
 int cgs_server_wait(cgs_server* server, uint64_t ticket, double timeout_s, cgs_request_info* info);
 /* Seconds since the server was created (the clock of cgs_request_info). */
 double cgs_server_clock(const cgs_server* server);
