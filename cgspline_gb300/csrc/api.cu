@@ -317,6 +317,29 @@ int run_batch(cgs_scene* sc, RenderSlot& slot, const std::vector<DevRequest>& ho
     return cuda_status(e);
 }
 
+// A scene's queries share its counters and engine scratch.  A query on a
+// stream other than the previous query's is ordered after that query's work;
+// a stream under capture is left to the captured graph's own order.
+int query_begin(cgs_scene* s, cudaStream_t st, bool& captured)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CGS_TRY(cudaStreamIsCapturing(st, &cs));
+    captured = cs != cudaStreamCaptureStatusNone;
+    if (!captured && s->queryIssued && st != s->queryStream) CGS_TRY(cudaStreamWaitEvent(st, s->queryDone, 0));
+    return CGS_OK;
+}
+
+void query_end(cgs_scene* s, cudaStream_t st, bool captured)
+{
+    s->lastStream = st;
+    s->lastCounters = s->counters.p;
+    if (!captured && cudaEventRecord(s->queryDone, st) == cudaSuccess)
+    {
+        s->queryStream = st;
+        s->queryIssued = true;
+    }
+}
+
 }  // namespace cgs
 
 extern "C" {
@@ -334,6 +357,8 @@ int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, in
     if (n == 0) return CGS_OK;
     CGS_TRY(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
+    bool captured = false;
+    if (int er = query_begin(s, st, captured)) return er;
     CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
     RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, rays->group};
     Query q {method, precision, tol};
@@ -345,8 +370,7 @@ int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, in
     cudaError_t e = run_query(s->dev(), r, n, nullptr, q, any_hit != 0,
                               HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, hits->patch,
                               s->engine.p, s->engineCapacity, kEnginePasses, s->counters.p, st, &s->launches);
-    s->lastStream = st;
-    s->lastCounters = s->counters.p;
+    query_end(s, st, captured);
     return cuda_status(e);
 }
 
@@ -360,6 +384,8 @@ int cgs_traverse(cgs_scene* s, const cgs_rays* rays, uint32_t n, int any_hit, ui
     if (n == 0) return CGS_OK;
     CGS_TRY(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
+    bool captured = false;
+    if (int er = query_begin(s, st, captured)) return er;
     CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
     RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, rays->group};
     s->launches = 0;
@@ -369,8 +395,7 @@ int cgs_traverse(cgs_scene* s, const cgs_rays* rays, uint32_t n, int any_hit, ui
     }
     cudaError_t e = run_traverse(s->dev(), r, n, any_hit != 0, s->engine.p, s->engineCapacity, s->counters.p, st,
                                  list_lengths, &s->launches);
-    s->lastStream = st;
-    s->lastCounters = s->counters.p;
+    query_end(s, st, captured);
     return cuda_status(e);
 }
 
@@ -379,6 +404,7 @@ int cgs_intersect_host(cgs_scene* s, const cgs_rays* rays, uint32_t n, int metho
 {
     if (!s || !rays || !hits) return CGS_ERR_INVALID_ARGUMENT;
     if (n == 0) return CGS_OK;
+    std::lock_guard<std::mutex> hg(s->hostMu);  // the staging buffers are in use until the call returns
     cudaStream_t st = (cudaStream_t)stream;
     cgs_rays dr {};
     cgs_hits dh {};
@@ -429,15 +455,17 @@ int cgs_patch_intersect(cgs_scene* s, uint32_t surface, const cgs_rays* rays, co
     if (surface >= s->surfaces.size()) return CGS_ERR_INVALID_ARGUMENT;
     CGS_TRY(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
+    bool captured = false;
+    if (int er = query_begin(s, st, captured)) return er;
     CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
     RaysSoA r {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, nullptr};
     Query q {method, 0, tol};
     s->launches = 1;
-    s->lastStream = st;
-    s->lastCounters = s->counters.p;
-    return cuda_status(launch_patch_pairs(s->dev(), surface, s->surfaces[surface].patchCount(), r, pids, n, q,
-                                          HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object}, s->counters.p,
-                                          st));
+    const cudaError_t e = launch_patch_pairs(s->dev(), surface, s->surfaces[surface].patchCount(), r, pids, n, q,
+                                             HitsSoA {hits->t, hits->u, hits->v, hits->patch, hits->object},
+                                             s->counters.p, st);
+    query_end(s, st, captured);
+    return cuda_status(e);
 }
 
 int cgs_patch_normal(cgs_scene* s, uint32_t surface, const uint32_t* pids, const float* u, const float* v, uint32_t n,
@@ -450,12 +478,14 @@ int cgs_patch_normal(cgs_scene* s, uint32_t surface, const uint32_t* pids, const
     if (n == 0) return CGS_OK;
     CGS_TRY(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
+    bool captured = false;
+    if (int er = query_begin(s, st, captured)) return er;
     CGS_TRY(cudaMemsetAsync(s->counters.p, 0, sizeof(Counters), st));
     s->launches = 1;
-    s->lastStream = st;
-    s->lastCounters = s->counters.p;
-    return cuda_status(launch_patch_normals(s->dev(), surface, s->surfaces[surface].patchCount(), pids, u, v, n,
-                                            normals, s->counters.p, st));
+    const cudaError_t e = launch_patch_normals(s->dev(), surface, s->surfaces[surface].patchCount(), pids, u, v, n,
+                                               normals, s->counters.p, st);
+    query_end(s, st, captured);
+    return cuda_status(e);
 }
 
 // RayTracer::render (src/rt/RayTracer.cu:107-180) for a batch of requests;
@@ -517,6 +547,7 @@ int cgs_render_host(cgs_scene* s, const cgs_camera* cam, uint32_t w, uint32_t h,
                     uint32_t* fb, float* linear, void* stream)
 {
     if (!s || (!fb && !linear) || w == 0 || h == 0) return CGS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> hg(s->hostMu);  // the staging buffers are in use until the call returns
     cudaStream_t st = (cudaStream_t)stream;
     {
         std::lock_guard<std::mutex> g(s->mu);

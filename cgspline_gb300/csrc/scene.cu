@@ -377,6 +377,7 @@ cgs_scene::~cgs_scene()
     scratch64.release(); counters.release(); hitI.release();
     slot.release();
     if (finished) cudaEventDestroy(finished);
+    if (queryDone) cudaEventDestroy(queryDone);
 }
 
 // =========================================================== C ABI ====
@@ -416,7 +417,12 @@ int cgs_scene_create(cgs_scene** out, int device)
     if (!s) return CGS_ERR_OUT_OF_MEMORY;
     s->device = device;
     s->groups.emplace_back();
-    if (cudaEventCreateWithFlags(&s->finished, cudaEventDisableTiming) != cudaSuccess) { delete s; return CGS_ERR_CUDA; }
+    if (cudaEventCreateWithFlags(&s->finished, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->queryDone, cudaEventDisableTiming) != cudaSuccess)
+    {
+        delete s;
+        return CGS_ERR_CUDA;
+    }
     *out = s;
     return CGS_OK;
 }

@@ -198,6 +198,12 @@ struct cgs_scene
     cgs::DBuf<uint32_t> fbStage;
     cgs::DBuf<float> linStage;
     cudaEvent_t finished = nullptr;
+    // queries share the counters and engine scratch: the last query's stream
+    // and an event after its work, so that a query on another stream waits
+    cudaEvent_t queryDone = nullptr;
+    cudaStream_t queryStream = nullptr;
+    bool queryIssued = false;
+    std::mutex hostMu;  // held through a host-staged call (cgs_intersect_host, cgs_render_host)
     cudaStream_t lastStream = nullptr;
     cgs::Counters* lastCounters = nullptr;
     int launches = 0;

@@ -10,6 +10,9 @@ fallback takes over.
   node and backtrack counts are equal with it on and off.
 - The polished hits stay within 1e-5 of the FP32 hits they refine (t), on the
   same patch.
+- Queries issued on two streams, which share the scene's engine scratch,
+  each return their own rays' hits; so do host-staged queries from two
+  threads.
 """
 import numpy as np
 import pytest
@@ -84,3 +87,48 @@ def test_polish_refines_in_place_at_full_size(setup):
     hit = f["patch"] >= 0
     rel = np.abs(f["t"][hit] - p["t"][hit]) / p["t"][hit]
     assert np.quantile(rel, 0.999) < 1e-5 and rel.max() < 1e-3
+
+
+def test_queries_on_two_streams_keep_their_own_hits(setup):
+    """A scene's queries share its engine scratch and counters: issued back to
+    back on two streams, the second waits for the first, and each returns the
+    hits of its own rays."""
+    rt, torch, g, rays = setup
+    a, b = rays[:, 0::2].contiguous(), rays[:, 1::2].contiguous()
+    ref_a, ref_b = host(g.intersect(a)), host(g.intersect(b))
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    torch.cuda.synchronize()
+    for _ in range(3):
+        ha = g.intersect(a, stream=s1)
+        hb = g.intersect(b, stream=s2)
+        torch.cuda.synchronize()
+        for ref, got in ((ref_a, host(ha)), (ref_b, host(hb))):
+            for k in ref:
+                assert np.array_equal(ref[k], got[k]), k
+    assert g.counters()["device_errors"] == 0
+
+
+def test_host_queries_from_two_threads_keep_their_own_hits(setup):
+    """cgs_intersect_host stages rays and hits in buffers of the scene: two
+    host threads querying one scene at once each get their own rays' hits."""
+    import threading
+    rt, torch, g, rays = setup
+    hr = rays.cpu().numpy()
+    parts = [np.ascontiguousarray(hr[:, 0::2]), np.ascontiguousarray(hr[:, 1::2][:, :500000])]
+    refs = [g.intersect(p) for p in parts]
+    got = [[], []]
+
+    def work(i):
+        for _ in range(3):
+            got[i].append(g.intersect(parts[i]))
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=120)
+    for i in range(2):
+        assert len(got[i]) == 3
+        for h in got[i]:
+            for k in refs[i]:
+                assert np.array_equal(refs[i][k], h[k]), k
