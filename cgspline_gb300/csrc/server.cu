@@ -138,6 +138,7 @@ int cgs_server::grow(Slot& s, int kind, uint32_t units, uint32_t nchunks)
     }
     // staging grows in powers of two up to the batch limit, so that a slot
     // settles on one capacity (and one captured graph per query kind)
+    if (units > maxQuery) return CGS_ERR_INVALID_ARGUMENT;  // batches are packed within maxQuery
     uint32_t cap = std::max(s.qcap, std::min(1024u, maxQuery));
     while (cap < units) cap = cap * 2 > maxQuery ? maxQuery : cap * 2;
     if (s.rs.bytes() - s.rs.engine.bytes() + query_bytes(cap) > share) s.rs.release();
