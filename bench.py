@@ -9,7 +9,7 @@ of every hit, on the reference's BVH topology (bit-exact build).
 
 value  = total rays (primary + bounce + shadow) / device time of K frames,
          scene resident in HBM, L2 flushed before every frame.
-e2e    = the same through cgs_render_host (host framebuffer, copies inside the
+e2e    = the same through cgs_render_host (pinned host framebuffer, copies inside the
          timed region).
 accuracy = max relative t error and hit/miss disagreement of the primary hits
          of a seeded 1% pixel subset against the pure-FP64 GPU search (itself
@@ -504,11 +504,14 @@ def main():
     rays_per_frame = counters["rays"]
     value = whole_job_mrays(rays_per_frame, args.steps, world, total_ms)
 
-    # e2e: the C-ABI host entry point (framebuffer copied to host inside the timed region)
+    # e2e: the C-ABI host entry point (framebuffer copied to pinned host memory
+    # inside the timed region)
+    host_fb = torch.empty((H, W), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    tracer.render_host(cam, g, W, H, linear=False, out=(host_fb, None))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        tracer.render_host(cam, g, W, H, linear=False)
+        tracer.render_host(cam, g, W, H, linear=False, out=(host_fb, None))
     e2e_s = time.perf_counter() - t0
     e2e = {"value": rays_per_frame * args.steps / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 44,
            "d2h_bytes_per_step": W * H * 4}

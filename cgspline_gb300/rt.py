@@ -382,10 +382,19 @@ class RayTracer:
                                   _ptr(frame.data), frame.stride, _ptr(frame.linear), _stream_handle(stream)),
               "cgs_render")
 
-    def render_host(self, camera, scene: GpuScene, width: int, height: int, linear: bool = True, stream=None):
-        """Render into host memory (copies inside); returns (packed (h,w) uint32, linear (h,w,3) or None)."""
-        fb = np.zeros((height, width), np.uint32)
-        lin = np.zeros((height, width, 3), np.float32) if linear else None
+    def render_host(self, camera, scene: GpuScene, width: int, height: int, linear: bool = True, stream=None,
+                    out=None):
+        """Render into host memory (copies inside); returns (packed (h,w) uint32, linear (h,w,3) or None).
+        out: (fb, lin) arrays to write into instead of new ones (e.g. views of pinned memory);
+        lin may be None."""
+        if out is not None:
+            fb, lin = out
+            assert fb.dtype == np.uint32 and fb.shape == (height, width) and fb.flags.c_contiguous
+            assert lin is None or (lin.dtype == np.float32 and lin.shape == (height, width, 3)
+                                   and lin.flags.c_contiguous)
+        else:
+            fb = np.zeros((height, width), np.uint32)
+            lin = np.zeros((height, width, 3), np.float32) if linear else None
         o = self.options.c()
         check(self.lib.cgs_render_host(scene.h, C.byref(camera_struct(camera)), width, height, C.byref(o),
                                        _np_ptr(fb), _np_ptr(lin),

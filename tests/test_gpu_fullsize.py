@@ -132,3 +132,16 @@ def test_host_queries_from_two_threads_keep_their_own_hits(setup):
         for h in got[i]:
             for k in refs[i]:
                 assert np.array_equal(refs[i][k], h[k]), k
+
+
+def test_render_host_into_caller_buffers(setup):
+    """cgs_render_host into caller-owned (pinned) host arrays gives the same
+    image as into fresh ones."""
+    rt, torch, g, rays = setup
+    tr = rt.RayTracer(rt.Options(recursion_depth=1))
+    fb0, lin0 = tr.render_host(S.camera_c2(), g, 640, 360)
+    fb = torch.empty((360, 640), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    lin = torch.empty((360, 640, 3), dtype=torch.float32, pin_memory=True).numpy()
+    fb1, lin1 = tr.render_host(S.camera_c2(), g, 640, 360, out=(fb, lin))
+    assert fb1 is fb and lin1 is lin
+    assert np.array_equal(fb0, fb) and np.array_equal(lin0, lin)
