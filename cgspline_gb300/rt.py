@@ -35,6 +35,13 @@ def _torch():
     return torch
 
 
+def _require(ok: bool, what: str):
+    """Argument check that stays in force under python -O: the library gets
+    raw pointers, so a wrong shape or type must stop here."""
+    if not ok:
+        raise ValueError(what)
+
+
 def _stream_handle(stream):
     if stream is None:
         torch = _torch()
@@ -78,7 +85,8 @@ class GpuScene:
             if g > 0:
                 gid = C.c_uint32()
                 check(self.lib.cgs_scene_add_group(self.h, C.byref(gid)), "cgs_scene_add_group")
-                assert gid.value == g
+                if gid.value != g:
+                    raise RuntimeError(f"cgs_scene_add_group gave group {gid.value}, expected {g}")
             self._add(sc)
         if build:
             self.build(stream)
@@ -192,7 +200,8 @@ class GpuScene:
         if isinstance(rays, np.ndarray):
             return self._intersect_host(rays, method, precision, tol, any_hit, stream, group)
         torch = _torch()
-        assert rays.is_cuda and rays.dtype == torch.float32 and rays.dim() == 2 and rays.shape[0] == 7
+        _require(rays.is_cuda and rays.dtype == torch.float32 and rays.dim() == 2 and rays.shape[0] == 7,
+                 "rays: a (7, n) float32 CUDA tensor")
         rays = rays.contiguous()
         n = rays.shape[1]
         if out is None:
@@ -203,7 +212,7 @@ class GpuScene:
         gp = None
         if group is not None:
             group = group.to(device=rays.device, dtype=torch.int32).contiguous()
-            assert group.numel() == n
+            _require(group.numel() == n, "group: one id per ray")
             gp = group.data_ptr()
         r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)], gp)
         h = _capi.Hits(fo[0].data_ptr(), fo[1].data_ptr(), fo[2].data_ptr(), io[0].data_ptr(), io[1].data_ptr())
@@ -217,7 +226,8 @@ class GpuScene:
         per-ray candidate-list lengths (int32 tensor; patches plus object
         markers, at most 64), or None with copy_lengths=False."""
         torch = _torch()
-        assert rays.is_cuda and rays.dtype == torch.float32 and rays.dim() == 2 and rays.shape[0] == 7
+        _require(rays.is_cuda and rays.dtype == torch.float32 and rays.dim() == 2 and rays.shape[0] == 7,
+                 "rays: a (7, n) float32 CUDA tensor")
         rays = rays.contiguous()
         n = rays.shape[1]
         if lengths is None and copy_lengths:
@@ -225,7 +235,7 @@ class GpuScene:
         gp = None
         if group is not None:
             group = group.to(device=rays.device, dtype=torch.int32).contiguous()
-            assert group.numel() == n
+            _require(group.numel() == n, "group: one id per ray")
             gp = group.data_ptr()
         r = _capi.Rays(*[rays[k].data_ptr() for k in range(7)], gp)
         check(self.lib.cgs_traverse(self.h, C.byref(r), n, int(any_hit), _ptr(lengths) if copy_lengths else None,
@@ -234,13 +244,14 @@ class GpuScene:
 
     def _intersect_host(self, rays, method, precision, tol, any_hit, stream, group=None):
         rays = np.ascontiguousarray(rays, np.float32)
+        _require(rays.ndim == 2 and rays.shape[0] == 7, "rays: a (7, n) float32 array")
         n = rays.shape[1]
         fo = np.zeros((3, n), np.float32)
         io = np.zeros((2, n), np.int32)
         gp = None
         if group is not None:
             group = np.ascontiguousarray(group, np.uint32)
-            assert group.size == n
+            _require(group.size == n, "group: one id per ray")
             gp = group.ctypes.data
         r = _capi.Rays(*[rays[k].ctypes.data for k in range(7)], gp)
         h = _capi.Hits(fo[0].ctypes.data, fo[1].ctypes.data, fo[2].ctypes.data, io[0].ctypes.data, io[1].ctypes.data)
@@ -389,9 +400,11 @@ class RayTracer:
         lin may be None."""
         if out is not None:
             fb, lin = out
-            assert fb.dtype == np.uint32 and fb.shape == (height, width) and fb.flags.c_contiguous
-            assert lin is None or (lin.dtype == np.float32 and lin.shape == (height, width, 3)
-                                   and lin.flags.c_contiguous)
+            _require(fb.dtype == np.uint32 and fb.shape == (height, width) and fb.flags.c_contiguous,
+                     "out[0]: a C-contiguous (height, width) uint32 array")
+            _require(lin is None or (lin.dtype == np.float32 and lin.shape == (height, width, 3)
+                                     and lin.flags.c_contiguous),
+                     "out[1]: None or a C-contiguous (height, width, 3) float32 array")
         else:
             fb = np.zeros((height, width), np.uint32)
             lin = np.zeros((height, width, 3), np.float32) if linear else None

@@ -56,3 +56,21 @@ def test_invalid_arguments_rejected_without_gpu(lib):
     assert lib.cgs_scene_destroy(None) == 1
     assert lib.cgs_bvh_build(None) == 1
     assert lib.cgs_render(None, None, 0, 0, None, None, 0, None, None) == 1
+
+
+def test_python_mirror_checks_arrays_before_the_library(lib):
+    """The Python mirror refuses wrongly shaped host arrays before it hands
+    their pointers to the library (checks that hold under python -O)."""
+    import numpy as np
+    from cgspline_gb300 import rt, scenes
+    tr = rt.RayTracer(rt.Options())
+    cam = scenes.camera_c1()
+    with pytest.raises(ValueError):
+        tr.render_host(cam, None, 4, 4, out=(np.zeros((3, 4), np.uint32), None))
+    with pytest.raises(ValueError):
+        tr.render_host(cam, None, 4, 4, out=(np.zeros((4, 4), np.int64), None))
+    with pytest.raises(ValueError):
+        tr.render_host(cam, None, 4, 4, out=(np.zeros((4, 4), np.uint32), np.zeros((4, 4), np.float32)))
+    with pytest.raises(ValueError):
+        rt.GpuScene._intersect_host(None, np.zeros((6, 5), np.float32), rt.CLIP, rt.FP32, rt.DEFAULT_TOL, False,
+                                    None)
