@@ -4,6 +4,11 @@ Loads ``oracle/_build/libcgs_oracle.so`` (the restatement in cgs_oracle.cpp)
 through ctypes.  Only tests/, __graft_entry__.smoke() and bench.py's
 cpu_baseline / reference arm may import this package; the product in
 cgspline_gb300/ never does.
+
+Parity unpinned: the reference program cannot be compiled without its
+un-vendored Ds submodule and holds no golden vectors, so the restatement is
+pinned by analytic known-answer patches, the reference's BVH and hash
+invariants and the agreement of its FP32 variants with its FP64 search.
 """
 from __future__ import annotations
 
