@@ -659,6 +659,8 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
 int cgs_render_running(cgs_scene* s)
 {
     if (!s) return 0;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (cudaSetDevice(s->device) != cudaSuccess) return 0;
     return cudaEventQuery(s->finished) == cudaErrorNotReady ? 1 : 0;
 }
 
