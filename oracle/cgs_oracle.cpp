@@ -313,9 +313,45 @@ template<class R, class F> inline bool approximateIntersection(F& onHit, const V
     return found;
 }
 
+// The x-axis range of the true convex hull of the bound points (x_i, ybot_i)
+// and (x_i, ytop_i): the lower chain of the bottoms and the upper chain of the
+// tops, each a monotone-chain hull (Andrew's algorithm), closed by the sides
+// at x = 0 and x = 1.  Not in the reference: its scan (clip_range below) walks
+// the points once and never revisits an accepted edge, so on some nets its
+// polygon leaves out part of the hull and the clip drops a root.
+template<class R> inline void hull_range_exact(const R* ybot, const R* ytop, R& lower, R& upper)
+{
+    const R xs[4] {R(0), R(1) / R(3), R(2) / R(3), R(1)};
+    V2<R> lo[4], up[4];
+    int nl = 0, nu = 0;
+    for (int i = 0; i < 4; i++)
+    {
+        const V2<R> q {xs[i], ybot[i]};
+        while (nl >= 2 && isCCW(lo[nl - 1] - lo[nl - 2], q - lo[nl - 2]) <= 0) nl--;
+        lo[nl++] = q;
+    }
+    for (int i = 3; i >= 0; i--)
+    {
+        const V2<R> q {xs[i], ytop[i]};
+        while (nu >= 2 && isCCW(up[nu - 1] - up[nu - 2], q - up[nu - 2]) <= 0) nu--;
+        up[nu++] = q;
+    }
+    lower = R(1); upper = R(0);
+    auto edge = [&](V2<R> A, V2<R> B) {
+        V2<R> s;
+        if (xAxisIntersection(s, A, B)) { lower = std::fmin(lower, s.x); upper = std::fmax(upper, s.y); }
+    };
+    for (int k = 0; k + 1 < nl; k++) edge(lo[k], lo[k + 1]);
+    edge(lo[nl - 1], up[0]);
+    for (int k = 0; k + 1 < nu; k++) edge(up[k], up[k + 1]);
+    edge(up[nu - 1], lo[0]);
+}
+
 // Fat-line clip of one sub-net: returns (lower, upper) after the anti-sliver
 // shrink.  src/Spline_BezierClipping.cu:250-353 (host) / :610-701 (device).
-template<class R> inline void clip_range(const V2<R>* p, int cutside, R& lower, R& upper)
+// kExact: the true hull's range (hull_range_exact) in place of the
+// reference's scan.
+template<class R, bool kExact = false> inline void clip_range(const V2<R>* p, int cutside, R& lower, R& upper)
 {
     const R over3[] {R(0), R(1) / R(3), R(2) / R(3), R(1)};
     lower = R(1); upper = R(0);
@@ -340,6 +376,13 @@ template<class R> inline void clip_range(const V2<R>* p, int cutside, R& lower, 
             }
         }
     }
+    if constexpr (kExact)
+    {
+        hull_range_exact(ybot, ytop, lower, upper);
+        lower = lower * R(0x0FFp-8);
+        upper = upper + (R(1) - upper) * R(0x001p-8);
+        return;
+    }
     const V2<R> hull[] {{over3[2], ybot[2]}, {over3[3], ybot[3]}, {over3[3], ytop[3]}, {over3[2], ytop[2]},
                         {over3[1], ytop[1]}, {over3[0], ytop[0]}, {over3[0], ybot[0]}};
     V2<R> P1 {over3[0], ybot[0]}, P2 {over3[1], ybot[1]};
@@ -363,7 +406,7 @@ struct ClipStats { uint64_t iterations = 0, pushes = 0, maxDepth = 0, overflow =
 
 // doBezierClipping2D_host, src/Spline_BezierClipping.cu:174-445 (the CPU
 // path of the reference: full sub-nets on an unbounded stack).
-template<class R, class F> bool clip2d_host(F& onHit, const V2<R>* patch, R tol, ClipStats* st)
+template<class R, class F, bool kExact = false> bool clip2d_host(F& onHit, const V2<R>* patch, R tol, ClipStats* st)
 {
     struct State { V2<R> patch[16]; V2<R> min, max, size; int cutside; };
     bool found = false;
@@ -389,7 +432,7 @@ template<class R, class F> bool clip2d_host(F& onHit, const V2<R>* patch, R tol,
             continue;
         }
         R lower, upper;
-        clip_range(p, e.cutside, lower, upper);
+        clip_range<R, kExact>(p, e.cutside, lower, upper);
         R delta = upper - lower;
         if (delta < 0)
             S.pop_back();
@@ -621,7 +664,10 @@ struct PatchHit { float t; float u, v; };
 // near-grazing candidate (the ray within asin(g_grazeSin) of the plane of
 // the patch's diagonals: 5 degrees for CGS_PREC_FP32_POLISH64, 30 for
 // CGS_PREC_FP32_GRAZE64) gets kClipDeviceB64P with tolerance 2^-20.
-enum Method { kClipHost = 0, kClipDevice = 1, kSubdiv = 2, kClipDeviceB64 = 3, kClipDeviceB64P = 4, kClipGraze = 5 };
+// kClipExactHull: the host clip with the true convex hull (hull_range_exact),
+// an oracle-only variant that shows the roots the reference's scan drops.
+enum Method { kClipHost = 0, kClipDevice = 1, kSubdiv = 2, kClipDeviceB64 = 3, kClipDeviceB64P = 4, kClipGraze = 5,
+              kClipExactHull = 6 };
 static float g_grazeSin = 0.5f;
 constexpr float kGrazeTol = 0x1p-20f;
 template<class R> inline bool grazing(const V4<R> P[16], V3<R> d)
@@ -674,6 +720,7 @@ bool intersect_patch(R& distance, V2<R>& uv, const Ray<R>& ray, const V4<R> P[16
     switch (method)
     {
     case kClipHost: return clip2d_host(onHit, net, tol, st);
+    case kClipExactHull: return clip2d_host<R, decltype(onHit), true>(onHit, net, tol, st);
     case kClipDevice: return clip2d_device(onHit, net, tol, st);
     case kClipDeviceB64:
     case kClipDeviceB64P: return clip2d_device<R, decltype(onHit), true>(onHit, net, tol, st);

@@ -275,3 +275,35 @@ def test_monte_carlo_render_restatement(oracle_mod):
     m = o.render_spp(S.camera_c2(), 48, 27, 4, depth=2)["rgb"]
     assert np.array_equal(a, b)
     assert abs(float(a.mean()) - float(m.mean())) < 0.05
+
+
+def test_exact_hull_recovers_roots_the_reference_scan_drops(oracle_mod):
+    """The reference finds the fat-line range from a one-pass scan of the
+    bound points (src/Spline_BezierClipping.cu:310-348 host, :655-693
+    device).  On some nets its polygon leaves out part of the true convex
+    hull, and the clip drops a root: the ray reports a farther surface.  On the
+    32x32 torus, every ray where subdivision finds a closer hit than the clip
+    gets it back from the exact-hull variant, whose hits lie on the surface;
+    the exact hull loses no hit the scan finds.  The GPU path keeps the
+    reference's scan, so it shares these misses with the oracle."""
+    sc, cam = S.scene_c2(nu=32, nv=32), S.camera_c2()
+    o = oracle_mod.OracleScene(sc)
+    rays = oracle_mod.camera_rays(cam, 512, 512)
+    rc = o.intersect(rays)
+    rx = o.intersect(rays, method=oracle_mod.CLIP_EXACT_HULL)
+    rs = o.intersect(rays, method=oracle_mod.SUBDIV)
+
+    def closer(a, b):
+        return (a["patch"] >= 0) & ((b["patch"] < 0) | (a["t"] < b["t"] * (1 - 1e-4)))
+
+    dropped = closer(rs, rc)
+    assert 0 < dropped.sum() < 1e-3 * (rc["patch"] >= 0).sum()
+    assert not closer(rc, rx).any()
+    assert not closer(rs, rx).any()
+    assert closer(rx, rc)[dropped].all()
+    nets = sc.surfaces[0].patches().astype(np.float64)
+    for i in np.nonzero(dropped)[0]:
+        p = int(rx["patch"][i])
+        point = S.eval_patches(nets[p:p + 1], np.array([rx["u"][i]]), np.array([rx["v"][i]]))[0][0]
+        on_ray = rays[:3, i].astype(np.float64) + float(rx["t"][i]) * rays[3:6, i].astype(np.float64)
+        assert np.linalg.norm(point - on_ray) < 1e-4 * float(rx["t"][i])
