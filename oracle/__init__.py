@@ -30,7 +30,8 @@ CLIP_HOST, CLIP_DEVICE, SUBDIV = 0, 1, 2
 # tolerance 2^-20
 CLIP_GRAZE64 = 5
 # the host clip with the true convex hull of the fat-line bounds in place of
-# the reference's one-pass scan (oracle only: finds roots that scan drops)
+# the reference's one-pass scan (oracle only: finds roots that scan drops);
+# with precision FP64 the FP64 search clips with it too
 CLIP_EXACT_HULL = 6
 GRAZE_5, GRAZE_30 = 0.0871557427, 0.5
 FP32, FP32_POLISH64, FP64 = 0, 1, 2

@@ -1226,9 +1226,11 @@ inline bool scene_occluded(const Scene& sc, const Ray<float>& ray0, const QueryO
 
 // FP64 "true t": the same two-level traversal and search in double with a
 // tight tolerance, followed by a Newton polish.  The ray is the FP32 input
-// promoted; hit.t is the ray parameter of the polished root.
+// promoted; hit.t is the ray parameter of the polished root.  exactHull: the
+// search clips with the true convex hull (hull_range_exact) instead of the
+// reference's scan.
 inline int scene_intersect_f64(const Scene& sc, double& t_out, double& u_out, double& v_out, uint32_t& patch_out,
-                               const Ray<float>& rayf, double tol)
+                               const Ray<float>& rayf, double tol, bool exactHull = false)
 {
     Ray<double> ray0 {cast3<double>(rayf.o), cast3<double>(rayf.d), double(rayf.max)};
     int nearest = -1;
@@ -1273,7 +1275,8 @@ inline int scene_intersect_f64(const Scene& sc, double& t_out, double& u_out, do
                 V3<double> Q = xyz(P[k]);
                 net[k] = {dot(axis0, Q - lr.o), dot(axis1, Q - lr.o)};
             }
-            clip2d_host(onHit, net, tol, nullptr);
+            if (exactHull) clip2d_host<double, decltype(onHit), true>(onHit, net, tol, nullptr);
+            else clip2d_host(onHit, net, tol, nullptr);
             (void)dist; (void)uv;
             if (any) { lt = best; lpatch = p; lu = bu; lv = bv; }
             return any;
@@ -1678,7 +1681,7 @@ int ora_intersect(void* s_, const float* rays, uint64_t n, int method, int preci
         if (precision == 2)
         {
             double t = 0, u = 0, v = 0; uint32_t p = 0;
-            int ob = scene_intersect_f64(*s, t, u, v, p, r, tol64);
+            int ob = scene_intersect_f64(*s, t, u, v, p, r, tol64, method == kClipExactHull);
             out_f[i] = ob >= 0 ? float(t) : INFINITY;
             out_f[n + i] = float(u); out_f[2 * n + i] = float(v);
             out_i[i] = ob >= 0 ? int32_t(p) : -1; out_i[n + i] = ob;

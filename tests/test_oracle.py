@@ -301,6 +301,11 @@ def test_exact_hull_recovers_roots_the_reference_scan_drops(oracle_mod):
     assert not closer(rc, rx).any()
     assert not closer(rs, rx).any()
     assert closer(rx, rc)[dropped].all()
+    # the FP64 search with either hull: the exact one finds every hit the
+    # scan finds, and more
+    x64 = o.intersect(rays, method=oracle_mod.CLIP_EXACT_HULL, precision=oracle_mod.FP64)
+    r64 = o.intersect(rays, precision=oracle_mod.FP64)
+    assert not closer(r64, x64).any() and closer(x64, r64).any()
     nets = sc.surfaces[0].patches().astype(np.float64)
     for i in np.nonzero(dropped)[0]:
         p = int(rx["patch"][i])
