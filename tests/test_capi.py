@@ -74,3 +74,30 @@ def test_python_mirror_checks_arrays_before_the_library(lib):
     with pytest.raises(ValueError):
         rt.GpuScene._intersect_host(None, np.zeros((6, 5), np.float32), rt.CLIP, rt.FP32, rt.DEFAULT_TOL, False,
                                     None)
+
+
+def test_header_serves_a_c_caller(lib, tmp_path):
+    """include/cgspline.h compiles as pedantic C99, and a C program links
+    against the library and calls it (calls that need no GPU)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    from cgspline_gb300 import build
+    so = build.build()
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <string.h>\n#include "cgspline.h"\n'
+        "int main(void)\n{\n"
+        "    if (cgs_scene_destroy(NULL) != CGS_ERR_INVALID_ARGUMENT) return 1;\n"
+        "    if (strlen(cgs_status_string(CGS_OK)) == 0) return 2;\n"
+        '    printf("%s\\n", cgs_status_string(CGS_ERR_INVALID_ARGUMENT));\n'
+        "    return 0;\n}\n")
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(so)
+    name = os.path.basename(so)[3:-3]  # libNAME.so -> NAME
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-o", str(exe), "-L", libdir, "-l" + name, "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    assert out.strip()
