@@ -13,6 +13,7 @@
 // placed, the others add rank+1 to their displacement -- which makes the table
 // a pure function of the keys.  Each round is two kernel launches (bid,
 // commit); there is no device-wide barrier and no spin-wait.
+#include <atomic>
 #include <algorithm>
 
 #include "kernels.h"
@@ -228,15 +229,25 @@ uint32_t bit_floor_u32(uint32_t x)
     return x ? r : 0;
 }
 
+// SM count of the current device, cached per device ordinal.  The cache
+// entries are atomics: concurrent first calls from several host threads
+// store the same value.
+int device_sms()
+{
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    int sms = (dev >= 0 && dev < kMaxDev) ? cache[dev].load(std::memory_order_relaxed) : 0;
+    if (sms > 0) return sms;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    if (dev >= 0 && dev < kMaxDev) cache[dev].store(sms, std::memory_order_relaxed);
+    return sms;
+}
+
 int grid_for(uint64_t items, int threads)
 {
-    static int sms = 0;
-    if (!sms)
-    {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int sms = device_sms();
     uint64_t g = (items + threads - 1) / threads;
     uint64_t cap = uint64_t(sms) * 8;
     return int(std::max<uint64_t>(1, std::min(g, cap)));

@@ -2,10 +2,10 @@
 // perfect-hash build without any device allocation.
 //
 // cgs_perfect_hash_build takes its working memory from cudaMallocAsync.  Some
-// callers cannot allocate at the moment they need a hash table: code running
-// while a stream is being captured into a CUDA graph, code inside a
-// framework's allocator callback, or services that must not grow the device
-// heap after start-up.  This entry point runs the same kernels on a
+// callers cannot allocate at the moment they need a hash table: code inside a
+// framework's allocator callback (allocating there re-enters the allocator),
+// or services that reserve their device memory at start-up and must not grow
+// the device heap afterwards.  This entry point runs the same kernels on a
 // fixed-size scratch array that lives in the library itself, so the caller
 // supplies only the keys and the output buffers.
 //
@@ -18,15 +18,14 @@
 // on the GPU (on different streams, or from different host threads without
 // ordering) race on the array and must be serialised by the caller.
 //
-// The first call on a device (with that device current) looks the array's
-// device address up with cudaGetSymbolAddress and caches it; make that first
-// call before any stream capture begins.
-#include <mutex>
-#include <numeric>
-#include <random>
-
+// In host code the array's name is a host-side stand-in, not a device
+// address.  Each call looks the device address up with cudaGetSymbolAddress
+// for the current device and checks the result; the lookup is cheap once the
+// module is loaded, and it stays correct after cudaDeviceReset, which may
+// load the module at another address.
 #include "../../include/cgspline.h"
 #include "kernels.h"
+#include "scene_impl.h"
 
 namespace {
 
@@ -36,40 +35,6 @@ constexpr size_t kNoAllocWords64 = 458797 + (800784 + 1) / 2;
 
 static __device__ __align__(256) unsigned long long g_noallocScratch[kNoAllocWords64];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noallocMutex;
-void* g_noallocAddress[kMaxDevices] = {};
-
-// std::mt19937(42) with std::uniform_int_distribution<uint32_t>(0, n) and
-// gcd(n, A) == 1 retries: the 16 trials' coefficients (as the allocating
-// entry point draws them).
-void draw_coefficients(uint32_t n, uint32_t A[16], uint32_t B[16])
-{
-    std::mt19937 mt(42);
-    std::uniform_int_distribution<uint32_t> d(0, n);
-    for (int t = 0; t < 16; t++)
-    {
-        uint32_t a, b;
-        do
-        {
-            a = d(mt);
-            if (a == 0) a = 31;
-            b = d(mt);
-        } while (std::gcd(n, a) > 1);
-        A[t] = a;
-        B[t] = b;
-    }
-}
-
-uint32_t displacement_size(uint32_t n)
-{
-    int s = int(n - 1) >> 1;
-    if (s < 2) s = 2;
-    uint32_t r = 1;
-    while (r <= uint32_t(s) / 2) r <<= 1;
-    return r;
-}
-
 }  // namespace
 
 extern "C" int cgs_perfect_hash_build_noalloc(const uint32_t* keys, uint32_t n, uint32_t* disp,
@@ -78,31 +43,20 @@ extern "C" int cgs_perfect_hash_build_noalloc(const uint32_t* keys, uint32_t n, 
 {
     if (!keys || !disp || !table || !params || n == 0) return CGS_ERR_INVALID_ARGUMENT;
     if (n > kNoAllocMaxKeys) return CGS_ERR_CAPACITY;
-    const uint32_t step = std::max<uint32_t>(4u, uint32_t(0.05f * float(n)));
-    if (displ_capacity < displacement_size(n) || table_capacity < n + 15u * step) return CGS_ERR_INVALID_ARGUMENT;
+    if (displ_capacity < cgs::displ_size(n) || table_capacity < cgs::table_capacity(n))
+        return CGS_ERR_INVALID_ARGUMENT;
     size_t w32 = 0, w64 = 0;
     cgs::hash_scratch_words(n, w32, w64);
     if (w64 + (w32 + 1) / 2 > kNoAllocWords64) return CGS_ERR_CAPACITY;
 
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CGS_ERR_CUDA;
     void* base = nullptr;
-    {
-        std::lock_guard<std::mutex> g(g_noallocMutex);
-        if (!g_noallocAddress[dev])
-        {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noallocScratch) != cudaSuccess || !p) return CGS_ERR_CUDA;
-            g_noallocAddress[dev] = p;
-        }
-        base = g_noallocAddress[dev];
-    }
+    if (cudaGetSymbolAddress(&base, g_noallocScratch) != cudaSuccess || !base) return CGS_ERR_CUDA;
     unsigned long long* base64 = static_cast<unsigned long long*>(base);
     uint32_t* base32 = reinterpret_cast<uint32_t*>(base64 + w64);
     cgs::HashScratch hs {};
     cgs::hash_scratch_carve(hs, n, base32, base64);
     uint32_t A[16], B[16];
-    draw_coefficients(n, A, B);
+    cgs::hash_coefficients(n, A, B);
     const int r = cgs::hash_build_device(keys, n, A, B, disp, table, table_capacity, hs, params,
                                          static_cast<cudaStream_t>(stream), nullptr);
     if (r == 4) return CGS_ERR_HASH_BUCKET_OVERFLOW;

@@ -348,18 +348,18 @@ int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uin
 
 /* cgs_perfect_hash_build without any device allocation.  This entry point
  * has no counterpart in the reference.  It exists for callers that cannot
- * allocate device memory when they need a table (for example while a stream
- * is being captured into a CUDA graph, inside an allocator callback, or in a
- * service that must not grow the device heap after start-up).  Its working
- * memory is a fixed array inside the library (about 6.9 MB, held on every
- * GPU that loads the library until the process exits), so n is limited to
- * CGS_NOALLOC_MAX_KEYS; larger inputs return CGS_ERR_CAPACITY.  The caller
- * still provides keys, disp and table (device) and params (host), exactly as
- * for cgs_perfect_hash_build, and gets the same results.  The first call on
- * a device resolves the array's address for that device; make it before any
- * stream capture.  All calls on a device share the array: each call clears
- * the parts that must start from zero, but calls that overlap on the GPU race
- * and must be serialised by the caller.  Synchronises `stream`. */
+ * allocate device memory when they need a table: code inside an allocator
+ * callback (allocating there would re-enter the allocator) or a service that
+ * reserves its device memory at start-up and must not grow the device heap
+ * afterwards.  Its working memory is a fixed array inside the library (about
+ * 6.9 MB, held on every GPU that loads the library until the process exits),
+ * so n is limited to CGS_NOALLOC_MAX_KEYS; larger inputs return
+ * CGS_ERR_CAPACITY.  The caller still provides keys, disp and table (device)
+ * and params (host), exactly as for cgs_perfect_hash_build, and gets the same
+ * results and status codes.  Each call looks the array's device address up
+ * for the current device.  All calls on a device share the array: each call
+ * clears the parts that must start from zero, but calls that overlap on the
+ * GPU race and must be serialised by the caller.  Synchronises `stream`. */
 #define CGS_NOALLOC_MAX_KEYS 262144u
 int cgs_perfect_hash_build_noalloc(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t displ_capacity,
                                    uint32_t* table, uint32_t table_capacity, uint32_t params[5], void* stream);
