@@ -84,6 +84,7 @@ def lib():
         L.ora_intersect_stats.argtypes = [P, fp, C.c_uint64, C.c_int, C.c_float, C.c_int, u32, C.c_int]
         L.ora_camera_rays.argtypes = [fp, C.c_uint32, C.c_uint32, fp]
         L.ora_patch_intersect.argtypes = [fp, u32, fp, C.c_float, C.c_int, P, P, P]
+        L.ora_patch_subdiv_host.argtypes = [fp, u32, fp, C.c_float, P, P]
         L.ora_patch_eval.argtypes = [fp, C.c_float, C.c_float, fp, fp]
         _lib = L
     return _lib
@@ -261,6 +262,20 @@ def patch_intersect(points, idx16, ray7, tol=2.0 ** -12, method=CLIP_HOST, t=np.
     hit = lib().ora_patch_intersect(np.ascontiguousarray(points, np.float32), np.ascontiguousarray(idx16, np.uint32),
                                     np.ascontiguousarray(ray7, np.float32), tol, method, _ptr(tt), _ptr(uv), _ptr(st))
     return bool(hit), float(tt[0]), uv, st
+
+
+def patch_subdiv_host(points, idx16, ray7, threshold=2.0 ** -4, t=np.inf, tmin=1.0):
+    """doSubdivision_host (src/Spline_Subdivision.cu:166-288) on one (ray,
+    patch) pair: 3-D sub-net boxes, triangle hits below `threshold` in u and
+    v.  The ray interval is [tmin, ray7[6]] (rt::intersect passes 1 and the
+    ray's max)."""
+    r = np.asarray(ray7, np.float32)
+    ray9 = np.array([*r[:6], tmin, r[6], 0.0], np.float32)
+    tt = np.array([t], np.float32)
+    uv = np.zeros(2, np.float32)
+    hit = lib().ora_patch_subdiv_host(np.ascontiguousarray(points, np.float32), np.ascontiguousarray(idx16, np.uint32),
+                                      ray9, threshold, _ptr(tt), _ptr(uv))
+    return bool(hit), float(tt[0]), uv
 
 
 def patch_eval(net16x4, u, v):

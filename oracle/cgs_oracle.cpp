@@ -728,6 +728,138 @@ bool intersect_patch(R& distance, V2<R>& uv, const Ray<R>& ray, const V4<R> P[16
     }
 }
 
+// ------------------------------------------------ host subdivision (3-D) --
+// doSubdivision_host, src/Spline_Subdivision.cu:166-288: the CPU variant,
+// which subdivides the 3-D net itself rather than a 2-D projection.  A stack
+// of parameter rectangles starts with u in [0, 1/2] and [1/2, 1]; each popped
+// rectangle's sub-net (subpatchV then subpatchU by de Casteljau slicing of
+// the homogeneous points, src/Spline.h:398-478) is bounded by the box of its
+// projected points; a box the ray misses is dropped; a rectangle smaller than
+// the threshold in both u and v (2^-4 by default, src/Spline.h:496-500) is
+// replaced by the two triangles of its corner points, and the nearer triangle
+// hit in front of the current best gives t and the rectangle's centre as
+// (u, v); otherwise it is halved along u or v alternately.  The box and
+// triangle tests come from the un-vendored Ds library; the semantics chosen
+// for them (also those of oracle/ds_compat) are a slab test clipped to the
+// ray's [tMin, tMax], and the Moller--Trumbore ray/triangle test with
+// |det| >= 1e-12 and t in [tMin, tMax].
+struct RayI { V3<float> o, d; float tmin, tmax; };
+
+inline bool box_hit(const Box& b, const RayI& r)  // Bounds3::intersect (Ds)
+{
+    float tMin = r.tmin, tMax = r.tmax;
+    const float lo[3] = {b.lo.x, b.lo.y, b.lo.z}, hi[3] = {b.hi.x, b.hi.y, b.hi.z};
+    const float o[3] = {r.o.x, r.o.y, r.o.z}, d[3] = {r.d.x, r.d.y, r.d.z};
+    for (int i = 0; i < 3; i++)
+    {
+        const float inv = 1.0f / d[i];
+        float t0 = (lo[i] - o[i]) * inv, t1 = (hi[i] - o[i]) * inv;
+        if (t0 > t1) std::swap(t0, t1);
+        if (t0 > tMin) tMin = t0;
+        if (t1 < tMax) tMax = t1;
+        if (tMin > tMax) return false;
+    }
+    return true;
+}
+
+inline bool triangle_hit(const RayI& r, V3<float> p0, V3<float> p1, V3<float> p2, float& t)  // triangle::intersect (Ds)
+{
+    const V3<float> e1 = p1 - p0, e2 = p2 - p0;
+    const V3<float> pv = cross(r.d, e2);
+    const float det = dot(e1, pv);
+    if (det > -1e-12f && det < 1e-12f) return false;
+    const float inv = 1.0f / det;
+    const V3<float> sv = r.o - p0;
+    const float u = dot(sv, pv) * inv;
+    if (u < 0 || u > 1) return false;
+    const V3<float> q = cross(sv, e1);
+    const float v = dot(r.d, q) * inv;
+    if (v < 0 || u + v > 1) return false;
+    const float tt = dot(e2, q) * inv;
+    if (tt < r.tmin || tt > r.tmax) return false;
+    t = tt;
+    return true;
+}
+
+// spline::slice on homogeneous points (src/Spline.h:324-364)
+template<int stride> inline void slice_dc4(V4<float>* c, float u, float v)
+{
+    auto C = [&](int i) -> V4<float>& { return c[i * stride]; };
+    const float iu = 1.0f - u;
+    const float vv = (v - u) / iu;
+    const float ivv = 1.0f - vv;
+    V4<float> P5, P6, P8;
+    P6 = u * C(1) + iu * C(0);
+    P5 = u * C(2) + iu * C(1);
+    C(2) = u * C(3) + iu * C(2);
+    P8 = u * P5 + iu * P6;
+    C(1) = u * C(2) + iu * P5;
+    C(0) = u * C(1) + iu * P8;
+    P6 = ivv * C(2) + vv * C(3);
+    P5 = ivv * C(1) + vv * C(2);
+    C(1) = ivv * C(0) + vv * C(1);
+    P8 = ivv * P5 + vv * P6;
+    C(2) = ivv * C(1) + vv * P5;
+    C(3) = ivv * C(2) + vv * P8;
+}
+
+inline Box projected_box(const V4<float>* p)  // spline::boundingbox, src/Spline.h:398-414
+{
+    Box b;
+    for (int i = 0; i < 16; i++) b.inflate(project(p[i]));
+    return b;
+}
+
+bool subdiv_host(float& distance, V2<float>& uv, const RayI& ray, const V4<float> P[16], float threshold)
+{
+    struct State { V2<float> min, max; bool cutside; };
+    if (!box_hit(projected_box(P), ray)) return false;
+    std::vector<State> st;
+    st.push_back({{0.0f, 0.0f}, {0.5f, 1.0f}, false});
+    st.push_back({{0.5f, 0.0f}, {1.0f, 1.0f}, false});
+    bool found = false;
+    V4<float> sub[16];
+    while (!st.empty())
+    {
+        const State e = st.back();
+        st.pop_back();
+        // spline::subpatchBoundingbox, src/Spline.h:464-478
+        for (int i = 0; i < 16; i++) sub[i] = P[i];
+        for (int i = 0; i < 4; i++) slice_dc4<4>(sub + i, e.min.y, e.max.y);
+        for (int i = 0; i < 4; i++) slice_dc4<1>(sub + 4 * i, e.min.x, e.max.x);
+        if (!box_hit(projected_box(sub), ray)) continue;
+        const float x = 0.5f * (e.min.x + e.max.x);
+        const float y = 0.5f * (e.min.y + e.max.y);
+        if ((e.max.x - e.min.x) < threshold && (e.max.y - e.min.y) < threshold)
+        {
+            const V3<float> p00 = project(sub[0]), p10 = project(sub[3]), p01 = project(sub[12]),
+                            p11 = project(sub[15]);
+            float t = 0, t1 = 0;
+            bool b0 = triangle_hit(ray, p10, p01, p00, t);
+            const bool b1 = triangle_hit(ray, p01, p10, p11, t1);
+            if (b0) { if (b1 && t1 < t) t = t1; }
+            else if (b1) { t = t1; b0 = true; }
+            if (b0 && t < distance)
+            {
+                distance = t;
+                uv = {x, y};
+                found = true;
+            }
+        }
+        else if (e.cutside)
+        {
+            st.push_back({{e.min.x, e.min.y}, {x, e.max.y}, !e.cutside});
+            st.push_back({{x, e.min.y}, {e.max.x, e.max.y}, !e.cutside});
+        }
+        else
+        {
+            st.push_back({{e.min.x, e.min.y}, {e.max.x, y}, !e.cutside});
+            st.push_back({{e.min.x, y}, {e.max.x, e.max.y}, !e.cutside});
+        }
+    }
+    return found;
+}
+
 // Newton polish of (u,v,t) on S(u,v) = o + t d in FP64.  Starts from the
 // search result; returns false (and leaves the inputs) if it diverges or
 // leaves the patch domain by more than 1e-6.
@@ -1894,6 +2026,26 @@ int ora_patch_intersect(const float* points4, const uint32_t* idx16, const float
     bool b = intersect_patch<float>(dist, uv, r, P, tol, method, &cs);
     if (b) { *inout_t = dist; out_uv[0] = uv.x; out_uv[1] = uv.y; }
     if (stats4) { stats4[0] = cs.iterations; stats4[1] = cs.pushes; stats4[2] = cs.maxDepth; stats4[3] = cs.overflow; }
+    return b ? 1 : 0;
+}
+
+// doSubdivision_host on one (ray, patch) pair.  ray9 = origin, unit
+// direction, tMin, tMax (and one unused slot); *inout_t is the current best
+// distance in, the hit's distance out.
+int ora_patch_subdiv_host(const float* points4, const uint32_t* idx16, const float* ray9, float threshold,
+                          float* inout_t, float* out_uv)
+{
+    V4<float> P[16];
+    for (int k = 0; k < 16; k++)
+    {
+        const float* p = points4 + 4 * idx16[k];
+        P[k] = {p[0], p[1], p[2], p[3]};
+    }
+    const RayI r {{ray9[0], ray9[1], ray9[2]}, {ray9[3], ray9[4], ray9[5]}, ray9[6], ray9[7]};
+    float dist = *inout_t;
+    V2<float> uv {0, 0};
+    const bool b = subdiv_host(dist, uv, r, P, threshold);
+    if (b) { *inout_t = dist; out_uv[0] = uv.x; out_uv[1] = uv.y; }
     return b ? 1 : 0;
 }
 
