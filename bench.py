@@ -12,14 +12,15 @@ value  = total rays (primary + bounce + shadow) / device time of K frames,
 e2e    = the same through cgs_render_host (pinned host framebuffer, copies inside the
          timed region).
 accuracy = max relative t error and hit/miss disagreement of the primary hits
-         of a seeded 1% pixel subset against the pure-FP64 GPU search (itself
-         held to the FP64 oracle by the test suite).
+         of a seeded 1% pixel subset against the FP64 oracle (and, beside it,
+         against the pure-FP64 GPU search).
 Further objects: split_longest (the same frame on the longest-axis BVH
 build), precision (2^20 grazing rays), batching (64 scenes in one batch
 against 64 plain launches), serving (Poisson request streams through the
 continuous-batching server against the plain one-request-per-launch server).
---impl reference: the reference's CPU path (the oracle's restatement of it)
-         on all host cores.
+--impl reference: the reference's CPU path (the oracle's restatement of it,
+         held bit-identical to the reference's own code by the tests) on all
+         host cores, one full frame per step.
 """
 from __future__ import annotations
 
@@ -131,6 +132,32 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def onchip_peaks():
+    """L1 and L2 load bandwidth of this GPU, measured now with the committed
+    probes (cgspline_gb300/membench/membench.cu: 16-byte loads, CUDA events,
+    best of three runs).  L1: every CTA re-reads its own 16 KB slice (4 CTAs
+    of 256 threads per SM); L2: all CTAs stream a 64 MB buffer through
+    ld.global.cg (bypassing L1)."""
+    import ctypes as C
+    from cgspline_gb300 import build as B
+    lib = C.CDLL(B.build_membench())
+    lib.cgs_membench.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int,
+                                 C.POINTER(C.c_double)]
+    out = {}
+    for name, level, nbytes, reps in (("l1", 1, 16 << 10, 4000), ("l2", 2, 64 << 20, 200)):
+        best = 0.0
+        for _ in range(3):
+            v = C.c_double(0.0)
+            e = lib.cgs_membench(level, nbytes, 4, 256, reps, 5, C.byref(v))
+            if e:
+                raise RuntimeError(f"cgs_membench({name}) failed: CUDA error {e}")
+            best = max(best, v.value)
+        out[name + "_gbs"] = best
+    out["how"] = ("membench.cu: L1 = 16 KB slice per CTA re-read 4000x with ld.global.nc.v4 (4 CTAs x 256 threads "
+                  "per SM); L2 = 64 MB buffer streamed 200x with ld.global.cg.v4; best of 3, 5 timed launches each")
+    return out
+
+
 def traffic_summary():
     """DRAM bytes per launch of the dominant kernel (k_collect, first pass over
     the frame's primary rays) from the committed ncu capture summary."""
@@ -161,6 +188,25 @@ def whole_job_mrays(rays_per_frame: int, steps: int, world: int, total_ms: float
 
 
 # ----------------------------------------------------------- CPU legs --
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def cpu_leg(scene, camera, sample_rows=1):
     """The oracle's restatement of the reference's CPU tracer on every host
     core, over every sample_rows-th row of the frame."""
@@ -169,6 +215,7 @@ def cpu_leg(scene, camera, sample_rows=1):
     r = o.render_rows(camera, W, H, 0, sample_rows, depth=DEPTH)
     rays = r["primary"] + r["bounce"] + r["shadow"]
     return {"value": rays / r["seconds"] / 1e6, "unit": "Mrays/s", "cores": r["threads"], "kind": "port",
+            "cpu_model": cpu_model(), "nproc": os.cpu_count(),
             "sample": f"every {sample_rows} row(s) of the {W}x{H} frame: {r['primary']} primary + {r['bounce']} "
                       f"bounce + {r['shadow']} shadow rays in {r['seconds']:.2f} s (oracle restatement, "
                       f"{r['threads']} threads, 32x32 tiles)",
@@ -176,16 +223,19 @@ def cpu_leg(scene, camera, sample_rows=1):
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU path on this host's cores (the
-    reference itself does not build here: its Ds dependency is absent), on
-    a bounded sample of rows of the headline frame per step."""
+    """--impl reference: the reference's CPU path on this host's cores, one
+    full headline frame per step (the same rows as the cpu_baseline leg).
+    The reference's own sources compile only where its tree is present,
+    which a GPU machine is not; this arm therefore times the oracle's
+    restatement of the reference's CPU tracer, which the tests hold
+    bit-identical to the reference build (hits and frames) on these scenes."""
     from cgspline_gb300 import scenes
     if rank != 0:
         return
     scene, cam = scenes.scene_c2(), scenes.camera_c2()
-    rows = 2
+    rows = 1
     for _ in range(args.warmup):
-        cpu_leg(scene, cam, rows * 4)
+        cpu_leg(scene, cam, 8)
     tot_rays, tot_s, leg = 0, 0.0, None
     for _ in range(args.steps):
         leg = cpu_leg(scene, cam, rows)
@@ -198,7 +248,8 @@ def run_reference(args, rank, world):
             "impl": "reference",
             "config": {"workload": f"torus 16384 patches, {W}x{H} primary + {DEPTH} bounce, PBR, 2 point lights, "
                                    f"CPU sample = every {rows} rows"},
-            "cpu_baseline": {k: leg[k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "Mrays/s"},
+            "cpu_baseline": {k: leg[k] for k in ("kind", "cores", "cpu_model", "nproc", "sample")}
+                            | {"value": v, "unit": "Mrays/s"},
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -229,6 +280,24 @@ def accuracy_vs_fp64(rt, g, rays, prec, group=None):
             "rays_over_1e-5": int((rel > 1e-5).sum()), "hit_miss_disagreement": float((hit_a != hit_r).mean()),
             "patch_disagreement": float((both & (a["patch"] != ref["patch"])).mean()),
             "reference": "pure-FP64 GPU search"}
+
+
+def accuracy_vs_oracle64(rt, g, rays, prec, scene):
+    """FP32 (+ polish) hits of `rays` against the FP64 oracle (the CPU
+    restatement of the reference's search run in double to 1e-9, every root
+    polished): the checker of the accuracy bar, untimed."""
+    import numpy as np
+
+    import oracle
+    ref = oracle.OracleScene(scene).intersect(rays.cpu().numpy(), precision=oracle.FP64)
+    a = {k: v.cpu().numpy() for k, v in g.intersect(rays, precision=prec).items()}
+    hit_a, hit_r = a["patch"] >= 0, ref["patch"] >= 0
+    both = hit_a & hit_r
+    rel = np.abs(a["t"][both] - ref["t"][both]) / ref["t"][both]
+    return {"rays": int(rays.shape[1]), "max_rel_t_err": float(rel.max(initial=0.0)),
+            "rays_over_1e-5": int((rel > 1e-5).sum()), "hit_miss_disagreement": float((hit_a != hit_r).mean()),
+            "patch_disagreement": float((both & (a["patch"] != ref["patch"])).mean()),
+            "reference": "FP64 oracle (CPU restatement of the reference's search in double, polished roots)"}
 
 
 def frame_leg(rt, torch, g, cam, tracer, frame, stream, flush, steps):
@@ -541,23 +610,33 @@ def main():
         k_flops = 12 * kc["nodes"]
         achieved = k_bytes / launch_s / 1e9
         tr = traffic_summary()
+        onchip = onchip_peaks()
+        dram_bytes = tr.get("bytes_per_launch") if tr else None
         # the frame as a whole: a ray (48 B in + out), a 64 B node per
         # inner-node visit, an 8 B hash probe per backtrack, a 256 B patch +
         # 64 B of candidate-list traffic per (ray, patch) search
         alg_bytes = 48 * nrays + 64 * nodes + 8 * hashes + 320 * cand
         alg_flops = 12 * nodes + 296 * cand + 470 * iters + 200 * nrays
         sec_per_frame = total_ms / args.steps / 1e3
-        extra["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                             "frac": achieved / peaks["hbm_gbs"],
-                             "traffic": tr.get("bytes_per_launch") if tr else None,
-                             "peak_source": pk,
+        extra["roofline"] = {"bound": "l1", "achieved": achieved, "peak": onchip["l1_gbs"], "unit": "GB/s",
+                             "frac": achieved / onchip["l1_gbs"],
+                             "traffic": dram_bytes,
+                             "peak_source": "measured in this run: " + onchip["how"],
                              "kernel": f"k_collect: traversal, first pass over the frame's {nprim} primary rays",
                              "launch_ms": launch_s * 1e3, "algorithmic_bytes_per_launch": k_bytes,
                              "per_ray": {"nodes": kc["nodes"] / nprim, "hash_lookups": kc["hash_lookups"] / nprim,
                                          "hash_table_reads": kc["hash_table_reads"] / nprim},
-                             "note": "the 6.6 MB scene is L2-resident: node reads are served by L1/L2, so the "
-                                     "algorithmic bytes exceed the DRAM traffic; the kernel is bound by the L1 "
-                                     "data pipe and instruction issue",
+                             "note": "the 6.6 MB scene is L2-resident and the node reads are served by L1/L2: "
+                                     "ncu shows the L1 data pipe as the busiest unit, so the algorithmic bytes "
+                                     "(28 B per ray, 64 B per inner-node visit, 8 B per backtrack) are set against "
+                                     "the measured L1 load bandwidth; the other roofs follow",
+                             "l2": {"peak": onchip["l2_gbs"], "unit": "GB/s", "frac": achieved / onchip["l2_gbs"],
+                                    "note": "algorithmic bytes against the L2 roof (an upper bound on the L2 "
+                                            "share: part of them hit in L1)"},
+                             "dram": {"achieved": (dram_bytes / launch_s / 1e9) if dram_bytes else None,
+                                      "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                      "frac": (dram_bytes / launch_s / 1e9 / peaks["hbm_gbs"]) if dram_bytes
+                                      else None, "peak_source": pk},
                              "fp32": {"achieved": k_flops / launch_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                                       "frac": k_flops / launch_s / 1e12 / fp32_peak,
                                       "peak_source": f"nominal 152 SM x 256 flop/clk at {mhz:.0f} MHz"},
@@ -570,7 +649,8 @@ def main():
         allr = rt.camera_rays(cam, W, H, device=local)
         sub = torch.from_numpy(scenes.random_subset(W * H, 0.01, seed=77)).to(dev)
         subset = allr[:, sub].contiguous()
-        extra["accuracy"] = accuracy_vs_fp64(rt, g, subset, prec)
+        extra["accuracy"] = accuracy_vs_oracle64(rt, g, subset, prec, scene)
+        extra["accuracy"]["vs_gpu_fp64"] = accuracy_vs_fp64(rt, g, subset, prec)
     if not args.quick and rank == 0:
         # plain per-frame GPU path (one thread per pixel, the whole chain inline)
         if sched != rt.PLAIN:

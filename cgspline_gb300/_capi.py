@@ -9,6 +9,8 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libcgspline_gb300.so")
+# the same sources built without multiply-add contraction (parity build)
+LIB_NOFMA_PATH = os.path.join(HERE, "_lib", "libcgspline_gb300_nofma.so")
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "scene not built",
@@ -88,7 +90,7 @@ class Counters(C.Structure):
                                           "kernel_launches", "hash_table_reads")]
 
 
-_lib = None
+_libs = {}
 
 # (name, restype, argtypes) for every entry point declared in include/cgspline.h
 P = C.c_void_p
@@ -141,22 +143,22 @@ SIGNATURES = [
 
 
 def load(path: str = LIB_PATH):
-    """Load the library (building it first if the sources are newer)."""
-    global _lib
-    if _lib is not None:
-        return _lib
+    """Load the library at `path` (the product build by default; building it
+    first if it is missing)."""
+    if path in _libs:
+        return _libs[path]
     if not os.path.exists(path):
         try:
             from . import build as _b
-            _b.build()
+            _b.build(fmad=path != LIB_NOFMA_PATH)
         except Exception as e:  # no nvcc / failed build: fail loudly
-            raise ImportError(f"libcgspline_gb300.so is missing and could not be built: {e}") from e
+            raise ImportError(f"{os.path.basename(path)} is missing and could not be built: {e}") from e
     lib = C.CDLL(path)
     for name, res, args in SIGNATURES:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = lib
+    _libs[path] = lib
     return lib
 
 

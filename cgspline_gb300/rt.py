@@ -68,10 +68,13 @@ class GpuScene:
 
     `scene` is one scenes.Scene or a list of them; scene k of a list becomes
     group k of the store (its own object-level BVH, lights and environment,
-    sharing the patch and BVH arrays with the others)."""
+    sharing the patch and BVH arrays with the others).  lib_path selects the
+    library build (the product build, or _capi.LIB_NOFMA_PATH for the parity
+    build without multiply-add contraction)."""
 
-    def __init__(self, scene, device: int = 0, build: bool = True, stream=None, split: int = SPLIT_REFERENCE):
-        self.lib = _capi.load()
+    def __init__(self, scene, device: int = 0, build: bool = True, stream=None, split: int = SPLIT_REFERENCE,
+                 lib_path: str = _capi.LIB_PATH):
+        self.lib = _capi.load(lib_path)
         self.scenes = list(scene) if isinstance(scene, (list, tuple)) else [scene]
         self.scene = self.scenes[0]
         self.device = device

@@ -1,11 +1,31 @@
-"""Generate the committed golden vectors under tests/golden/.
+"""Generate the committed golden vectors under tests/golden/ from the reference itself.
 
-c1_golden.npz: the 4x4-patch heightfield scene (seed 1), its BVH and perfect
-hash, and closest hits of 128x128 camera rays, as computed by the oracle's
-restatement of the reference host path (oracle/cgs_oracle.cpp).  When the
-reference's own sources were compiled here (oracle/_ref, see
-oracle/build_ref.py), the script also checks that they give the same BVH and
-hits and records that in the file ("pinned_by_reference" = 1).
+Every expected output in these files is computed by the reference program's
+own hot-path code, compiled unchanged from its sources into oracle/_ref (see
+oracle/build_ref.py), and checked here against the oracle's restatement
+(oracle/cgs_oracle.cpp): the script refuses to write a file where the two
+differ, and records "pinned_by_reference" = 1 in every file it writes.  The
+reference tree must be present (it is not on the GPU machines, which use the
+committed files).
+
+  c1_golden.npz      the 4x4-patch heightfield (seed 1): scene, BVH, perfect
+                     hash and closest hits of 128x128 camera rays (the inputs
+                     are stored; the BVH and hash arrays are the oracle's,
+                     the BVH checked equal to the reference's);
+  torus32_golden.npz the displaced torus on a 32x32 patch grid (seed 2):
+                     closest hits of 160x90 camera rays and a 64x36 frame
+                     (depth 1, one material for the whole torus);
+  union_golden.npz   union scene 5 of the batching workload at <= 20,000
+                     patches (19,800 patches, 51 objects): closest and any
+                     hits of 96x96 camera rays and a 64x64 frame;
+  teaset_golden.npz  the reference's own teaset scene (assets/scenes/
+                     Teaset01.dl with the .be surfaces it names): the scene's
+                     surfaces, objects, light and camera, closest hits of
+                     160x90 camera rays and a 96x54 frame.
+
+The seeded scenes are regenerated by the tests from cgspline_gb300.scenes;
+each file stores a SHA-256 of the scene arrays so that a changed generator is
+caught.  The teaset's geometry is stored in the file itself.
 
 Run:  python tests/golden/make_golden.py
 """
@@ -17,35 +37,96 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
 
 import oracle  # noqa: E402
+from golden_data import one_material, scene_sha, torus32, union5  # noqa: E402,F401
+from oracle import ref as R  # noqa: E402
 from cgspline_gb300 import scenes as S  # noqa: E402
+
+REFERENCE_ROOT = os.environ.get("CGS_REFERENCE_ROOT", "/root/reference")
+
+
+def teaset():
+    from cgspline_gb300 import dl
+    return dl.load_dl(os.path.join(REFERENCE_ROOT, "assets", "scenes", "Teaset01.dl"))
+
+
+def same_hits(a, b, keys=("t", "u", "v", "patch", "object")):
+    return all(np.array_equal(a[k], b[k]) for k in keys)
+
+
+def reference_outputs(sc, cam, w, h, fw, fh, depth=1):
+    """Closest (and any) hits of w x h camera rays and an fw x fh frame, from
+    the reference build; each checked equal to the oracle's."""
+    r = R.RefScene(sc)
+    o = oracle.OracleScene(sc)
+    for k in list(range(len(sc.surfaces))) + [-1]:
+        rb, ob = r.bvh(k), o.bvh(k)
+        if not all(np.array_equal(rb[f], ob[f]) for f in ("nodes", "keys", "indices")):
+            raise SystemExit(f"BVH {k}: reference and oracle differ")
+    rays = oracle.camera_rays(cam, w, h)
+    hr, ho = r.intersect(rays), o.intersect(rays)
+    if not same_hits(hr, ho):
+        raise SystemExit("closest hits: reference and oracle differ")
+    ar, ao = r.intersect(rays, any_hit=True), o.intersect(rays, any_hit=True)
+    if not np.array_equal(ar["hit"], ao["patch"] >= 0):
+        raise SystemExit("any hits: reference and oracle differ")
+    fr = r.render(cam, fw, fh, depth=depth)
+    fo = o.render(cam, fw, fh, depth=depth)
+    if not (np.array_equal(fr["packed"], fo["packed"]) and np.array_equal(fr["rgb"], fo["rgb"])):
+        raise SystemExit("frames: reference and oracle differ")
+    print(f"  {int((hr['patch'] >= 0).sum())} hits of {rays.shape[1]} rays; "
+          f"{int(ar['hit'].sum())} blocked; frame {fw}x{fh}: reference == oracle")
+    return dict(camera=cam.packed(), width=np.int32(w), height=np.int32(h), t=hr["t"], u=hr["u"], v=hr["v"],
+                patch=hr["patch"], object=hr["object"], any_hit=ar["hit"], frame_width=np.int32(fw),
+                frame_height=np.int32(fh), depth=np.int32(depth), frame_packed=fr["packed"], frame_rgb=fr["rgb"],
+                pinned_by_reference=np.int32(1))
 
 
 def main():
+    if not R.available():
+        raise SystemExit(f"the reference build is needed: {R.unavailable_reason()}")
+
+    # C1: the inputs, BVH and hash in the file (as before), checked against the reference
     sc = S.scene_c1()
     o = oracle.OracleScene(sc)
+    r = R.RefScene(sc)
     b = o.bvh(0)
+    rb = r.bvh(0)
+    if not all(np.array_equal(rb[k], b[k]) for k in ("nodes", "keys", "indices")):
+        raise SystemExit("C1 BVH: reference and oracle differ")
     rays = oracle.camera_rays(S.camera_c1(), 128, 128)
-    r = o.intersect(rays)
-    pinned = 0
-    try:
-        from oracle import ref as R
-        if R.available():
-            rr = R.intersect_scene(sc, rays)
-            rb = R.bvh_export(sc)
-            same_bvh = all(np.array_equal(rb[k], b[k]) for k in ("nodes", "keys", "indices"))
-            same_hits = np.array_equal(rr["patch"], r["patch"]) and np.array_equal(rr["t"], r["t"])
-            pinned = int(same_bvh and same_hits)
-            print("reference build agrees:", same_bvh, same_hits)
-    except ImportError:
-        pass
+    hr, ho = r.intersect(rays), o.intersect(rays)
+    if not same_hits(hr, ho):
+        raise SystemExit("C1 hits: reference and oracle differ")
     np.savez_compressed(os.path.join(HERE, "c1_golden.npz"), points=sc.surfaces[0].points,
                         indices=sc.surfaces[0].indices, bvh_nodes=b["nodes"], bvh_keys=b["keys"],
                         bvh_indices=b["indices"], bvh_table=b["table"], bvh_disp=b["disp"],
                         hash_params=np.array([b["A"], b["B"], b["N"], b["mask"]], np.uint32), rays=rays,
-                        t=r["t"], u=r["u"], v=r["v"], patch=r["patch"], pinned_by_reference=np.int32(pinned))
-    print("wrote c1_golden.npz; hits", int((r["patch"] >= 0).sum()), "of", rays.shape[1])
+                        t=hr["t"], u=hr["u"], v=hr["v"], patch=hr["patch"], pinned_by_reference=np.int32(1))
+    print("c1_golden.npz: hits", int((hr["patch"] >= 0).sum()), "of", rays.shape[1], "(reference == oracle)")
+
+    for name, make, size, frame in (("torus32", torus32, (160, 90), (64, 36)),
+                                    ("union", union5, (96, 96), (64, 64))):
+        sc, cam = make()
+        print(f"{name}_golden.npz: {sc.patch_count} patches, {len(sc.objects)} objects")
+        out = reference_outputs(sc, cam, *size, *frame)
+        np.savez_compressed(os.path.join(HERE, f"{name}_golden.npz"), scene_sha=np.bytes_(scene_sha(sc)), **out)
+
+    sc, cam = teaset()
+    print(f"teaset_golden.npz: {sc.patch_count} patches, {len(sc.objects)} objects")
+    out = reference_outputs(sc, cam, 160, 90, 96, 54)
+    geo = {}
+    for k, s in enumerate(sc.surfaces):
+        geo[f"surface{k}_points"] = s.points
+        geo[f"surface{k}_indices"] = s.indices
+    objs = np.array([[o.surface, *o.local2world, *o.world2local, *o.material.packed()] for o in sc.objects],
+                    np.float32)
+    lights = np.array([l.packed() for l in sc.lights], np.float32)
+    np.savez_compressed(os.path.join(HERE, "teaset_golden.npz"), surfaces=np.int32(len(sc.surfaces)), objects=objs,
+                        lights=lights, background=np.asarray(sc.background, np.float32),
+                        ambient=np.asarray(sc.ambient, np.float32), scene_sha=np.bytes_(scene_sha(sc)), **geo, **out)
 
 
 if __name__ == "__main__":

@@ -9,7 +9,9 @@ import pytest
 
 from cgspline_gb300 import dl, scenes as S
 
-REF_ASSETS = "/root/reference/assets"
+# the reference tree's assets, where the tree is present (the teaset scene's
+# geometry also lives in tests/golden/teaset_golden.npz for machines without it)
+REF_ASSETS = os.path.join(os.environ.get("CGS_REFERENCE_ROOT", "/root/reference"), "assets")
 
 SYNTH = """
 // a synthetic scene in the reference's description language

@@ -1,0 +1,109 @@
+"""The CUDA path against the reference program's own outputs (tests/golden/).
+
+The fixtures were computed by the reference's hot-path code compiled from its
+sources (tests/golden/make_golden.py); the GPU runs the same scenes and rays
+through the C ABI.  Two builds of the library are checked:
+
+* the product build (multiply-add contraction on): hit/miss and any-hit
+  decisions identical; the same patch on every hit except where one of the
+  two hits lies within 1e-4 of its patch's edge (a root that rounding puts
+  on the other side of the domain boundary); t within 1e-5 relative and
+  (u, v) within 1e-3 on hits of the same patch; frames with the same packed
+  sRGB pixels and linear RMSE below 1e-5;
+* the parity build (nvcc --fmad=false, the same sources): t within 1e-6
+  relative and (u, v) within 1e-6 of the reference, and bit-identical to the
+  oracle's restatement of the reference's GPU clip structure
+  (doBezierClipping2D_device: sub-nets re-derived from the patch on a pop,
+  where the reference's CPU path keeps them on its stack).
+"""
+import numpy as np
+import pytest
+
+import golden_data as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    return torch
+
+
+@pytest.fixture(scope="module")
+def rt():
+    from cgspline_gb300 import rt
+    return rt
+
+
+def host(d):
+    return {k: v.cpu().numpy() for k, v in d.items()}
+
+
+def near_edge(u, v, tol=1e-4):
+    return np.minimum.reduce([u, 1 - u, v, 1 - v]) < tol
+
+
+def check_hits(g, r, t_rtol, uv_atol, max_edge_fraction=1e-5):
+    """g against r (dicts of t, u, v, patch): returns (hits, edge disagreements)."""
+    gp, rp = np.asarray(g["patch"]), np.asarray(r["patch"])
+    assert np.array_equal(gp >= 0, rp >= 0), f"hit/miss disagreements: {int(((gp >= 0) != (rp >= 0)).sum())}"
+    hit = rp >= 0
+    diff = hit & (gp != rp)
+    if diff.any():
+        edge = near_edge(np.asarray(g["u"])[diff], np.asarray(g["v"])[diff]) | \
+            near_edge(np.asarray(r["u"])[diff], np.asarray(r["v"])[diff])
+        assert edge.all(), f"{int((~edge).sum())} patch disagreements away from patch edges"
+        assert diff.sum() <= max(2, max_edge_fraction * hit.sum()), int(diff.sum())
+    same = hit & ~diff
+    rel = np.abs(np.asarray(g["t"])[same] - np.asarray(r["t"])[same]) / np.asarray(r["t"])[same]
+    assert rel.max(initial=0) <= t_rtol, rel.max()
+    duv = np.maximum(np.abs(np.asarray(g["u"])[same] - np.asarray(r["u"])[same]),
+                     np.abs(np.asarray(g["v"])[same] - np.asarray(r["v"])[same]))
+    assert duv.max(initial=0) <= uv_atol, duv.max()
+    return int(hit.sum()), int(diff.sum())
+
+
+@pytest.mark.parametrize("name", G.NAMES)
+def test_product_build_matches_reference(rt, torch, name):
+    g = G.load(name)
+    sc, cam = G.scene(name, g)
+    gs = rt.GpuScene(sc)
+    from oracle import camera_rays
+    rays = torch.from_numpy(camera_rays(cam, int(g["width"]), int(g["height"]))).cuda()
+    h = host(gs.intersect(rays))
+    nhit, _ = check_hits(h, g, t_rtol=1e-5, uv_atol=1e-3)
+    assert nhit == int((g["patch"] >= 0).sum()) > 4000
+    a = host(gs.intersect(rays, any_hit=True))
+    assert np.array_equal(a["patch"] >= 0, g["any_hit"])
+    fb, lin = rt.RayTracer(rt.Options(recursion_depth=int(g["depth"]))).render_host(
+        cam, gs, int(g["frame_width"]), int(g["frame_height"]))
+    assert np.array_equal(fb, g["frame_packed"])
+    assert float(np.sqrt(((lin - g["frame_rgb"]) ** 2).mean())) < 1e-5
+    assert gs.counters()["device_errors"] == 0
+    gs.close()
+
+
+@pytest.mark.parametrize("name", G.NAMES)
+def test_parity_build_matches_reference(rt, torch, oracle_mod, name):
+    from cgspline_gb300 import _capi
+    g = G.load(name)
+    sc, cam = G.scene(name, g)
+    gs = rt.GpuScene(sc, lib_path=_capi.LIB_NOFMA_PATH)
+    rays_h = oracle_mod.camera_rays(cam, int(g["width"]), int(g["height"]))
+    h = host(gs.intersect(torch.from_numpy(rays_h).cuda()))
+    check_hits(h, g, t_rtol=1e-6, uv_atol=1e-6, max_edge_fraction=0)
+    od = oracle_mod.OracleScene(sc).intersect(rays_h, method=oracle_mod.CLIP_DEVICE)
+    for k in ("t", "u", "v", "patch", "object"):
+        assert np.array_equal(h[k], od[k]), k
+    gs.close()
+
+
+def test_c1_fixture_on_parity_build(rt, torch, oracle_mod):
+    import os
+    from cgspline_gb300 import _capi, scenes as S
+    g = np.load(os.path.join(G.GOLDEN, "c1_golden.npz"))
+    gs = rt.GpuScene(S.scene_c1(), lib_path=_capi.LIB_NOFMA_PATH)
+    h = host(gs.intersect(torch.from_numpy(g["rays"]).cuda()))
+    check_hits(h, g, t_rtol=1e-6, uv_atol=1e-6, max_edge_fraction=0)
+    gs.close()
