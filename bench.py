@@ -282,7 +282,7 @@ def accuracy_vs_fp64(rt, g, rays, prec, group=None):
             "reference": "pure-FP64 GPU search"}
 
 
-def accuracy_vs_oracle64(rt, g, rays, prec, scene):
+def accuracy_vs_oracle64(rt, g, rays, prec, scene, method=None):
     """FP32 (+ polish) hits of `rays` against the FP64 oracle (the CPU
     restatement of the reference's search run in double to 1e-9, every root
     polished): the checker of the accuracy bar, untimed."""
@@ -290,7 +290,8 @@ def accuracy_vs_oracle64(rt, g, rays, prec, scene):
 
     import oracle
     ref = oracle.OracleScene(scene).intersect(rays.cpu().numpy(), precision=oracle.FP64)
-    a = {k: v.cpu().numpy() for k, v in g.intersect(rays, precision=prec).items()}
+    kw = {} if method is None else {"method": method}
+    a = {k: v.cpu().numpy() for k, v in g.intersect(rays, precision=prec, **kw).items()}
     hit_a, hit_r = a["patch"] >= 0, ref["patch"] >= 0
     both = hit_a & hit_r
     rel = np.abs(a["t"][both] - ref["t"][both]) / ref["t"][both]
@@ -338,7 +339,90 @@ def precision_leg(rt, scenes, torch, dev, g, scene, flush, n=1 << 20):
                           "hit_miss_disagreement": float(((a["patch"] >= 0) != (ref["patch"] >= 0)).mean()),
                           "patch_disagreement": float((both & (a["patch"] != ref["patch"])).mean())})
     out["fp64"]["hits"] = int((ref["patch"] >= 0).sum())
+    # the checker: every level (and the GPU's own FP64 search) against the FP64 oracle
+    import oracle
+    host_rays = rays.cpu().numpy()
+    o64 = oracle.OracleScene(scene).intersect(host_rays, precision=oracle.FP64)
+    for name in ("fp64", "fp32", "fp32_polish64", "fp32_graze64"):
+        a = res[name]
+        both = (a["patch"] >= 0) & (o64["patch"] >= 0)
+        rel = np.abs(a["t"][both] - o64["t"][both]) / o64["t"][both]
+        out[name]["vs_oracle64"] = {"max_rel_t_err": float(rel.max(initial=0.0)),
+                                    "rays_over_1e-5": int((rel > 1e-5).sum()),
+                                    "hit_miss_disagreement": float(((a["patch"] >= 0) != (o64["patch"] >= 0)).mean())}
     return out
+
+
+def subdivision_leg(rt, torch, g, cam, flush, scene, subset):
+    """The two intersectors of the reference on the frame's 2,073,600 primary
+    rays (closest hit, FP32, tolerance 2^-12): Bezier clipping
+    (doBezierClipping) and subdivision (doSubdivision, the device variant's
+    bisection), each timed alone with L2 flushed; their agreement on every
+    ray, and each against the FP64 oracle on the 1% subset."""
+    import numpy as np
+    stream = torch.cuda.current_stream()
+    rays = rt.camera_rays(cam, W, H, device=torch.cuda.current_device())
+    n = int(rays.shape[1])
+    out = {"rays": n, "workload": f"torus 16384 patches, {W}x{H} primary rays, closest hit, FP32"}
+    res = {}
+    for name, method in (("clip", rt.CLIP), ("subdivision", rt.SUBDIV)):
+        g.intersect(rays, method=method)
+        torch.cuda.synchronize()
+        holder = {}
+        ms = timed(torch, stream, flush, lambda: holder.update(r=g.intersect(rays, method=method)), 3)
+        res[name] = {k: v.cpu().numpy() for k, v in holder["r"].items()}
+        c = g.counters()
+        out[name] = {"Mrays_s": n / (sum(ms) / 3 * 1e-3) / 1e6, "ms": sum(ms) / 3,
+                     "clip_or_subdivision_iterations_per_ray": c["iterations"] / max(1, c["rays"]),
+                     "accuracy": accuracy_vs_oracle64(rt, g, subset, rt.FP32, scene, method=method)}
+    a, b = res["clip"], res["subdivision"]
+    ha, hb = a["patch"] >= 0, b["patch"] >= 0
+    both = ha & hb
+    rel = np.abs(a["t"][both] - b["t"][both]) / a["t"][both]
+    out["agreement"] = {"hit_miss_disagreement": float((ha != hb).mean()),
+                        "patch_disagreement": float((both & (a["patch"] != b["patch"])).mean()),
+                        "max_rel_t_diff": float(rel.max(initial=0.0)),
+                        "rays_t_diff_over_1e-5": int((rel > 1e-5).sum()),
+                        "subdivision_closer_by_1e-5": int((both & (b["t"] < a["t"] * (1 - 1e-5))).sum()),
+                        "clip_closer_by_1e-5": int((both & (a["t"] < b["t"] * (1 - 1e-5))).sum())}
+    return out
+
+
+def store_build(rt, scs, dev, split):
+    """A resident store of scenes `scs`, built with its phases timed: adding
+    the surfaces and objects, the host BVH build (cgs_bvh_build, all host
+    cores), upload + perfect-hash build (cgs_hash_build); then the hash build
+    alone a second time (the store is resident: keys in, tables out).  The
+    hash build's algorithmic bytes are its keys read and its displacement
+    and table words written, 4 bytes each, against the HBM roof."""
+    import torch
+    t0 = time.perf_counter()
+    store = rt.GpuScene(scs, device=dev.index or 0, split=split, build=False)
+    t1 = time.perf_counter()
+    check = rt._capi.check
+    check(store.lib.cgs_bvh_build(store.h), "cgs_bvh_build")
+    t2 = time.perf_counter()
+    check(store.lib.cgs_hash_build(store.h, None), "cgs_hash_build")
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    check(store.lib.cgs_hash_build(store.h, None), "cgs_hash_build")
+    torch.cuda.synchronize()
+    t4 = time.perf_counter()
+    nb = store.nbvh()
+    alg = 0
+    for k in list(range(store.surfaces)) + [-1 - g for g in range(store.groups)]:
+        _, _, n_table, n_disp, n_keys = store.bvh_sizes(k)
+        alg += 4 * (n_keys + n_disp + n_table)
+    peaks, pk = measured_peaks()
+    hash_s = t4 - t3
+    timing = {"total_s": t3 - t0, "add_s": t1 - t0, "bvh_build_s": t2 - t1, "upload_and_hash_s": t3 - t2,
+              "hash_build_s": hash_s, "bvhs": nb,
+              "hash_roofline": {"bound": "hbm", "achieved": alg / hash_s / 1e9, "peak": peaks["hbm_gbs"],
+                                "unit": "GB/s", "frac": alg / hash_s / 1e9 / peaks["hbm_gbs"],
+                                "algorithmic_bytes": alg, "peak_source": pk,
+                                "note": "keys read + displacement and table words written, 4 B each; the build "
+                                        "is bound by its round barriers (launches, block syncs), not by bytes"}}
+    return store, timing
 
 
 def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
@@ -358,9 +442,9 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
     out = {"scenes": 64, "patches": int(sum(s.patch_count for s in scs)),
            "primary_rays": int(sum(side * side for _, side in cams)), "scene_gen_s": gen_s}
     for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_LONGEST)):
-        t0 = time.perf_counter()
-        store = rt.GpuScene(scs, device=dev.index or 0, split=split)
-        out[f"store_build_s_{split_name}"] = time.perf_counter() - t0
+        store, tm = store_build(rt, scs, dev, split)
+        out[f"store_build_s_{split_name}"] = tm["total_s"]
+        out[f"store_build_{split_name}"] = tm
         out["footprint_mb"] = store.footprint() / 2 ** 20
         reqs = [rt.Request.alloc(i, c, side, side, 1, DEPTH, device=dev.index or 0)
                 for i, (c, side) in enumerate(cams)]
@@ -433,9 +517,9 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
            "slots": slots, "memory_budget_gb": budget_gb, "scene_gen_s": gen_s, "rates": []}
     stores = {}
     for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_LONGEST)):
-        t0 = time.perf_counter()
-        stores[split_name] = rt.GpuScene(scs, device=dev.index or 0, split=split)
-        out[f"store_build_s_{split_name}"] = time.perf_counter() - t0
+        stores[split_name], tm = store_build(rt, scs, dev, split)
+        out[f"store_build_s_{split_name}"] = tm["total_s"]
+        out[f"store_build_{split_name}"] = tm
     out["footprint_mb"] = stores["reference"].footprint() / 2 ** 20
     # inputs and outputs are allocated before the timed streams
     reqs = []
@@ -678,6 +762,8 @@ def main():
         g2.close()
         if not args.no_precision:
             extra["precision"] = precision_leg(rt, scenes, torch, dev, g, scene, flush)
+        if args.scene == "c2":
+            extra["subdivision"] = subdivision_leg(rt, torch, g, cam, flush, scene, subset)
         # the traversal occupancy cap leaves room for the wavefront's overlapping
         # shadow query; the batched and served queries have no such overlap and
         # run the traversal at full occupancy

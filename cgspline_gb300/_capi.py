@@ -61,7 +61,7 @@ class Hits(C.Structure):
 
 class EngineConfig(C.Structure):
     _fields_ = [(k, C.c_int) for k in ("passes", "collect_threads", "resolve_threads", "collect_occupancy",
-                                       "resolve_occupancy", "backtrack_cache")]
+                                       "resolve_occupancy", "backtrack_cache", "compressed_nodes")]
 
 
 class ServerOptions(C.Structure):

@@ -577,7 +577,7 @@ int cgs_engine_config_get(cgs_engine_config* out)
     if (!out) return CGS_ERR_INVALID_ARGUMENT;
     const EngineConfig c = engine_config();
     *out = cgs_engine_config {c.passes, c.collectThreads, c.resolveThreads, c.collectOccupancy, c.resolveOccupancy,
-                              c.backtrackCache};
+                              c.backtrackCache, c.compressedNodes};
     return CGS_OK;
 }
 
@@ -585,7 +585,7 @@ int cgs_engine_config_set(const cgs_engine_config* in)
 {
     if (!in) return CGS_ERR_INVALID_ARGUMENT;
     const EngineConfig c {in->passes, in->collect_threads, in->resolve_threads, in->collect_occupancy,
-                          in->resolve_occupancy, in->backtrack_cache};
+                          in->resolve_occupancy, in->backtrack_cache, in->compressed_nodes};
     return set_engine_config(c) ? CGS_OK : CGS_ERR_INVALID_ARGUMENT;
 }
 
@@ -616,10 +616,11 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
         for (int ct : {128, 256})
             for (int rt : {64, 128})
                 for (int full : {1, 0})
+                    for (int cq : {0, 1})
             {
                 // traversal blocks: as many as fit, or three quarters of that (768
                 // threads per SM), which leaves room for the overlapping queries
-                const EngineConfig c {passes, ct, rt, full ? 0 : (ct == 256 ? 3 : 6), 0, saved.backtrackCache};
+                const EngineConfig c {passes, ct, rt, full ? 0 : (ct == 256 ? 3 : 6), 0, saved.backtrackCache, cq};
                 set_engine_config(c);
                 std::vector<float> ms;
                 for (int k = 0; k < repeats + 2 && status == CGS_OK; k++)
@@ -649,7 +650,8 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
     if (status != CGS_OK) return status;
     if (best)
         *best = cgs_engine_config {winner.passes, winner.collectThreads, winner.resolveThreads,
-                                   winner.collectOccupancy, winner.resolveOccupancy, winner.backtrackCache};
+                                   winner.collectOccupancy, winner.resolveOccupancy, winner.backtrackCache,
+                                   winner.compressedNodes};
     if (best_ms) *best_ms = winnerMs;
     s->lastStream = st;
     s->lastCounters = s->slot.counters.p;
@@ -670,6 +672,32 @@ int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uin
     if (!keys || !disp || !table || !params || n == 0) return CGS_ERR_INVALID_ARGUMENT;
     if (dcap < displ_size(n) || tcap < table_capacity(n)) return CGS_ERR_INVALID_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
+    if (n <= kHashGlobalBlockMaxKeys)
+    {
+        // one CTA builds the table, its scratch in shared memory up to
+        // kHashBlockMaxKeys keys, else in global memory (hash_build_blocks)
+        HashJob J {};
+        J.n = n; J.tableCap = tcap; J.mask = displ_size(n) - 1;
+        hash_coefficients(n, J.A, J.B);
+        uint32_t* dj = nullptr;
+        const size_t jobWords = (sizeof(HashJob) + 3) / 4 + 1;
+        const size_t scratch = n > kHashBlockMaxKeys ? size_t(hash_block_scratch_words(n)) + 2 : 0;
+        CGS_TRY(cudaMallocAsync(&dj, (jobWords + 8 + scratch) * sizeof(uint32_t), st));
+        uint32_t res[8] = {};
+        uint32_t* gs = scratch ? dj + ((jobWords + 8 + 1) & ~size_t(1)) : nullptr;
+        cudaError_t e = cudaMemcpyAsync(dj, &J, sizeof J, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = hash_build_blocks(keys, reinterpret_cast<const HashJob*>(dj), 1, n, disp, table, dj + jobWords, st,
+                                  gs);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(res, dj + jobWords, sizeof res, cudaMemcpyDeviceToHost, st);
+        cudaFreeAsync(dj, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return CGS_ERR_CUDA;
+        for (int k = 0; k < 5; k++) params[k] = res[1 + k];
+        if (res[0] == 4) return CGS_ERR_HASH_BUCKET_OVERFLOW;
+        if (res[0]) return CGS_ERR_HASH_FAILED;
+        return CGS_OK;
+    }
     size_t w32 = 0, w64 = 0;
     hash_scratch_words(n, w32, w64);
     uint32_t* s32 = nullptr;

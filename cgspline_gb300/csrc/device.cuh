@@ -30,6 +30,7 @@ struct DevBVH
     uint32_t nodeBase, indexBase, tableBase, dispBase;
     uint32_t A, B, N, mask;  // h(k) = (A k + B + disp[k & mask]) mod N, src/rt/PerfectHashFunction.h:58-63
     unsigned long long Nmagic;  // ceil(2^64 / N): x mod N by multiplication (fastmod_u32)
+    uint32_t compressed;        // 1: every node has a record in the compressed mirror
 };
 
 // x mod N for 32-bit x and N >= 1 with M = ceil(2^64 / N) (Lemire, Kaser,
@@ -65,6 +66,7 @@ struct DevScene
 {
     const float4* patches;
     const float4* nodes;
+    const uint4* qnodes;       // 32-byte compressed mirror of nodes (two uint4 per node)
     const uint32_t* indices;
     const uint32_t* tables;
     const uint32_t* disps;
@@ -113,6 +115,13 @@ __device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b)
 {
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
+__device__ __forceinline__ void ldg256u(const uint4* p, uint4& a, uint4& b)
+{
+    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
         : "l"(p));
 }
 
@@ -884,6 +893,53 @@ __device__ __forceinline__ bool slab(float& tMin, float3 lo, float3 hi, float3 o
     }
     tMin = tm;
     return tm < tM && tM > 0.0001f;
+}
+
+// Box tests on the compressed node mirror (32 bytes per node, written by
+// pack_qnodes in scene.cu): the entry distances of a node's two child boxes,
+// or for a leaf of its own box (left slot).  A grid byte q of an axis stands
+// for the coordinate P + q s, s = 2^(e-127); its slab distance
+// (P + q s - o) inv is evaluated as fma(2^23 + q, s inv, (P - o) inv - 2^23 s inv),
+// where 2^23 + q is q placed in a float's mantissa by a byte permute (exact,
+// no integer-to-float conversion).  Subtracting 2^23 s inv costs at most half
+// a grid step of rounding (for nodes within 2^23 grid steps of the ray's
+// origin; beyond that the rounding of (P - o) inv dominates, as it does in
+// the exact test), and the encoder widens every box by at least one step, so
+// a ray meets each decoded box wherever it meets the exact one, entering no
+// later.  A ray parallel to an axis (inv = +-inf) gets NaN distances on
+// that axis, which fmaxf / fminf skip: the axis then accepts, conservatively.
+constexpr uint32_t kQNodeLeaf = 1u;
+
+__device__ __forceinline__ void qslab_axis(uint32_t Pbits, uint32_t sbits, uint32_t q, float o, float inv,
+                                           float& tmL, float& tML, float& tmR, float& tMR)
+{
+    const float step = __uint_as_float(sbits) * inv;
+    const float base = fmaf(-8388608.0f, step, (__uint_as_float(Pbits) - o) * inv);
+    const float lLo = fmaf(__uint_as_float(__byte_perm(q, 0x4B000000u, 0x7540u)), step, base);
+    const float lHi = fmaf(__uint_as_float(__byte_perm(q, 0x4B000000u, 0x7541u)), step, base);
+    const float rLo = fmaf(__uint_as_float(__byte_perm(q, 0x4B000000u, 0x7542u)), step, base);
+    const float rHi = fmaf(__uint_as_float(__byte_perm(q, 0x4B000000u, 0x7543u)), step, base);
+    const bool s = signbit(inv);
+    tmL = fmaxf(tmL, s ? lHi : lLo);
+    tML = fminf(tML, s ? lLo : lHi);
+    tmR = fmaxf(tmR, s ? rHi : rLo);
+    tMR = fminf(tMR, s ? rLo : rHi);
+}
+
+// a = words 0-3 (origins, scale exponents, flags), b = words 4-7 (grid
+// bytes per axis, right child / first element).  Returns the two boxes'
+// entries and whether the ray meets them (the exact test's condition).
+__device__ __forceinline__ void qslab2(const uint4& a, const uint4& b, float3 o, float3 inv, float& L0, bool& iL,
+                                       float& R0, bool& iR)
+{
+    float tmL = -INFINITY, tML = INFINITY, tmR = -INFINITY, tMR = INFINITY;
+    qslab_axis(a.x, (a.w << 23) & 0x7F800000u, b.x, o.x, inv.x, tmL, tML, tmR, tMR);
+    qslab_axis(a.y, (a.w << 15) & 0x7F800000u, b.y, o.y, inv.y, tmL, tML, tmR, tMR);
+    qslab_axis(a.z, (a.w << 7) & 0x7F800000u, b.z, o.z, inv.z, tmL, tML, tmR, tMR);
+    L0 = tmL;
+    R0 = tmR;
+    iL = tmL < tML && tML > 0.0001f;
+    iR = tmR < tMR && tMR > 0.0001f;
 }
 
 // BVH::hashIntersect (src/rt/BVH.h:178-350): stackless descent that visits

@@ -90,11 +90,12 @@ Eng carve(uint32_t* base, uint32_t cap)
 
 // The BVH a lane walks: its index in the scene's BVH table and the two bases
 // every step uses.
-struct BvhRef { uint32_t idx, nodeBase, indexBase; };
+struct BvhRef { uint32_t idx, nodeBase, indexBase; bool compressed; };
 
 __device__ __forceinline__ BvhRef bvh_ref(const DevScene& S, uint32_t idx)
 {
-    return BvhRef {idx, __ldg(&S.bvhs[idx].nodeBase), __ldg(&S.bvhs[idx].indexBase)};
+    return BvhRef {idx, __ldg(&S.bvhs[idx].nodeBase), __ldg(&S.bvhs[idx].indexBase),
+                   __ldg(&S.bvhs[idx].compressed) != 0};
 }
 
 // Warp-wide refill: every lane in `need` gets the next index from *fetch.
@@ -128,7 +129,13 @@ __device__ __forceinline__ void load_ray(const RaysSoA& r, uint32_t i, float3& o
 // the same node.  `rvalid` counts the entries at the top of the ring that are
 // still intact; an object's traversal nests inside the object level's on the
 // same ring, since it leaves the object only with nothing postponed.
-template<bool kAny>
+//
+// kQ: read the 32-byte compressed node mirror (one 256-bit load; child boxes
+// on an 8-bit grid, widened outward) instead of the exact 64-byte records.
+// The decoded boxes contain the exact ones, so the walk meets every leaf the
+// exact walk meets (and a few more), with leaf entries no later: the list
+// holds the same patches plus some the resolve step then clips or culls.
+template<bool kAny, bool kQ>
 __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, RaysSoA rays, uint32_t n0,
                                                                 const uint32_t* nDev, Eng E, int pass, int cache,
                                                                 Counters* cnt)
@@ -257,22 +264,38 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         }
         else
         {
-            const float4* q = S.nodes + 4ull * (B.nodeBase + node);
-            // one round trip for the whole 64-byte node
-            float4 q0, q1, q2, q3;
-            ldg256(q, q0, q1);
-            ldg256(q + 2, q2, q3);
-            const uint32_t left = __float_as_uint(q3.x), right = __float_as_uint(q3.y);
+            // the node: its compressed record (one 256-bit load) where the BVH
+            // has them, else the exact 64-byte record (two); the box tests of
+            // an inner node's children, or of a leaf's own box when the leaf
+            // was reached through a backtrack
             const float3 ro = co, ri = ci;
+            uint32_t left, right;
+            float L0 = 0.0f, R0 = 0.0f;
+            bool mL = false, mR = false;
+            if (kQ && B.compressed)
+            {
+                uint4 qa, qb;
+                ldg256u(S.qnodes + 2ull * (B.nodeBase + node), qa, qb);
+                const bool isLeaf = ((qa.w >> 24) & kQNodeLeaf) != 0;
+                left = isLeaf ? EMPTY : node + 1;
+                right = qb.w;
+                if (!isLeaf || jumped) qslab2(qa, qb, ro, ri, L0, mL, R0, mR);
+            }
+            else
+            {
+                const float4* q = S.nodes + 4ull * (B.nodeBase + node);
+                float4 q0, q1, q2, q3;
+                ldg256(q, q0, q1);
+                ldg256(q + 2, q2, q3);
+                left = __float_as_uint(q3.x);
+                right = __float_as_uint(q3.y);
+                if (left != EMPTY || jumped) mL = slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), ro, ri);
+                if (left != EMPTY) mR = slab(R0, f3(q1.z, q1.w, q2.x), f3(q2.y, q2.z, q2.w), ro, ri);
+            }
             if (left == EMPTY)
             {
-                if (jumped)
-                {
-                    // reached through the hash: its entry is the slab test of its own box
-                    float L0;
-                    slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), ro, ri);
-                    leafEntry = L0;
-                }
+                // reached through a backtrack: its entry is the slab test of its own box
+                if (jumped) leafEntry = L0;
                 jumped = false;
                 // the leaf's first element and the one after it in the same step: a
                 // one-element leaf (the build's element count per leaf) is done here
@@ -314,9 +337,8 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
                 lc.nodes++;
                 jumped = false;
                 const float lim = clim;
-                float L0, R0;
-                const bool iL = slab(L0, f3(q0.x, q0.y, q0.z), f3(q0.w, q1.x, q1.y), ro, ri) && L0 < lim;
-                const bool iR = slab(R0, f3(q1.z, q1.w, q2.x), f3(q2.y, q2.z, q2.w), ro, ri) && R0 < lim;
+                const bool iL = mL && L0 < lim;
+                const bool iR = mR && R0 < lim;
                 if (iL || iR) post <<= 1;
                 if (iL && iR)
                 {
@@ -592,13 +614,26 @@ int resident(const void* fn, int threads)
 
 // Resident blocks per SM of kernel fn at `threads` per block (cached: the
 // values depend only on the kernel and the block size).
-template<bool kAny, bool kG64> int per_sm(bool collect, int threads)
+template<bool kAny, bool kG64> int per_sm(bool collect, int threads, bool compressed = true)
 {
-    static const int v[2][2] = {
-        {resident((const void*)k_collect<kAny>, 128) / sms(), resident((const void*)k_collect<kAny>, 256) / sms()},
+    static const int v[3][2] = {
+        {resident((const void*)k_collect<kAny, false>, 128) / sms(),
+         resident((const void*)k_collect<kAny, false>, 256) / sms()},
         {resident((const void*)k_resolve<kAny, kG64>, 64) / sms(),
-         resident((const void*)k_resolve<kAny, kG64>, 128) / sms()}};
-    return collect ? v[0][threads == 256] : v[1][threads == 128];
+         resident((const void*)k_resolve<kAny, kG64>, 128) / sms()},
+        {resident((const void*)k_collect<kAny, true>, 128) / sms(),
+         resident((const void*)k_collect<kAny, true>, 256) / sms()}};
+    return collect ? v[compressed ? 2 : 0][threads == 256] : v[1][threads == 128];
+}
+
+template<bool kAny>
+void launch_collect(int grid, int threads, cudaStream_t stream, const DevScene& S, RaysSoA rays, uint32_t n,
+                    const uint32_t* nDev, Eng E, int pass, const EngineConfig& c, Counters* cnt)
+{
+    if (c.compressedNodes)
+        k_collect<kAny, true><<<grid, threads, 0, stream>>>(S, rays, n, nDev, E, pass, c.backtrackCache, cnt);
+    else
+        k_collect<kAny, false><<<grid, threads, 0, stream>>>(S, rays, n, nDev, E, pass, c.backtrackCache, cnt);
 }
 
 template<bool kAny, bool kG64>
@@ -607,7 +642,7 @@ void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Q
 {
     const EngineConfig c = engine_config();
     const int ct = c.collectThreads, rt = c.resolveThreads;
-    const int pc = per_sm<kAny, kG64>(true, ct), pr = per_sm<kAny, kG64>(false, rt);
+    const int pc = per_sm<kAny, kG64>(true, ct, c.compressedNodes != 0), pr = per_sm<kAny, kG64>(false, rt);
     const int cb = sms() * std::max(1, c.collectOccupancy ? std::min(c.collectOccupancy, pc) : pc);
     const int rb = sms() * std::max(1, c.resolveOccupancy ? std::min(c.resolveOccupancy, pr) : pr);
     const uint32_t warps = (n + 31) / 32;
@@ -615,7 +650,7 @@ void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Q
     const int gr = int(std::min<uint32_t>(uint32_t(rb), warps / (rt / 32) + 1));
     for (int p = 0; p < c.passes; p++)
     {
-        k_collect<kAny><<<gc, ct, 0, stream>>>(S, rays, n, nDev, E, p, c.backtrackCache, cnt);
+        launch_collect<kAny>(gc, ct, stream, S, rays, n, nDev, E, p, c, cnt);
         k_resolve<kAny, kG64><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
         nl += 2;
     }
@@ -647,7 +682,8 @@ bool valid_engine_config(const EngineConfig& c)
 {
     return c.passes >= 1 && c.passes <= kMaxPasses && (c.collectThreads == 128 || c.collectThreads == 256) &&
            (c.resolveThreads == 64 || c.resolveThreads == 128) && c.collectOccupancy >= 0 && c.collectOccupancy <= 32 &&
-           c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1);
+           c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
+           (c.compressedNodes == 0 || c.compressedNodes == 1);
 }
 
 bool set_engine_config(const EngineConfig& c)
@@ -704,11 +740,12 @@ cudaError_t run_traverse(const DevScene& S, RaysSoA rays, uint32_t n, bool any, 
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const EngineConfig c = engine_config();
     const int ct = c.collectThreads;
-    const int pc = any ? per_sm<true, false>(true, ct) : per_sm<false, false>(true, ct);
+    const bool cq = c.compressedNodes != 0;
+    const int pc = any ? per_sm<true, false>(true, ct, cq) : per_sm<false, false>(true, ct, cq);
     const int cb = sms() * std::max(1, c.collectOccupancy ? std::min(c.collectOccupancy, pc) : pc);
     const int gc = int(std::min<uint32_t>(uint32_t(cb), (n + 31) / 32 / (ct / 32) + 1));
-    if (any) k_collect<true><<<gc, ct, 0, stream>>>(S, rays, n, nullptr, E, 0, c.backtrackCache, cnt);
-    else k_collect<false><<<gc, ct, 0, stream>>>(S, rays, n, nullptr, E, 0, c.backtrackCache, cnt);
+    if (any) launch_collect<true>(gc, ct, stream, S, rays, n, nullptr, E, 0, c, cnt);
+    else launch_collect<false>(gc, ct, stream, S, rays, n, nullptr, E, 0, c, cnt);
     if (launches) *launches += 1;
     if (listLengths) cudaMemcpyAsync(listLengths, E.count, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, stream);
     return cudaGetLastError();

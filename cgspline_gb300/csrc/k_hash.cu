@@ -14,6 +14,7 @@
 // a pure function of the keys.  Each round is two kernel launches (bid,
 // commit); there is no device-wide barrier and no spin-wait.
 #include <atomic>
+#include <type_traits>
 #include <algorithm>
 
 #include "kernels.h"
@@ -24,6 +25,7 @@ namespace {
 
 constexpr uint32_t kCap = 4;
 constexpr int kThreads = 256;
+constexpr int kBlockThreads = 1024;  // one CTA per small BVH
 constexpr int kRankChunk = 4096;  // buckets per rank block (counts fit 16 bits)
 
 enum : uint32_t { kActive = 1u, kFeasible = 2u };
@@ -245,6 +247,231 @@ int device_sms()
     return sms;
 }
 
+// ------------------------------------------------------- one CTA per BVH --
+// The same build for one BVH run entirely by one CTA: the bid and commit
+// phases of a round are separated by __syncthreads instead of kernel
+// launches, and a whole store's BVHs are built by one launch, one CTA each,
+// with no host round trip between trials.  Up to kHashBlockMaxKeys keys the
+// buckets, ranks, displacements, slot owners and occupancy bitmap live in
+// shared memory (kShared); up to kHashGlobalBlockMaxKeys in a global scratch
+// area per BVH (mostly L2-resident).  The rounds, ranks, tie rule (lowest
+// rank wins a slot) and displacement steps are those of k_bid / k_commit,
+// so the tables are the same.  Slot owners are tags with the round in the
+// high half and the rank in the low half: 16 + 16 bits in shared memory
+// (rounds < 2^11, ranks < 2^16 there), 32 + 32 bits in global memory.
+struct BlockScratchLayout
+{
+    uint32_t* bkeys;  // [4 nb]
+    uint32_t* dcur;   // [nb]
+    uint32_t* bsize;  // [nb]
+    uint32_t* rank;   // [nb]
+    uint32_t* state;  // [nb]: bit 0 active, bit 1 feasible
+    uint32_t* occ;    // [ceil(nmax / 32)]
+    void* owner;      // [nmax] tags
+};
+
+// Words of a global scratch area for a BVH of n keys (owner tags 64-bit).
+__host__ __device__ inline uint64_t block_scratch_words(uint32_t nb, uint32_t nmax)
+{
+    return 8ull * nb + (nmax + 31) / 32 + 1 + 2ull * nmax;  // +1: 8-byte alignment of the tags
+}
+
+__device__ __forceinline__ uint4 warp_incl_scan4(uint4 v)
+{
+    for (int off = 1; off < 32; off <<= 1)
+    {
+        uint4 u;
+        u.x = __shfl_up_sync(0xFFFFFFFFu, v.x, off);
+        u.y = __shfl_up_sync(0xFFFFFFFFu, v.y, off);
+        u.z = __shfl_up_sync(0xFFFFFFFFu, v.z, off);
+        u.w = __shfl_up_sync(0xFFFFFFFFu, v.w, off);
+        if ((threadIdx.x & 31) >= uint32_t(off)) { v.x += u.x; v.y += u.y; v.z += u.z; v.w += u.w; }
+    }
+    return v;
+}
+
+template<bool kShared>
+__global__ void __launch_bounds__(kBlockThreads) k_hash_block(const uint32_t* __restrict__ keys,
+                                                              const HashJob* __restrict__ jobs, uint32_t* disps,
+                                                              uint32_t* tables, uint32_t* out, uint32_t nbMax,
+                                                              uint32_t nmaxMax, uint32_t* gscratch)
+{
+    using Tag = typename std::conditional<kShared, uint32_t, unsigned long long>::type;
+    extern __shared__ __align__(16) uint32_t sm[];
+    __shared__ uint32_t sErr, sFail, sCount[4], sRemain[4];
+    __shared__ uint4 sWarp[kBlockThreads / 32];
+    const HashJob& J = jobs[blockIdx.x];
+    const uint32_t n = J.n, mask = J.mask, nb = mask + 1;
+    const uint32_t step = max(4u, uint32_t(0.05f * float(n)));
+    BlockScratchLayout L;
+    {
+        const uint32_t nbs = kShared ? nbMax : nb;
+        const uint32_t nms = kShared ? nmaxMax : n + 16u * step;
+        uint32_t* p = kShared ? sm : gscratch + J.scratchOff;
+        L.bkeys = p; p += 4ull * nbs;
+        L.dcur = p; p += nbs;
+        L.bsize = p; p += nbs;
+        L.rank = p; p += nbs;
+        L.state = p; p += nbs;
+        L.occ = p; p += (nms + 31) / 32;
+        if (!kShared && (reinterpret_cast<uintptr_t>(p) & 7u)) p++;
+        L.owner = p;
+    }
+    uint32_t *bkeys = L.bkeys, *dcur = L.dcur, *bsize = L.bsize, *rank = L.rank, *state = L.state, *occ = L.occ;
+    Tag* owner = static_cast<Tag*>(L.owner);
+    const uint32_t tid = threadIdx.x, bd = blockDim.x;
+    uint32_t* res = out + 8ull * blockIdx.x;
+
+    for (uint32_t b = tid; b < nb; b += bd) bsize[b] = 0;
+    if (tid == 0) { sErr = 0; sFail = 0; }
+    __syncthreads();
+    for (uint32_t i = tid; i < n; i += bd)
+    {
+        const uint32_t key = keys[J.keyOff + i], j = key & mask;
+        const uint32_t s = atomicAdd(bsize + j, 1u);
+        if (s >= kCap) atomicOr(&sErr, kErrOverflow);  // reference: __trap()
+        else bkeys[kCap * j + s] = key;
+    }
+    __syncthreads();
+    if (sErr)
+    {
+        // as hash_build_device reports a bucket overflow (found in trial 0)
+        if (tid == 0) { res[0] = 4; res[1] = J.A[0]; res[2] = J.B[0]; res[3] = n; res[4] = mask; res[5] = 0; }
+        return;
+    }
+
+    // rank[b]: buckets b' < b of the same size; contiguous buckets per thread,
+    // the four classes' counts scanned block-wide
+    const uint32_t per = (nb + bd - 1) / bd, b0 = tid * per;
+    uint4 local = make_uint4(0, 0, 0, 0);
+    for (uint32_t k = 0; k < per && b0 + k < nb; k++)
+    {
+        const uint32_t sz = bsize[b0 + k];
+        local.x += sz == 1; local.y += sz == 2; local.z += sz == 3; local.w += sz == 4;
+    }
+    const uint4 incl = warp_incl_scan4(local);
+    if ((tid & 31) == 31) sWarp[tid >> 5] = incl;
+    __syncthreads();
+    if (tid < 32)
+    {
+        const uint32_t nw = bd >> 5;
+        const uint4 w = tid < nw ? sWarp[tid] : make_uint4(0, 0, 0, 0);
+        const uint4 wi = warp_incl_scan4(w);
+        if (tid < nw) sWarp[tid] = make_uint4(wi.x - w.x, wi.y - w.y, wi.z - w.z, wi.w - w.w);
+        if (tid == 31) { sCount[0] = wi.x; sCount[1] = wi.y; sCount[2] = wi.z; sCount[3] = wi.w; }
+    }
+    __syncthreads();
+    {
+        const uint4 wb = sWarp[tid >> 5];
+        uint32_t run[4] = {wb.x + incl.x - local.x, wb.y + incl.y - local.y, wb.z + incl.z - local.z,
+                           wb.w + incl.w - local.w};
+        for (uint32_t k = 0; k < per && b0 + k < nb; k++)
+        {
+            const uint32_t b = b0 + k, sz = bsize[b];
+            rank[b] = (sz >= 1 && sz <= kCap) ? run[sz - 1]++ : 0u;
+        }
+    }
+
+    uint32_t N = n, trial = 0, A = 0, B = 0;
+    bool ok = false;
+    for (trial = 0; trial < 16; trial++)
+    {
+        A = J.A[trial];
+        B = J.B[trial];
+        for (uint32_t w = tid; w < (N + 31) / 32; w += bd) occ[w] = 0;
+        for (uint32_t w = tid; w < N; w += bd) owner[w] = Tag(~Tag(0));
+        for (uint32_t b = tid; b < nb; b += bd)
+        {
+            dcur[b] = 0;
+            state[b] = (bsize[b] >= 1 && bsize[b] <= kCap) ? kActive : 0u;
+        }
+        if (tid == 0)
+        {
+            sFail = 0;
+            for (int c = 0; c < 4; c++) sRemain[c] = sCount[c];
+        }
+        __syncthreads();
+        for (uint32_t cls = kCap; cls >= 1; cls--)
+        {
+            if (sCount[cls - 1] == 0) continue;
+            for (uint32_t r = 0; r < 32; r++)
+            {
+                const uint32_t round = trial * 128u + (kCap - cls) * 32u + r;
+                const Tag tagHi = kShared ? Tag(0xFFFFu - round) << 16 : Tag(0xFFFFFFFFu - round) << 32;
+                for (uint32_t b = tid; b < nb; b += bd)
+                {
+                    if (bsize[b] != cls || !(state[b] & kActive)) continue;
+                    uint32_t sl[kCap];
+                    bool f = true;
+                    for (uint32_t k = 0; k < cls; k++)
+                    {
+                        sl[k] = (A * bkeys[kCap * b + k] + B + dcur[b]) % N;
+                        if (occ[sl[k] >> 5] & (1u << (sl[k] & 31))) f = false;
+                        for (uint32_t m = 0; m < k; m++) if (sl[m] == sl[k]) f = false;
+                    }
+                    state[b] = f ? (kActive | kFeasible) : kActive;
+                    if (f)
+                        for (uint32_t k = 0; k < cls; k++) atomicMin(owner + sl[k], tagHi | Tag(rank[b]));
+                }
+                __syncthreads();
+                for (uint32_t b = tid; b < nb; b += bd)
+                {
+                    if (bsize[b] != cls || !(state[b] & kActive)) continue;
+                    bool win = (state[b] & kFeasible) != 0;
+                    uint32_t sl[kCap];
+                    for (uint32_t k = 0; k < cls; k++)
+                    {
+                        sl[k] = (A * bkeys[kCap * b + k] + B + dcur[b]) % N;
+                        if (win && owner[sl[k]] != (tagHi | Tag(rank[b]))) win = false;
+                    }
+                    if (win)
+                    {
+                        for (uint32_t k = 0; k < cls; k++) atomicOr(occ + (sl[k] >> 5), 1u << (sl[k] & 31));
+                        state[b] = 0;
+                        atomicSub(sRemain + cls - 1, 1u);
+                    }
+                    else
+                    {
+                        dcur[b] += rank[b] + 1;
+                        if (r == 31) atomicAdd(&sFail, 1u);
+                    }
+                }
+                __syncthreads();
+                if (sRemain[cls - 1] == 0) break;
+            }
+        }
+        __syncthreads();
+        if (sFail == 0) { ok = true; break; }
+        N += step;
+        __syncthreads();
+    }
+    if (!ok)
+    {
+        // as hash_build_device reports a failed build: the last trial's
+        // coefficients and the table size grown past it
+        if (tid == 0)
+        {
+            res[0] = 3; res[1] = J.A[15]; res[2] = J.B[15]; res[3] = N; res[4] = mask; res[5] = 16;
+        }
+        return;
+    }
+    uint32_t* table = tables + J.tableOff;
+    for (uint32_t b = tid; b < nb; b += bd) disps[J.dispOff + b] = dcur[b];
+    for (uint32_t w = tid; w < N; w += bd) table[w] = EMPTY;
+    __syncthreads();
+    for (uint32_t i = tid; i < n; i += bd)
+    {
+        const uint32_t key = keys[J.keyOff + i];
+        const uint32_t h = (A * key + B + dcur[key & mask]) % N;
+        if (atomicCAS(table + h, EMPTY, i) != EMPTY) atomicOr(&sErr, kErrDuplicate);
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+        res[0] = sErr ? 5u : 0u; res[1] = A; res[2] = B; res[3] = N; res[4] = mask; res[5] = trial;
+    }
+}
+
 int grid_for(uint64_t items, int threads)
 {
     const int sms = device_sms();
@@ -347,6 +574,55 @@ int hash_build_device(const uint32_t* keys, uint32_t n, const uint32_t A[16], co
     if (cudaStreamSynchronize(stream) != cudaSuccess) return -1;
     if (host[M_ERR] & kErrDuplicate) return 5;
     return 0;
+}
+
+
+namespace {
+
+void block_sizes(uint32_t n, uint32_t& nb, uint32_t& nmax)
+{
+    n = std::max<uint32_t>(n, 1u);
+    int sh = int(n - 1) >> 1;
+    if (sh < 2) sh = 2;
+    nb = bit_floor_u32(uint32_t(sh));
+    const uint32_t step = std::max<uint32_t>(4u, uint32_t(0.05f * float(n)));
+    nmax = n + 16u * step;
+}
+
+}  // namespace
+
+size_t hash_block_smem(uint32_t maxKeys)
+{
+    uint32_t nb = 0, nmax = 0;
+    block_sizes(maxKeys, nb, nmax);
+    return sizeof(uint32_t) * (8ull * nb + nmax + (nmax + 31) / 32);
+}
+
+uint64_t hash_block_scratch_words(uint32_t n)
+{
+    uint32_t nb = 0, nmax = 0;
+    block_sizes(n, nb, nmax);
+    return block_scratch_words(nb, nmax);
+}
+
+cudaError_t hash_build_blocks(const uint32_t* keys, const HashJob* jobs, uint32_t njobs, uint32_t maxKeys,
+                              uint32_t* disps, uint32_t* tables, uint32_t* out, cudaStream_t stream,
+                              uint32_t* gscratch)
+{
+    if (njobs == 0) return cudaSuccess;
+    if (maxKeys > kHashGlobalBlockMaxKeys || (maxKeys > kHashBlockMaxKeys && !gscratch)) return cudaErrorInvalidValue;
+    if (maxKeys > kHashBlockMaxKeys)
+    {
+        k_hash_block<false><<<njobs, kBlockThreads, 0, stream>>>(keys, jobs, disps, tables, out, 0, 0, gscratch);
+        return cudaGetLastError();
+    }
+    uint32_t nb = 0, nmax = 0;
+    block_sizes(maxKeys, nb, nmax);
+    const size_t smem = hash_block_smem(maxKeys);
+    cudaError_t e = cudaFuncSetAttribute(k_hash_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    k_hash_block<true><<<njobs, kBlockThreads, smem, stream>>>(keys, jobs, disps, tables, out, nb, nmax, nullptr);
+    return cudaGetLastError();
 }
 
 }  // namespace cgs

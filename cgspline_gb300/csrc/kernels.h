@@ -81,6 +81,7 @@ struct EngineConfig
     int collectOccupancy = 0;
     int resolveOccupancy = 0;
     int backtrackCache = 1;  // 1: backtracks read postponed siblings from a per-lane ring first
+    int compressedNodes = 0; // 1: the traversal reads the 32-byte compressed node mirror
 };
 EngineConfig engine_config();
 bool set_engine_config(const EngineConfig& c);
@@ -179,6 +180,31 @@ struct HashScratch
 // Sizes of the scratch for n keys (in 4-byte words, owner in 8-byte words).
 void hash_scratch_words(uint32_t n, size_t& words32, size_t& words64);
 void hash_scratch_carve(HashScratch& s, uint32_t n, uint32_t* base32, unsigned long long* base64);
+
+// One BVH's build in a batch (hash_build_blocks): its keys at
+// keys[keyOff..keyOff+n), displacements written at disps[dispOff..+mask+1),
+// table at tables[tableOff..+tableCap), the 16 trials' coefficients; a
+// BVH above kHashBlockMaxKeys keys works in gscratch[scratchOff..+
+// hash_block_scratch_words(n)).
+struct HashJob
+{
+    uint32_t keyOff, n, dispOff, tableOff, tableCap, mask, scratchOff, pad;
+    uint32_t A[16], B[16];
+};
+constexpr uint32_t kHashBlockMaxKeys = 8192;          // one CTA, scratch in shared memory
+constexpr uint32_t kHashGlobalBlockMaxKeys = 131072;  // one CTA, scratch in global memory
+// Dynamic shared memory of the CTA that builds a BVH of maxKeys keys.
+size_t hash_block_smem(uint32_t maxKeys);
+// Global scratch words of the CTA that builds a BVH of n keys (above kHashBlockMaxKeys).
+uint64_t hash_block_scratch_words(uint32_t n);
+// Builds every job's table, one CTA each, in one launch (asynchronous):
+// all jobs at most kHashBlockMaxKeys keys (shared-memory scratch), or all in
+// (kHashBlockMaxKeys, kHashGlobalBlockMaxKeys] with gscratch.  out[8 j ..]:
+// status (0 ok, 3 no trial found a table, 4 bucket overflow, 5 duplicate
+// slot), A, B, N, mask, trial -- the values hash_build_device returns.
+cudaError_t hash_build_blocks(const uint32_t* keys, const HashJob* jobs, uint32_t njobs, uint32_t maxKeys,
+                              uint32_t* disps, uint32_t* tables, uint32_t* out, cudaStream_t stream,
+                              uint32_t* gscratch = nullptr);
 
 // Deterministic perfect hash of keys[0..n).  A[], B[] are the 16 trials'
 // coefficients, drawn on the host.  Writes disp[displSize] and

@@ -1,7 +1,10 @@
 // scene.cu -- the scene store of libcgspline_gb300.so: surfaces, objects and
 // groups, the host BVH build, device upload, the perfect-hash build of every
 // BVH, and the C ABI entry points that build and inspect a store.
+#include <atomic>
 #include <bit>
+#include <thread>
+#include <cmath>
 #include <numeric>
 #include <random>
 
@@ -184,6 +187,112 @@ void pack_nodes(const HostBVH& b, std::vector<float4>& out)
     }
 }
 
+// ------------------------------------------------- compressed node mirror --
+// A device-only copy of every BVH node in 32 bytes (one 256-bit load, one
+// 32-byte sector) next to the exact 64-byte record, for the traversal
+// kernel.  The child boxes are stored as 8-bit offsets on a per-axis grid
+// (the compressed-wide-BVH encoding of Ylitie, Karras and Laine, HPG 2017,
+// for binary nodes):
+//
+//   words 0-2  origin P (float) per axis
+//   word  3    bytes 0-2: e per axis (grid step s = 2^(e-127)); byte 3: flags
+//              (bit 0: leaf)
+//   words 4-6  per axis the bytes (left lo, left hi, right lo, right hi); a
+//              leaf keeps its own box in the left bytes
+//   word  7    right child (inner node; the left child is the next node in
+//              pre-order) or the leaf's first element index
+//
+// A byte q stands for the coordinate P + q s.  Every child box is widened on
+// the grid by at least one step beyond its exact bounds (lo' <= lo - s,
+// hi' >= hi + s), which covers the half-step rounding of the traversal's
+// decode, so the decoded boxes contain the exact ones: a ray meets every box
+// the exact test meets, at an entry distance no larger than the exact one.
+// The traversal then visits the same leaves (and a few more) and finds the
+// same hits.  A BVH with a node that has no such record (a non-finite box
+// coordinate, an extent no grid of 2^-126..2^127 covers, or a left child
+// that does not follow its parent, as a loaded blob may have) is read from
+// the exact records only.
+namespace {
+
+constexpr uint32_t kQLeaf = 1u;
+
+float round_down_float(double x)
+{
+    float f = float(x);
+    if (double(f) > x) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+
+// Grid of one axis of a node covering [lo, hi] with a two-step margin below
+// lo and at least two steps above hi inside 255 steps.  False if none.
+bool axis_grid(double lo, double hi, float& P, int& e)
+{
+    if (!std::isfinite(lo) || !std::isfinite(hi) || hi < lo) return false;
+    // the smallest e with 250 s >= extent, from the binary exponent of
+    // extent / 250 (then checked upward)
+    const double extent = hi - lo;
+    int e0 = extent > 0.0 ? std::max(1, std::ilogb(extent / 250.0) + 127) : 1;
+    while (e0 < 254 && std::ldexp(250.0, e0 - 127) < extent) e0++;
+    for (e = e0; e <= 254; e++)
+    {
+        const double s = std::ldexp(1.0, e - 127);
+        P = round_down_float(lo - 2.0 * s);
+        if (!std::isfinite(P)) return false;
+        if ((hi - double(P)) / s <= 253.0) return true;
+    }
+    return false;
+}
+
+}  // namespace
+
+// Appends the BVH's compressed records (two uint4 per node); false, with
+// zero records written for the failing node on, if a node has none.
+bool pack_qnodes(const HostBVH& b, std::vector<uint4>& out)
+{
+    bool all = true;
+    for (size_t i = 0; i < b.nodes.size(); i++)
+    {
+        const Node& n = b.nodes[i];
+        const bool leaf = n.left == EMPTY;
+        uint32_t w[8] = {};
+        // the compressed record names only the right child: the left one must follow
+        bool ok = leaf || n.left == i + 1;
+        uint32_t bytes[3] = {}, ex[3] = {};
+        for (int a = 0; a < 3 && ok; a++)
+        {
+            const Box& L = n.leftBox;
+            const Box& R = n.rightBox;
+            const double lo = leaf ? double(L.lo[a]) : std::min(double(L.lo[a]), double(R.lo[a]));
+            const double hi = leaf ? double(L.hi[a]) : std::max(double(L.hi[a]), double(R.hi[a]));
+            float P = 0;
+            int e = 0;
+            if (!axis_grid(lo, hi, P, e)) { ok = false; break; }
+            const double s = std::ldexp(1.0, e - 127);
+            auto qlo = [&](double c) { return std::ceil((c - double(P)) / s) - 2.0; };
+            auto qhi = [&](double c) { return std::floor((c - double(P)) / s) + 2.0; };
+            const double q[4] = {qlo(L.lo[a]), qhi(L.hi[a]), leaf ? 0.0 : qlo(R.lo[a]), leaf ? 0.0 : qhi(R.hi[a])};
+            for (double v : q) if (!(v >= 0.0 && v <= 255.0)) ok = false;
+            if (!ok) break;
+            std::memcpy(&w[a], &P, 4);
+            ex[a] = uint32_t(e);
+            bytes[a] = uint32_t(q[0]) | (uint32_t(q[1]) << 8) | (uint32_t(q[2]) << 16) | (uint32_t(q[3]) << 24);
+        }
+        if (!ok)
+        {
+            all = false;
+            w[0] = w[1] = w[2] = 0;
+            ex[0] = ex[1] = ex[2] = 127;
+            bytes[0] = bytes[1] = bytes[2] = 0;
+        }
+        w[3] = ex[0] | (ex[1] << 8) | (ex[2] << 16) | ((leaf ? kQLeaf : 0u) << 24);
+        w[4] = bytes[0]; w[5] = bytes[1]; w[6] = bytes[2];
+        w[7] = n.right;
+        out.push_back(make_uint4(w[0], w[1], w[2], w[3]));
+        out.push_back(make_uint4(w[4], w[5], w[6], w[7]));
+    }
+    return all;
+}
+
 // Lights of all groups, concatenated; groupLights[g] = (first, count);
 // groupEnv[g] = background rgb, ambient rgb.
 int upload_lights(cgs_scene* sc)
@@ -214,6 +323,7 @@ int cgs::upload_store(cgs_scene* sc)
 {
     const uint32_t nb = sc->nbvh();
     std::vector<float4> hp, hn;
+    std::vector<uint4> hq;
     std::vector<uint32_t> hi, pbase, pmat, gtop;
     std::vector<DevMaterial> hm;
     std::vector<DevObject> ho;
@@ -227,6 +337,7 @@ int cgs::upload_store(cgs_scene* sc)
         d.nodeBase = uint32_t(hn.size() / 4);
         d.indexBase = uint32_t(hi.size());
         pack_nodes(b, hn);
+        d.compressed = pack_qnodes(b, hq) ? 1u : 0u;
         hi.insert(hi.end(), b.indices.begin(), b.indices.end());
         uint32_t n = uint32_t(b.keys.size());
         d.tableBase = tableCursor;
@@ -270,6 +381,7 @@ int cgs::upload_store(cgs_scene* sc)
     }
     CGS_TRY(sc->patches.reserve(hp.size()));
     CGS_TRY(sc->nodes.reserve(hn.size()));
+    CGS_TRY(sc->qnodes.reserve(hq.size()));
     CGS_TRY(sc->indices.reserve(hi.size()));
     CGS_TRY(sc->tables.reserve(tableCursor));
     CGS_TRY(sc->disps.reserve(dispCursor));
@@ -282,6 +394,7 @@ int cgs::upload_store(cgs_scene* sc)
     CGS_TRY(sc->counters.reserve(1));
     CGS_TRY(cudaMemcpy(sc->patches.p, hp.data(), hp.size() * sizeof(float4), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->nodes.p, hn.data(), hn.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CGS_TRY(cudaMemcpy(sc->qnodes.p, hq.data(), hq.size() * sizeof(uint4), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->indices.p, hi.data(), hi.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CGS_TRY(cudaMemcpy(sc->patchBase.p, pbase.data(), pbase.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     if (!pmat.empty())
@@ -301,33 +414,118 @@ namespace {
 int upload(cgs_scene* sc) { return upload_store(sc); }
 
 // BVH::buildHashTable (src/rt/BVH.cpp:24-39) for every BVH of the store.
+// BVHs of at most kHashBlockMaxKeys keys (most: one per surface) are built
+// together, one CTA each with its scratch in shared memory, in one launch;
+// those of at most kHashGlobalBlockMaxKeys likewise with a global scratch
+// area each, in a second launch; one host round trip reads both launches'
+// results.  Larger BVHs run the multi-launch build one at a time.
 int hash_all(cgs_scene* sc, cudaStream_t stream)
 {
     const uint32_t nb = sc->nbvh();
-    uint32_t maxn = 1;
-    for (uint32_t k = 0; k < nb; k++) maxn = std::max<uint32_t>(maxn, uint32_t(sc->bvh(k).keys.size()));
-    size_t w32 = 0, w64 = 0;
-    hash_scratch_words(maxn, w32, w64);
-    CGS_TRY(sc->scratch32.reserve(w32));
-    CGS_TRY(sc->scratch64.reserve(w64));
-    CGS_TRY(sc->keys.reserve(maxn));
+    std::vector<uint32_t> small, mid, large;
+    uint32_t maxSmall = 1, maxMid = 1, maxLarge = 1;
+    size_t blockKeys = 0;
+    uint64_t midScratch = 0;
     for (uint32_t k = 0; k < nb; k++)
     {
-        const HostBVH& b = sc->bvh(k);
-        uint32_t n = uint32_t(b.keys.size());
-        HashScratch hs {};
-        hash_scratch_carve(hs, n, sc->scratch32.p, sc->scratch64.p);
-        CGS_TRY(cudaMemcpyAsync(sc->keys.p, b.keys.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
-        uint32_t A[16], B[16], params[5];
-        hash_coefficients(n, A, B);
-        DevBVH& d = sc->hbvh[k];
-        int r = hash_build_device(sc->keys.p, n, A, B, sc->disps.p + d.dispBase, sc->tables.p + d.tableBase,
-                                  sc->tableCap[k], hs, params, stream, &sc->launches);
-        if (r == 4) return CGS_ERR_HASH_BUCKET_OVERFLOW;
-        if (r < 0) return CGS_ERR_CUDA;
-        if (r) return CGS_ERR_HASH_FAILED;
-        d.A = params[0]; d.B = params[1]; d.N = params[2]; d.mask = params[3];
-        d.Nmagic = fastmod_magic(d.N);
+        const uint32_t n = uint32_t(sc->bvh(k).keys.size());
+        if (n <= kHashBlockMaxKeys) { small.push_back(k); maxSmall = std::max(maxSmall, n); blockKeys += n; }
+        else if (n <= kHashGlobalBlockMaxKeys)
+        {
+            mid.push_back(k);
+            maxMid = std::max(maxMid, n);
+            blockKeys += n;
+            midScratch += hash_block_scratch_words(n) + 1;
+        }
+        else { large.push_back(k); maxLarge = std::max(maxLarge, n); }
+    }
+    CGS_TRY(sc->keys.reserve(std::max<size_t>({blockKeys, size_t(maxLarge), 1})));
+    if (!small.empty() || !mid.empty())
+    {
+        std::vector<uint32_t> hk;
+        hk.reserve(blockKeys);
+        std::vector<HashJob> jobs(small.size() + mid.size());
+        uint64_t scratchCursor = 0;
+        for (size_t j = 0; j < jobs.size(); j++)
+        {
+            const uint32_t k = j < small.size() ? small[j] : mid[j - small.size()];
+            const HostBVH& b = sc->bvh(k);
+            const uint32_t n = uint32_t(b.keys.size());
+            HashJob& J = jobs[j];
+            J.keyOff = uint32_t(hk.size());
+            J.n = n;
+            J.dispOff = sc->hbvh[k].dispBase;
+            J.tableOff = sc->hbvh[k].tableBase;
+            J.tableCap = sc->tableCap[k];
+            J.mask = displ_size(n) - 1;
+            J.scratchOff = 0;
+            J.pad = 0;
+            if (j >= small.size())
+            {
+                if (scratchCursor > 0xFFFFFFFFull) return CGS_ERR_OUT_OF_MEMORY;
+                J.scratchOff = uint32_t(scratchCursor);
+                scratchCursor += (hash_block_scratch_words(n) + 2) & ~1ull;  // keep 8-byte alignment
+            }
+            hash_coefficients(n, J.A, J.B);
+            hk.insert(hk.end(), b.keys.begin(), b.keys.end());
+        }
+        const size_t jobWords = (jobs.size() * sizeof(HashJob) + 3) / 4;
+        CGS_TRY(sc->hashJobs.reserve(jobWords + 8 * jobs.size()));
+        if (!mid.empty()) CGS_TRY(sc->scratch32.reserve(std::max<uint64_t>(scratchCursor, 1)));
+        uint32_t* dJobs = sc->hashJobs.p;
+        uint32_t* dOut = sc->hashJobs.p + jobWords;
+        CGS_TRY(cudaMemcpyAsync(sc->keys.p, hk.data(), hk.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+        CGS_TRY(cudaMemcpyAsync(dJobs, jobs.data(), jobs.size() * sizeof(HashJob), cudaMemcpyHostToDevice, stream));
+        const HashJob* dj = reinterpret_cast<const HashJob*>(dJobs);
+        if (!small.empty())
+        {
+            CGS_TRY(hash_build_blocks(sc->keys.p, dj, uint32_t(small.size()), maxSmall, sc->disps.p, sc->tables.p,
+                                      dOut, stream));
+            sc->launches += 1;
+        }
+        if (!mid.empty())
+        {
+            CGS_TRY(hash_build_blocks(sc->keys.p, dj + small.size(), uint32_t(mid.size()), maxMid, sc->disps.p,
+                                      sc->tables.p, dOut + 8 * small.size(), stream, sc->scratch32.p));
+            sc->launches += 1;
+        }
+        std::vector<uint32_t> res(8 * jobs.size());
+        CGS_TRY(cudaMemcpyAsync(res.data(), dOut, res.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        CGS_TRY(cudaStreamSynchronize(stream));
+        for (size_t j = 0; j < jobs.size(); j++)
+        {
+            const uint32_t* r = &res[8 * j];
+            if (r[0] == 4) return CGS_ERR_HASH_BUCKET_OVERFLOW;
+            if (r[0]) return CGS_ERR_HASH_FAILED;
+            DevBVH& d = sc->hbvh[j < small.size() ? small[j] : mid[j - small.size()]];
+            d.A = r[1]; d.B = r[2]; d.N = r[3]; d.mask = r[4];
+            d.Nmagic = fastmod_magic(d.N);
+        }
+    }
+    if (!large.empty())
+    {
+        size_t w32 = 0, w64 = 0;
+        hash_scratch_words(maxLarge, w32, w64);
+        CGS_TRY(sc->scratch32.reserve(w32));
+        CGS_TRY(sc->scratch64.reserve(w64));
+        for (uint32_t k : large)
+        {
+            const HostBVH& b = sc->bvh(k);
+            const uint32_t n = uint32_t(b.keys.size());
+            HashScratch hs {};
+            hash_scratch_carve(hs, n, sc->scratch32.p, sc->scratch64.p);
+            CGS_TRY(cudaMemcpyAsync(sc->keys.p, b.keys.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+            uint32_t A[16], B[16], params[5];
+            hash_coefficients(n, A, B);
+            DevBVH& d = sc->hbvh[k];
+            int r = hash_build_device(sc->keys.p, n, A, B, sc->disps.p + d.dispBase, sc->tables.p + d.tableBase,
+                                      sc->tableCap[k], hs, params, stream, &sc->launches);
+            if (r == 4) return CGS_ERR_HASH_BUCKET_OVERFLOW;
+            if (r < 0) return CGS_ERR_CUDA;
+            if (r) return CGS_ERR_HASH_FAILED;
+            d.A = params[0]; d.B = params[1]; d.N = params[2]; d.mask = params[3];
+            d.Nmagic = fastmod_magic(d.N);
+        }
     }
     CGS_TRY(cudaMemcpyAsync(sc->bvhs.p, sc->hbvh.data(), nb * sizeof(DevBVH), cudaMemcpyHostToDevice, stream));
     CGS_TRY(cudaStreamSynchronize(stream));
@@ -356,7 +554,7 @@ bool bvh_index(const cgs_scene* s, int32_t which, uint32_t& k)
 cgs::DevScene cgs_scene::dev() const
 {
     DevScene S {};
-    S.patches = patches.p; S.nodes = nodes.p; S.indices = indices.p; S.tables = tables.p; S.disps = disps.p;
+    S.patches = patches.p; S.nodes = nodes.p; S.qnodes = qnodes.p; S.indices = indices.p; S.tables = tables.p; S.disps = disps.p;
     S.bvhs = bvhs.p; S.patchBase = patchBase.p; S.objects = dobjects.p; S.materials = materials.p;
     S.patchMaterial = patchMaterial.p; S.lights = dlights.p;
     S.groupTop = groupTop.p; S.groupLights = groupLights.p; S.groupEnv = groupEnv.p;
@@ -368,8 +566,9 @@ cgs::DevScene cgs_scene::dev() const
 cgs_scene::~cgs_scene()
 {
     cudaSetDevice(device);
-    patches.release(); nodes.release();
+    patches.release(); nodes.release(); qnodes.release();
     for (auto* b : {&indices, &tables, &disps, &patchBase, &patchMaterial, &keys, &groupTop, &scratch32, &groupStage,
+                    &hashJobs,
                     &engine, &fbStage})
         b->release();
     rayStage.release(); hitF.release(); linStage.release(); groupEnv.release();
@@ -533,18 +732,44 @@ int cgs_bvh_build(cgs_scene* s)
     if (s->objects.empty()) return CGS_ERR_INVALID_ARGUMENT;
     for (const Group& gr : s->groups)
         if (gr.objects.empty()) return CGS_ERR_EMPTY_LEAF;
+    // the surfaces' and groups' BVHs are independent: built on all host
+    // cores, largest first, each by one thread (the same result as in order)
+    const size_t ns = s->surfaces.size(), ng = s->groups.size();
+    std::vector<std::pair<uint64_t, size_t>> work;
+    for (size_t i = 0; i < ns; i++) work.push_back({s->surfaces[i].patchCount(), i});
+    for (size_t g = 0; g < ng; g++)
+    {
+        uint64_t cost = 0;
+        for (uint32_t o : s->groups[g].objects) cost += s->surfaces[s->objects[o].surface].indices.size() / 16;
+        work.push_back({cost, ns + g});
+    }
+    std::sort(work.begin(), work.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+    std::atomic<size_t> next {0};
+    auto worker = [&]() {
+        for (size_t w; (w = next.fetch_add(1)) < work.size();)
+        {
+            const size_t i = work[w].second;
+            if (i < ns)
+            {
+                s->surfaces[i].bvh.split_mode = s->splitMode;
+                build_surface_bvh(s->surfaces[i]);
+            }
+            else
+            {
+                s->groups[i - ns].top.split_mode = s->splitMode;
+                build_group_bvh(s, s->groups[i - ns]);
+            }
+        }
+    };
+    const size_t nt = std::min<size_t>(work.size(), std::max(1u, std::min(64u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
     for (auto& sf : s->surfaces)
-    {
-        sf.bvh.split_mode = s->splitMode;
-        build_surface_bvh(sf);
         if (sf.bvh.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
-    }
     for (auto& gr : s->groups)
-    {
-        gr.top.split_mode = s->splitMode;
-        build_group_bvh(s, gr);
         if (gr.top.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
-    }
     s->bvhBuilt = true;
     s->uploaded = s->hashed = false;
     return CGS_OK;
@@ -575,7 +800,7 @@ int cgs_scene_footprint(const cgs_scene* s, uint64_t* bytes)
 {
     if (!s || !bytes) return CGS_ERR_INVALID_ARGUMENT;
     uint64_t b = 0;
-    b += s->patches.bytes() + s->nodes.bytes() + s->indices.bytes() + s->tables.bytes() + s->disps.bytes();
+    b += s->patches.bytes() + s->nodes.bytes() + s->qnodes.bytes() + s->indices.bytes() + s->tables.bytes() + s->disps.bytes();
     b += s->patchBase.bytes() + s->patchMaterial.bytes() + s->bvhs.bytes() + s->dobjects.bytes();
     b += s->materials.bytes() + s->dlights.bytes() + s->groupTop.bytes() + s->groupLights.bytes();
     b += s->groupEnv.bytes();

@@ -174,6 +174,7 @@ struct cgs_scene
 
     // device side
     cgs::DBuf<float4> patches, nodes;
+    cgs::DBuf<uint4> qnodes;  // the compressed mirror of nodes (32 bytes per node)
     cgs::DBuf<uint32_t> indices, tables, disps, patchBase, patchMaterial, keys, groupTop;
     cgs::DBuf<uint2> groupLights;
     cgs::DBuf<float> groupEnv;
@@ -184,6 +185,7 @@ struct cgs_scene
     std::vector<cgs::DevBVH> hbvh;
     std::vector<uint32_t> tableCap;  // per BVH
     cgs::DBuf<uint32_t> scratch32;
+    cgs::DBuf<uint32_t> hashJobs;  // the batched hash build's job table and results
     cgs::DBuf<unsigned long long> scratch64;
     cgs::DBuf<cgs::Counters> counters;
 

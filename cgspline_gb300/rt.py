@@ -169,6 +169,22 @@ class GpuScene:
         obj.h, obj.scenes, obj.scene, obj.device, obj._keep, obj.surface_base = h, [], None, device, [], []
         return obj
 
+    @property
+    def surfaces(self) -> int:
+        """Surfaces in the store (each has its patch BVH)."""
+        return sum(len(sc.surfaces) for sc in self.scenes)
+
+    def nbvh(self) -> int:
+        """BVHs in the store: one per surface and one object-level BVH per group."""
+        return self.surfaces + self.groups
+
+    def bvh_sizes(self, which: int):
+        """(nodes, leaf-list words, table size, displacement size, keys) of BVH
+        `which` (surface id, or -1-g for the object level of group g)."""
+        sz = np.zeros(5, np.uint32)
+        check(self.lib.cgs_bvh_sizes(self.h, which, _np_ptr(sz)), "cgs_bvh_sizes")
+        return tuple(int(x) for x in sz)
+
     def footprint(self) -> int:
         b = C.c_uint64()
         check(self.lib.cgs_scene_footprint(self.h, C.byref(b)), "cgs_scene_footprint")

@@ -318,13 +318,21 @@ typedef struct cgs_engine_config {
      * goes through the perfect hash, as in BVH::hashIntersect.  Both visit
      * the same nodes in the same order and give the same hits. */
     int backtrack_cache;
+    /* 1: the traversal kernel reads a 32-byte compressed copy of each BVH
+     * node (child boxes on an 8-bit grid of the node's box, widened outward
+     * so that they contain the exact boxes); 0 (default): the exact 64-byte
+     * records.  The compressed boxes are met wherever the exact ones are, so
+     * both settings give the same hits; the exported BVH is the exact one.
+     * The autotuner tries both. */
+    int compressed_nodes;
 } cgs_engine_config;
 int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
 
 /* The autotuner: renders the batch (wavefront schedule) under each candidate
  * setting (passes 1, 2, 4 x collect 128, 256 x resolve 64, 128 threads x
- * traversal blocks per SM: as many as fit, or 768 threads' worth), times
+ * traversal blocks per SM: as many as fit, or 768 threads' worth x exact or
+ * compressed nodes), times
  * `repeats` graph replays of each with CUDA events, and keeps the fastest
  * (median) as the process-wide setting.  Synchronises `stream`. */
 int cgs_autotune_render(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,
@@ -342,7 +350,10 @@ int cgs_scene_counters(cgs_scene* scene, cgs_counters* out);
  * Outputs (device): disp[displ_capacity], table[table_capacity] with
  * table[h(keys[i])] = i; params (host) = A, B, N, mask, trials.
  * displacement size = bit_floor(max(2, (n-1)>>1)); table_capacity must be at
- * least n + 15*max(4, 0.05n).  Synchronises `stream`. */
+ * least n + 15*max(4, 0.05n).  Up to 131,072 keys one thread block builds the
+ * table in one launch (its scratch in shared memory up to 8,192 keys);
+ * larger inputs run the multi-launch build (two launches per round).  All
+ * give the same tables.  Synchronises `stream`. */
 int cgs_perfect_hash_build(const uint32_t* keys, uint32_t n, uint32_t* disp, uint32_t displ_capacity,
                            uint32_t* table, uint32_t table_capacity, uint32_t params[5], void* stream);
 

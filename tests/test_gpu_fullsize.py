@@ -72,6 +72,29 @@ def test_engine_settings_agree_at_full_size(setup):
     assert (runs[0][0]["patch"] >= 0).mean() > 0.2
 
 
+def test_compressed_nodes_give_identical_hits(setup):
+    """The traversal on the 32-byte compressed node mirror against the exact
+    64-byte records: the same hits, bit for bit, on the full frame, closest
+    and any hit, at FP32 and with the FP64 polish; the conservative boxes add
+    a few node visits."""
+    rt, torch, g, rays = setup
+    base = rt.engine_config()
+    out = {}
+    try:
+        for cq in (1, 0):
+            rt.set_engine_config(compressed_nodes=cq)
+            out[cq] = (host(g.intersect(rays)), g.counters(), host(g.intersect(rays, any_hit=True)),
+                       host(g.intersect(rays, precision=rt.FP32_POLISH64)))
+    finally:
+        rt.set_engine_config(**base)
+    (h1, c1, a1, p1), (h0, c0, a0, p0) = out[1], out[0]
+    for k in h1:
+        assert np.array_equal(h1[k], h0[k]), k
+        assert np.array_equal(p1[k], p0[k]), k
+    assert np.array_equal(a1["patch"] >= 0, a0["patch"] >= 0)
+    assert c1["device_errors"] == 0 and c0["nodes"] <= c1["nodes"] <= 1.25 * c0["nodes"]
+
+
 def test_closest_and_any_hit_agree_at_full_size(setup):
     rt, torch, g, rays = setup
     c = host(g.intersect(rays))

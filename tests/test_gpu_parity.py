@@ -90,7 +90,37 @@ def test_bvh_and_hash_bit_exact_torus(c2_small_gpu, c2_small_oracle):
     assert (g["A"], g["B"], g["N"]) == (o["A"], o["B"], o["N"])
 
 
-@pytest.mark.parametrize("n", [1, 2, 31, 1000, 32767, 65537, 1 << 20])
+def test_store_hash_tables_bit_exact(rt, oracle_mod):
+    """The batched store build (every BVH of up to 8,192 keys by one thread
+    block, in one launch; larger ones by the multi-launch build) against the
+    oracle, BVH by BVH: two union scenes (57 and 51 object surfaces, 13,144
+    and 61,974 patches) and the full torus (one BVH of 32,767 keys)."""
+    scenes = [S.scene_c4(17), S.scene_c4(5), S.scene_c2()]
+    store = rt.GpuScene(scenes)
+    base = obase = 0
+    nbig = 0
+    for g, sc in enumerate(scenes):
+        o = oracle_mod.OracleScene(sc)
+        for k in list(range(len(sc.surfaces))) + [-1]:
+            gb = store.bvh(base + k if k >= 0 else -1 - g)
+            ob = o.bvh(k)
+            if k < 0:
+                # an object-level BVH lists the store's object ids; the
+                # oracle's scene numbers its objects from 0
+                ind = gb["indices"].copy()
+                ind[ind != 0xFFFFFFFF] -= obase
+                gb["indices"] = ind
+            for f in ("nodes", "keys", "indices", "table", "disp"):
+                assert np.array_equal(gb[f], ob[f]), (g, k, f)
+            assert (gb["A"], gb["B"], gb["N"], gb["mask"]) == (ob["A"], ob["B"], ob["N"], ob["mask"])
+            nbig += gb["keys"].size > 8192
+        base += len(sc.surfaces)
+        obase += len(sc.objects)
+    assert nbig >= 1
+    store.close()
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 1000, 8191, 8192, 8193, 32767, 65537, 1 << 20])
 def test_perfect_hash_matches_oracle(rt, oracle_mod, n):
     keys = np.arange(1, n + 1, dtype=np.uint32)
     o = oracle_mod.hash_build(keys)
