@@ -518,13 +518,37 @@ __device__ __forceinline__ void project_net64(float2* net, const float4* __restr
     }
 }
 
-// The ray within asin(sinmax) of the plane of the patch's diagonals.
+// The precision form's near-grazing test of a candidate: the ray within
+// asin(sinmax) of the plane of the patch's diagonals or of any of the nine
+// cells of its control net (a cell's normal: the cross product of its edges
+// along u and v at its first corner), or those ten normals on both sides of
+// the ray (the patch folds over the ray's direction: a silhouette).  The
+// cells' normals bound the patch's, interior control points included, so a
+// bumpy patch tangent to the ray somewhere inside is caught even where its
+// diagonals and corners are not.
 __device__ __forceinline__ bool near_grazing(const float4* __restrict__ P, float3 d, float sinmax)
 {
-    const float3 a = xyz(__ldg(P + 15)) - xyz(__ldg(P)), b = xyz(__ldg(P + 12)) - xyz(__ldg(P + 3));
-    const float3 n = cross(a, b);
-    const float l = len(n);
-    return l > 0.0f && fabsf(dot(n, d)) < sinmax * l;
+    bool pos = false, neg = false, near = false;
+    auto test = [&](float3 n) {
+        const float l = len(n);
+        if (!(l > 0.0f)) return;
+        const float c = dot(n, d);
+        if (fabsf(c) < sinmax * l) near = true;
+        if (c > 0.0f) pos = true;
+        else neg = true;
+    };
+    test(cross(xyz(__ldg(P + 15)) - xyz(__ldg(P)), xyz(__ldg(P + 12)) - xyz(__ldg(P + 3))));
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+    {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+        {
+            const float3 p = xyz(__ldg(P + 4 * j + i));
+            test(cross(xyz(__ldg(P + 4 * j + i + 1)) - p, xyz(__ldg(P + 4 * (j + 1) + i)) - p));
+        }
+    }
+    return near || (pos && neg);
 }
 
 // doBezierClipping2D_device (src/Spline_BezierClipping.cu:547-828) with the

@@ -33,6 +33,13 @@ CLIP_GRAZE64 = 5
 # the reference's one-pass scan (oracle only: finds roots that scan drops);
 # with precision FP64 the FP64 search clips with it too
 CLIP_EXACT_HULL = 6
+
+
+def set_graze_mode(mode: int):
+    """The near-grazing test of CLIP_GRAZE64: 1 (default) the diagonals' and
+    the nine control-net cells' normals, with silhouettes; 0 the diagonals'
+    plane alone."""
+    lib().ora_set_graze_mode(int(mode))
 GRAZE_5, GRAZE_30 = 0.0871557427, 0.5
 FP32, FP32_POLISH64, FP64 = 0, 1, 2
 
@@ -85,6 +92,7 @@ def lib():
         L.ora_camera_rays.argtypes = [fp, C.c_uint32, C.c_uint32, fp]
         L.ora_patch_intersect.argtypes = [fp, u32, fp, C.c_float, C.c_int, P, P, P]
         L.ora_patch_subdiv_host.argtypes = [fp, u32, fp, C.c_float, P, P]
+        L.ora_set_graze_mode.argtypes = [C.c_int]
         L.ora_patch_eval.argtypes = [fp, C.c_float, C.c_float, fp, fp]
         _lib = L
     return _lib

@@ -36,6 +36,7 @@
 #include <numeric>
 #include <random>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace ora {
@@ -660,22 +661,48 @@ struct PatchHit { float t; float u, v; };
 
 // kClipDeviceB64: kClipDevice with FP64 fat-line bounds; kClipDeviceB64P:
 // the same on a net projected in FP64 (rounded to the search type).
-// kClipGraze: the precision form's clip -- kClipDevice, except that a
-// near-grazing candidate (the ray within asin(g_grazeSin) of the plane of
-// the patch's diagonals: 5 degrees for CGS_PREC_FP32_POLISH64, 30 for
-// CGS_PREC_FP32_GRAZE64) gets kClipDeviceB64P with tolerance 2^-20.
+// kClipGraze: the precision form's clip (CGS_PREC_FP32_GRAZE64) --
+// kClipDevice, except that a near-grazing candidate (grazing(): within
+// asin(g_grazeSin) = 30 degrees of a control-net normal, or a silhouette)
+// gets kClipDeviceB64P with tolerance 2^-20.
 // kClipExactHull: the host clip with the true convex hull (hull_range_exact),
 // an oracle-only variant that shows the roots the reference's scan drops.
 enum Method { kClipHost = 0, kClipDevice = 1, kSubdiv = 2, kClipDeviceB64 = 3, kClipDeviceB64P = 4, kClipGraze = 5,
               kClipExactHull = 6 };
 static float g_grazeSin = 0.5f;
 constexpr float kGrazeTol = 0x1p-20f;
+// The precision form's near-grazing test of a candidate (restates
+// near_grazing in the CUDA path).  Mode 1 (the default): the ray within
+// asin(g_grazeSin) of the plane of the patch's diagonals or of any of the
+// nine cells of its control net (each cell's normal: the cross product of
+// its edges along u and v at its first corner), or those ten normals on both
+// sides of the ray (the patch folds over the ray's direction somewhere: a
+// silhouette).  The cells' normals bound the patch's, interior control
+// points included, so a bumpy patch tangent to the ray inside is caught even
+// where its diagonals and corners are not.  Mode 0: the diagonals' plane
+// alone (the earlier test, for comparison).
+static int g_grazeMode = 1;
 template<class R> inline bool grazing(const V4<R> P[16], V3<R> d)
 {
-    V3<R> a = xyz(P[15]) - xyz(P[0]), b = xyz(P[12]) - xyz(P[3]);
-    V3<R> n = cross(a, b);
-    R l = length(n);
-    return l > R(0) && std::fabs(dot(n, d)) < R(g_grazeSin) * l;
+    bool pos = false, neg = false;
+    auto test = [&](V3<R> nn) {
+        const R ln = length(nn);
+        if (!(ln > R(0))) return false;
+        const R c = dot(nn, d);
+        if (std::fabs(c) < R(g_grazeSin) * ln) return true;
+        (c > 0 ? pos : neg) = true;
+        return false;
+    };
+    if (test(cross(xyz(P[15]) - xyz(P[0]), xyz(P[12]) - xyz(P[3])))) return true;
+    if (g_grazeMode == 0) return false;
+    for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++)
+        {
+            const V3<R> tu = xyz(P[4 * j + i + 1]) - xyz(P[4 * j + i]);
+            const V3<R> tv = xyz(P[4 * (j + 1) + i]) - xyz(P[4 * j + i]);
+            if (test(cross(tu, tv))) return true;
+        }
+    return pos && neg;
 }
 
 // spline::doBezierClipping / doSubdivision_device front end,
@@ -1729,6 +1756,8 @@ void ora_scene_set_split(void* s_, int mode) { static_cast<Scene*>(s_)->splitMod
 void ora_philox(uint32_t* ctr4, uint32_t k0, uint32_t k1) { philox(ctr4, k0, k1); }
 // the grazing margin of kClipGraze (process-wide; not thread-safe against running queries)
 void ora_set_graze_sin(float s) { g_grazeSin = s; }
+// the near-grazing test of CLIP_GRAZE64 (process-wide; see grazing())
+void ora_set_graze_mode(int m) { g_grazeMode = m; }
 
 static const BVH* pick_bvh(const Scene* s, int which)
 {

@@ -235,6 +235,35 @@ def test_grazing_variant_restatement(oracle_mod):
     assert np.array_equal(a["patch"] >= 0, b["patch"] >= 0)
 
 
+def test_grazing_test_catches_bumpy_patches(oracle_mod):
+    """On the C2 torus (16,384 patches whose interior control points are
+    displaced by about a patch width) a grazing ray can be tangent to a patch
+    inside it while the plane of the patch's diagonals is far from the ray:
+    the diagonals-only test sends that candidate to the plain FP32 search,
+    which loses the root, and the ray reports a farther patch.  The precision
+    form's test (the control-net cells' normals, and silhouettes) catches it:
+    on 8,192 seeded grazing rays, far fewer hits on another patch than the
+    FP64 search's (6 against 86) and far fewer beyond 1e-5 (11 against 108)."""
+    from cgspline_gb300 import scenes as S
+    sc = S.scene_c2()
+    o = oracle_mod.OracleScene(sc)
+    rays = S.grazing_rays(sc.surfaces[0], 8192, seed=21)
+    ref = o.intersect(rays, precision=oracle_mod.FP64)
+    out = {}
+    try:
+        for mode in (0, 1):
+            oracle_mod.set_graze_mode(mode)
+            g = o.intersect(rays, method=oracle_mod.CLIP_GRAZE64, precision=oracle_mod.FP32_POLISH64,
+                            graze_sin=oracle_mod.GRAZE_30)
+            both = (g["patch"] >= 0) & (ref["patch"] >= 0)
+            rel = np.abs(g["t"][both] - ref["t"][both]) / ref["t"][both]
+            out[mode] = (int((both & (g["patch"] != ref["patch"])).sum()), int((rel > 1e-5).sum()))
+    finally:
+        oracle_mod.set_graze_mode(1)
+    assert out[1][0] <= 12 and out[1][0] * 5 <= out[0][0], out
+    assert out[1][1] <= 20 and out[1][1] * 5 <= out[0][1], out
+
+
 def test_longest_axis_split_same_hits(oracle_mod):
     """The longest-axis build changes only the tree: same hits, far fewer
     node visits than the reference's always-y split."""
