@@ -61,7 +61,8 @@ class Hits(C.Structure):
 
 class EngineConfig(C.Structure):
     _fields_ = [(k, C.c_int) for k in ("passes", "collect_threads", "resolve_threads", "collect_occupancy",
-                                       "resolve_occupancy", "backtrack_cache", "compressed_nodes")]
+                                       "resolve_occupancy", "backtrack_cache", "compressed_nodes",
+                                       "queue_chunk", "packet_width")]
 
 
 class ServerOptions(C.Structure):

@@ -3,6 +3,8 @@
 // batched frame renders, and the standalone perfect-hash build.
 #include "scene_impl.h"
 
+#include <map>
+
 using namespace cgs;
 
 namespace cgs {
@@ -572,26 +574,35 @@ int cgs_camera_rays(const cgs_camera* cam, uint32_t w, uint32_t h, int flip_y, f
     return cuda_status(launch_camera_rays(c, w, h, rays, (cudaStream_t)stream));
 }
 
+static cgs_engine_config to_c(const EngineConfig& c)
+{
+    return cgs_engine_config {c.passes,         c.collectThreads,  c.resolveThreads, c.collectOccupancy,
+                              c.resolveOccupancy, c.backtrackCache, c.compressedNodes, c.queueChunk,
+                              c.packetWidth};
+}
+
 int cgs_engine_config_get(cgs_engine_config* out)
 {
     if (!out) return CGS_ERR_INVALID_ARGUMENT;
     const EngineConfig c = engine_config();
-    *out = cgs_engine_config {c.passes, c.collectThreads, c.resolveThreads, c.collectOccupancy, c.resolveOccupancy,
-                              c.backtrackCache, c.compressedNodes};
+    *out = to_c(c);
     return CGS_OK;
 }
 
 int cgs_engine_config_set(const cgs_engine_config* in)
 {
     if (!in) return CGS_ERR_INVALID_ARGUMENT;
-    const EngineConfig c {in->passes, in->collect_threads, in->resolve_threads, in->collect_occupancy,
-                          in->resolve_occupancy, in->backtrack_cache, in->compressed_nodes};
+    const EngineConfig c {in->passes,          in->collect_threads, in->resolve_threads,
+                          in->collect_occupancy, in->resolve_occupancy, in->backtrack_cache,
+                          in->compressed_nodes,  in->queue_chunk,     in->packet_width};
     return set_engine_config(c) ? CGS_OK : CGS_ERR_INVALID_ARGUMENT;
 }
 
-// The autotuner: renders the batch (wavefront schedule) under every
-// candidate engine setting, times `repeats` replays of each on the device,
-// and keeps the fastest (median) as the process-wide setting.
+// The autotuner: a coordinate descent over the engine settings.  Each
+// candidate renders the batch (wavefront schedule) `repeats` + 2 times, the
+// last `repeats` timed with CUDA events on `stream`; its median is its score.
+// Two rounds visit the knobs in turn, each set to its fastest value with the
+// others held; scores are kept, so a setting is timed once.
 int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n, const cgs_render_options* opt,
                         int repeats, cgs_engine_config* best, double* best_ms, void* stream)
 {
@@ -606,53 +617,78 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
     if (cudaEventQuery(s->finished) == cudaErrorNotReady) return CGS_ERR_BUSY;
     cudaStream_t st = (cudaStream_t)stream;
     const EngineConfig saved = engine_config();
-    EngineConfig winner = saved;
-    double winnerMs = 1e300;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CGS_TRY(cudaEventCreate(&e0));
     if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return CGS_ERR_CUDA; }
     int status = CGS_OK;
-    for (int passes : {1, 2, 4})
-        for (int ct : {128, 256})
-            for (int rt : {64, 128})
-                for (int full : {1, 0})
-                    for (int cq : {0, 1})
+
+    // the knobs; `capped` stands for the traversal's blocks per SM: as many as
+    // fit (0), or three quarters of that (768 threads per SM), which leaves
+    // room for the overlapping queries
+    struct Point { int passes, ct, rt, capped, cq, chunk, width; };
+    auto config = [&](const Point& p) {
+        EngineConfig c = saved;
+        c.passes = p.passes; c.collectThreads = p.ct; c.resolveThreads = p.rt;
+        c.collectOccupancy = p.capped ? 768 / p.ct : 0; c.resolveOccupancy = 0;
+        c.compressedNodes = p.cq; c.queueChunk = p.chunk; c.packetWidth = p.width;
+        return c;
+    };
+    auto key = [](const Point& p) {
+        return ((((((int64_t(p.passes) * 512 + p.ct) * 256 + p.rt) * 2 + p.capped) * 2 + p.cq) * 128 + p.chunk) * 64) +
+               p.width;
+    };
+    std::map<int64_t, double> scores;
+    auto score = [&](const Point& p) -> double {
+        const auto it = scores.find(key(p));
+        if (it != scores.end()) return it->second;
+        if (!set_engine_config(config(p))) return 1e300;
+        std::vector<float> ms;
+        for (int k = 0; k < repeats + 2 && status == CGS_OK; k++)
+        {
+            RenderBatch bk = b;
+            if (k >= 2 && cudaEventRecord(e0, st) != cudaSuccess) status = CGS_ERR_CUDA;
+            if (status == CGS_OK) status = run_batch(s, s->slot, host, bk, CGS_SCHED_WAVEFRONT, st, &s->launches);
+            if (status == CGS_OK && k >= 2)
             {
-                // traversal blocks: as many as fit, or three quarters of that (768
-                // threads per SM), which leaves room for the overlapping queries
-                const EngineConfig c {passes, ct, rt, full ? 0 : (ct == 256 ? 3 : 6), 0, saved.backtrackCache, cq};
-                set_engine_config(c);
-                std::vector<float> ms;
-                for (int k = 0; k < repeats + 2 && status == CGS_OK; k++)
-                {
-                    RenderBatch bk = b;
-                    if (k >= 2 && cudaEventRecord(e0, st) != cudaSuccess) status = CGS_ERR_CUDA;
-                    if (status == CGS_OK) status = run_batch(s, s->slot, host, bk, CGS_SCHED_WAVEFRONT, st, &s->launches);
-                    if (status == CGS_OK && k >= 2)
-                    {
-                        float t = 0.0f;
-                        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-                            cudaEventElapsedTime(&t, e0, e1) != cudaSuccess)
-                            status = CGS_ERR_CUDA;
-                        ms.push_back(t);
-                    }
-                    else if (status == CGS_OK && cudaStreamSynchronize(st) != cudaSuccess)
-                        status = CGS_ERR_CUDA;
-                }
+                float t = 0.0f;
+                if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&t, e0, e1) != cudaSuccess)
+                    status = CGS_ERR_CUDA;
+                ms.push_back(t);
+            }
+            else if (status == CGS_OK && cudaStreamSynchronize(st) != cudaSuccess)
+                status = CGS_ERR_CUDA;
+        }
+        if (status != CGS_OK || ms.empty()) return 1e300;
+        std::sort(ms.begin(), ms.end());
+        return scores[key(p)] = ms[ms.size() / 2];
+    };
+
+    // start from the current setting, rounded onto the search grid
+    Point cur {saved.passes, saved.collectThreads, saved.resolveThreads, saved.collectOccupancy != 0 ? 1 : 0,
+               saved.compressedNodes, saved.queueChunk, saved.packetWidth};
+    double curMs = score(cur);
+    const std::vector<std::pair<int Point::*, std::vector<int>>> knobs {
+        {&Point::passes, {1, 2, 4}}, {&Point::ct, {128, 256}},   {&Point::rt, {64, 128}},
+        {&Point::capped, {0, 1}},    {&Point::cq, {0, 1}},       {&Point::chunk, {32, 48, 64}},
+        {&Point::width, {1, 8, 16}}};
+    for (int round = 0; round < 2 && status == CGS_OK; round++)
+        for (const auto& [field, values] : knobs)
+            for (int v : values)
+            {
                 if (status != CGS_OK) break;
-                std::sort(ms.begin(), ms.end());
-                const double med = ms[ms.size() / 2];
-                if (med < winnerMs) { winnerMs = med; winner = c; }
+                Point p = cur;
+                p.*field = v;
+                const double ms = score(p);
+                if (ms < curMs) { curMs = ms; cur = p; }
             }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    const EngineConfig winner = config(cur);
     set_engine_config(status == CGS_OK ? winner : saved);
     if (status != CGS_OK) return status;
-    if (best)
-        *best = cgs_engine_config {winner.passes, winner.collectThreads, winner.resolveThreads,
-                                   winner.collectOccupancy, winner.resolveOccupancy, winner.backtrackCache,
-                                   winner.compressedNodes};
-    if (best_ms) *best_ms = winnerMs;
+    if (best) *best = to_c(winner);
+    if (best_ms) *best_ms = curMs;
     s->lastStream = st;
     s->lastCounters = s->slot.counters.p;
     return CGS_OK;

@@ -44,7 +44,7 @@ namespace {
 
 constexpr int kCollectThreads = 256;   // launch bound; runtime block size 128 or 256
 constexpr int kResolveThreads = 128;   // launch bound; runtime block size 64 or 128
-constexpr uint32_t kChunk = 64;        // list entries per ray and pass
+constexpr uint32_t kChunk = 64;        // list entries per ray and pass (the most; EngineConfig::queueChunk)
 // One collect step appends at most two entries: a leaf's first patch and,
 // when that patch ends the leaf and nothing is postponed inside the object,
 // the marker that leaves the object.
@@ -67,6 +67,8 @@ struct Eng  // per-ray engine state, SoA over the query's capacity
     int32_t *obj, *lpatch;
     float *leafEntry, *limit, *lt, *lu, *lv;
     uint32_t* ctl;  // per pass: collect fetch, resolve fetch
+    uint32_t chunk;        // list entries a ray may fill per pass (<= kChunk)
+    uint32_t packetWidth;  // idle lanes a warp gathers before the traversal refills it
 };
 
 constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 16;
@@ -99,10 +101,14 @@ __device__ __forceinline__ BvhRef bvh_ref(const DevScene& S, uint32_t idx)
 }
 
 // Warp-wide refill: every lane in `need` gets the next index from *fetch.
-__device__ __forceinline__ uint32_t warp_fetch(uint32_t* fetch, bool need)
+// width > 1: the warp waits until at least `width` of its lanes need one (or
+// none is busy) and then refills them together: rays enter the warp in
+// packets, which keeps its lanes at similar depths of similar walks.
+__device__ __forceinline__ uint32_t warp_fetch(uint32_t* fetch, bool need, uint32_t width = 1, bool busy = false)
 {
     unsigned m = __ballot_sync(0xFFFFFFFFu, need);
     if (!m) return EMPTY;
+    if (width > 1 && uint32_t(__popc(m)) < width && __ballot_sync(0xFFFFFFFFu, busy)) return EMPTY;
     int leader = __ffs(m) - 1;
     uint32_t base = 0;
     if ((int)lane_id() == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
@@ -163,8 +169,9 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
     for (;;)
     {
         const bool need = !active && !exhausted;
-        const uint32_t idx = warp_fetch(E.ctl + 4 * pass, need);
-        if (need)
+        // a lane the packet rule holds back gets EMPTY (ray counts stay below 2^31)
+        const uint32_t idx = warp_fetch(E.ctl + 4 * pass, need, E.packetWidth, active);
+        if (need && idx != EMPTY)
         {
             if (idx >= n)
                 exhausted = true;
@@ -219,7 +226,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         if (__ballot_sync(0xFFFFFFFFu, active || !exhausted) == 0) break;
         if (!active) continue;
 
-        if (ncand + kMaxAppendsPerStep > kChunk)
+        if (ncand + kMaxAppendsPerStep > E.chunk)
         {
             // no room for what one step may append: park before this step
             E.node[rid] = node; E.key[rid] = key; E.post[rid] = post; E.leaf[rid] = leaf;
@@ -683,7 +690,8 @@ bool valid_engine_config(const EngineConfig& c)
     return c.passes >= 1 && c.passes <= kMaxPasses && (c.collectThreads == 128 || c.collectThreads == 256) &&
            (c.resolveThreads == 64 || c.resolveThreads == 128) && c.collectOccupancy >= 0 && c.collectOccupancy <= 32 &&
            c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
-           (c.compressedNodes == 0 || c.compressedNodes == 1);
+           (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 16 &&
+           c.queueChunk <= int(kChunk) && c.queueChunk % 8 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32;
 }
 
 bool set_engine_config(const EngineConfig& c)
@@ -715,6 +723,11 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
         return launch_query_fp64(S, rays, n, nDev, kTolFP64, hits, cnt, stream);
     }
     Eng E = carve(scratch, capacity);
+    {
+        const EngineConfig ec = engine_config();
+        E.chunk = uint32_t(ec.queueChunk);
+        E.packetWidth = uint32_t(ec.packetWidth);
+    }
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const int flat = sms() * 4;
     k_init<<<flat, 256, 0, stream>>>(rays, n, nDev, hits, any ? occluded : nullptr, E);
@@ -737,6 +750,11 @@ cudaError_t run_traverse(const DevScene& S, RaysSoA rays, uint32_t n, bool any, 
     if (n == 0) return cudaSuccess;
     if (n > capacity) return cudaErrorInvalidValue;
     Eng E = carve(scratch, capacity);
+    {
+        const EngineConfig ec = engine_config();
+        E.chunk = uint32_t(ec.queueChunk);
+        E.packetWidth = uint32_t(ec.packetWidth);
+    }
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const EngineConfig c = engine_config();
     const int ct = c.collectThreads;

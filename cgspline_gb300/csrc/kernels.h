@@ -82,6 +82,8 @@ struct EngineConfig
     int resolveOccupancy = 0;
     int backtrackCache = 1;  // 1: backtracks read postponed siblings from a per-lane ring first
     int compressedNodes = 0; // 1: the traversal reads the 32-byte compressed node mirror
+    int queueChunk = 64;     // candidate-list entries a ray may fill per pass (16..64, multiple of 8)
+    int packetWidth = 1;     // the traversal refills a warp once this many lanes are idle (1..32)
 };
 EngineConfig engine_config();
 bool set_engine_config(const EngineConfig& c);

@@ -534,8 +534,9 @@ def set_engine_config(**kw):
 
 
 def autotune(scene: GpuScene, requests, options: Options | None = None, repeats: int = 3, stream=None):
-    """cgs_autotune_render: time every candidate engine setting on this batch
-    and keep the fastest.  Returns (settings dict, median ms)."""
+    """cgs_autotune_render: a coordinate descent over the engine settings on
+    this batch (two rounds over the knobs, each timed `repeats` times); keeps
+    the fastest.  Returns (settings dict, median ms)."""
     lib = _capi.load()
     arr = (_capi.RenderRequest * len(requests))()
     for k, q in enumerate(requests):

@@ -325,16 +325,28 @@ typedef struct cgs_engine_config {
      * both settings give the same hits; the exported BVH is the exact one.
      * The autotuner tries both. */
     int compressed_nodes;
+    /* Candidate-list entries a ray may fill in one collect pass before it
+     * parks (16..64, a multiple of 8; default 64).  Smaller lists park rays
+     * sooner and hand the resolve kernel shorter, more even rows. */
+    int queue_chunk;
+    /* Packet refill (1..32; default 1): the traversal kernel gives a warp's
+     * idle lanes new rays only once at least this many are idle, or none of
+     * its lanes is busy, so that rays enter a warp in packets of adjacent
+     * pixels; 1 refills every idle lane at once. */
+    int packet_width;
 } cgs_engine_config;
 int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
 
-/* The autotuner: renders the batch (wavefront schedule) under each candidate
- * setting (passes 1, 2, 4 x collect 128, 256 x resolve 64, 128 threads x
- * traversal blocks per SM: as many as fit, or 768 threads' worth x exact or
- * compressed nodes), times
- * `repeats` graph replays of each with CUDA events, and keeps the fastest
- * (median) as the process-wide setting.  Synchronises `stream`. */
+/* The autotuner: renders the batch (wavefront schedule) and times `repeats`
+ * renders of it with CUDA events per candidate setting, keeping the fastest
+ * (median) as the process-wide setting.  The search is a coordinate descent
+ * from the current setting, two rounds over the knobs in turn (passes 1, 2,
+ * 4; collect 128, 256 and resolve 64, 128 threads; traversal blocks per SM
+ * as many as fit or 768 threads' worth; exact or compressed nodes; queue
+ * chunk 32, 48, 64; packet width 1, 8, 16), each knob set to its fastest
+ * value with the others held; a setting already timed is not timed again.
+ * Synchronises `stream`. */
 int cgs_autotune_render(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,
                         const cgs_render_options* options, int repeats, cgs_engine_config* best,
                         double* best_ms, void* stream);

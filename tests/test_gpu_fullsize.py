@@ -53,8 +53,13 @@ def test_engine_settings_agree_at_full_size(setup):
     try:
         for cfg in ({"passes": 2, "backtrack_cache": 1}, {"passes": 1, "backtrack_cache": 0},
                     {"passes": 8, "collect_threads": 128, "resolve_threads": 128, "backtrack_cache": 1},
-                    {"passes": 2, "backtrack_cache": 0}):
-            rt.set_engine_config(**cfg)
+                    {"passes": 2, "backtrack_cache": 0},
+                    {"passes": 2, "backtrack_cache": 1, "packet_width": 8},
+                    {"passes": 2, "backtrack_cache": 1, "queue_chunk": 16, "packet_width": 8},
+                    {"passes": 1, "backtrack_cache": 1, "queue_chunk": 40, "packet_width": 32},
+                    {"passes": 4, "backtrack_cache": 0, "queue_chunk": 32, "packet_width": 16,
+                     "compressed_nodes": 1}):
+            rt.set_engine_config(**{**base, **cfg})
             h = host(g.intersect(rays))
             c = g.counters()
             assert c["device_errors"] == 0
@@ -67,6 +72,12 @@ def test_engine_settings_agree_at_full_size(setup):
     (h1, c1), (h0, c0) = got[(("backtrack_cache", 1), ("passes", 2))], got[(("backtrack_cache", 0), ("passes", 2))]
     for k in h1:
         assert np.array_equal(h1[k], h0[k]), k
+    # the packet refill changes when a warp takes its rays, not which rays
+    # park or what a ray meets: the same hits, bit for bit, and the same nodes
+    hw, cw = got[(("backtrack_cache", 1), ("packet_width", 8), ("passes", 2))]
+    for k in h1:
+        assert np.array_equal(hw[k], h1[k]), k
+    assert cw["nodes"] == c1["nodes"] and cw["hash_lookups"] == c1["hash_lookups"]
     assert c1["nodes"] == c0["nodes"] and c1["hash_lookups"] == c0["hash_lookups"]
     assert c0["hash_table_reads"] == c0["hash_lookups"] and c1["hash_table_reads"] < c1["hash_lookups"] // 100
     assert (runs[0][0]["patch"] >= 0).mean() > 0.2
