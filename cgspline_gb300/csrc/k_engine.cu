@@ -691,7 +691,8 @@ bool valid_engine_config(const EngineConfig& c)
            (c.resolveThreads == 64 || c.resolveThreads == 128) && c.collectOccupancy >= 0 && c.collectOccupancy <= 32 &&
            c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
            (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 16 &&
-           c.queueChunk <= int(kChunk) && c.queueChunk % 8 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32;
+           c.queueChunk <= int(kChunk) && c.queueChunk % 8 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32 &&
+           (c.rayOrder == 0 || c.rayOrder == 1);
 }
 
 bool set_engine_config(const EngineConfig& c)

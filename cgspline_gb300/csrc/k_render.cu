@@ -247,17 +247,39 @@ struct Q  // a ray queue: 9 floats per ray (SoA with stride = capacity) + sample
     }
 };
 
-__global__ void k_wf_camera(const RenderBatch* __restrict__ bp, Q q, float* accum, uint32_t* count)
+// The pixel that queue position p of a w x h image takes in tile order: the
+// image is cut into bands of 4 rows and each band into chunks 8 columns wide
+// (narrower at the right edge, lower in the last band), taken chunk by chunk,
+// row by row inside a chunk, so that a warp's 32 rays cover an 8 x 4 tile.
+// A bijection of [0, w*h).
+__device__ __forceinline__ uint32_t tiled_pixel(uint32_t p, uint32_t w, uint32_t h)
+{
+    const uint32_t band = p / (4 * w);
+    const uint32_t m = p - band * 4 * w;
+    const uint32_t hb = min(4u, h - 4 * band);
+    const uint32_t c = m / (8 * hb);
+    const uint32_t q = m - c * 8 * hb;
+    const uint32_t cw = min(8u, w - 8 * c);
+    return (4 * band + q / cw) * w + 8 * c + q % cw;
+}
+
+// Primary rays of every sample.  Queue position k holds sample k (scanline
+// order), or with `tiled` the sample of its request's tile-order pixel; the
+// ray carries its sample index, which keys the accumulation and the
+// Monte-Carlo stream, so the order changes no result.
+__global__ void k_wf_camera(const RenderBatch* __restrict__ bp, Q q, float* accum, uint32_t* count, int tiled)
 {
     const RenderBatch b = *bp;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < b.samples; k += gridDim.x * blockDim.x)
     {
         const DevRequest& r = b.req[find_request(b.req, b.nreq, k, false)];
-        const uint32_t local = k - r.sampleBase, pixel = local / r.spp, s = local % r.spp;
+        const uint32_t local = k - r.sampleBase, s = local % r.spp;
+        const uint32_t pixel = tiled ? tiled_pixel(local / r.spp, r.width, r.height) : local / r.spp;
+        const uint32_t smp = r.sampleBase + pixel * r.spp + s;
         const float2 xy = sample_xy(r, pixel, s);
         const float3 o = f3(r.cam.pos[0], r.cam.pos[1], r.cam.pos[2]);
-        q.put(k, o, pixel_dir(r.cam, xy.x, xy.y), f3(1.0f, 1.0f, 1.0f), k, r.group, uint32_t(r.depth));
-        accum[3ull * k] = 0.0f; accum[3ull * k + 1] = 0.0f; accum[3ull * k + 2] = 0.0f;
+        q.put(k, o, pixel_dir(r.cam, xy.x, xy.y), f3(1.0f, 1.0f, 1.0f), smp, r.group, uint32_t(r.depth));
+        accum[3ull * smp] = 0.0f; accum[3ull * smp + 1] = 0.0f; accum[3ull * smp + 2] = 0.0f;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) { count[0] = b.samples; count[1] = 0; count[2] = 0; }
 }
@@ -454,7 +476,7 @@ cudaError_t launch_render_wavefront(const DevScene& S, const RenderBatch& b, con
     const uint32_t scap = cap * lcap;
     Q q[2] = {{wb.ray[0], wb.sample[0], wb.group[0], wb.depth[0], cap},
               {wb.ray[1], wb.sample[1], wb.group[1], wb.depth[1], cap}};
-    k_wf_camera<<<gFlat, 256, 0, stream>>>(bDev, q[0], wb.accum, wb.count);
+    k_wf_camera<<<gFlat, 256, 0, stream>>>(bDev, q[0], wb.accum, wb.count, engine_config().rayOrder);
     nl++;
     Query qa = b.q;
     qa.precision = 0;  // shadow rays: any hit at level 0

@@ -84,6 +84,7 @@ struct EngineConfig
     int compressedNodes = 0; // 1: the traversal reads the 32-byte compressed node mirror
     int queueChunk = 64;     // candidate-list entries a ray may fill per pass (16..64, multiple of 8)
     int packetWidth = 1;     // the traversal refills a warp once this many lanes are idle (1..32)
+    int rayOrder = 0;        // primary rays of a render: 0 in scanline order, 1 in 8 x 4 pixel tiles
 };
 EngineConfig engine_config();
 bool set_engine_config(const EngineConfig& c);

@@ -334,6 +334,11 @@ typedef struct cgs_engine_config {
      * its lanes is busy, so that rays enter a warp in packets of adjacent
      * pixels; 1 refills every idle lane at once. */
     int packet_width;
+    /* Order of a render's primary rays in the ray queue (0 default: scanline;
+     * 1: 8 x 4 pixel tiles, so that a warp's rays are neighbours in both
+     * directions).  Every ray keeps its sample index, so frames are the
+     * same under both. */
+    int ray_order;
 } cgs_engine_config;
 int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
@@ -344,7 +349,8 @@ int cgs_engine_config_set(const cgs_engine_config* config);
  * from the current setting, two rounds over the knobs in turn (passes 1, 2,
  * 4; collect 128, 256 and resolve 64, 128 threads; traversal blocks per SM
  * as many as fit or 768 threads' worth; exact or compressed nodes; queue
- * chunk 32, 48, 64; packet width 1, 8, 16), each knob set to its fastest
+ * chunk 32, 48, 64; packet width 1, 8, 16; scanline or tiled ray order),
+ * each knob set to its fastest
  * value with the others held; a setting already timed is not timed again.
  * Synchronises `stream`. */
 int cgs_autotune_render(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,

@@ -213,7 +213,7 @@ def test_engine_settings_and_autotune(rt, store, torch):
             assert np.abs(got["t"][hit] - ref["t"][hit]).max(initial=0) <= 1e-6 * ref["t"][hit].max(initial=1)
         from cgspline_gb300._capi import CgsError
         for bad in ({"passes": 9}, {"queue_chunk": 12}, {"queue_chunk": 72}, {"queue_chunk": 20},
-                    {"packet_width": 0}, {"packet_width": 33}):
+                    {"packet_width": 0}, {"packet_width": 33}, {"ray_order": 2}):
             with pytest.raises(CgsError):
                 rt.set_engine_config(**bad)
         reqs = [rt.Request.alloc(1, S.camera_c2(), 64, 36), rt.Request.alloc(0, S.camera_c1(), 32, 32)]
@@ -255,6 +255,29 @@ def test_monte_carlo_same_alone_and_in_mix(rt, store, torch):
     torch.cuda.synchronize()
     for a, b in zip(plain, mix):
         assert (a.linear - b.linear).abs().max().item() < 1e-5
+
+
+@pytest.mark.parametrize("sampling", [0, 1])
+def test_tiled_ray_order_gives_same_frames(rt, store, torch, sampling):
+    """Primary rays queued in 8 x 4 pixel tiles instead of scanline order:
+    the same frames, bit for bit (sizes that leave partial tiles, spp > 1,
+    bounces, both bounce models)."""
+    specs = [(1, S.camera_c2(), 93, 53, 1, 2), (0, S.camera_c1(), 37, 22, 3, 1), (1, S.camera_c2(), 8, 4, 2, 1),
+             (1, S.camera_c2(), 5, 3, 1, 0), (0, S.camera_c1(), 64, 33, 1, 3)]
+    base = rt.engine_config()
+    out = {}
+    try:
+        for order in (0, 1):
+            rt.set_engine_config(ray_order=order)
+            reqs = [rt.Request.alloc(g, c, w, h, spp=s, recursion_depth=d, linear=True) for g, c, w, h, s, d in specs]
+            rt.RayTracer(rt.Options(schedule=rt.WAVEFRONT, sampling=sampling)).render_batch(reqs, store)
+            torch.cuda.synchronize()
+            assert store.counters()["device_errors"] == 0
+            out[order] = [(r.linear.clone(), r.framebuffer.clone()) for r in reqs]
+    finally:
+        rt.set_engine_config(**base)
+    for spec, (la, fa), (lb, fb) in zip(specs, out[0], out[1]):
+        assert torch.equal(la, lb) and torch.equal(fa, fb), spec[2:]
 
 
 def test_scene_blob_round_trip(rt, pair, torch, tmp_path):
