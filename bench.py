@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--engine", default=None,
                     help="fixed engine settings for the frame instead of the autotuner's pick, e.g. "
                          "passes=2,collect_threads=256,resolve_threads=128,collect_occupancy=3 (profiling runs)")
+    ap.add_argument("--only", default=None, choices=["batching", "serving", "batch-render"],
+                    help="run only this leg and print its JSON object (profiling runs; no bench line); "
+                         "batch-render: the batching workload's batched render alone, --warmup + --steps times")
     ap.add_argument("--scene", default="c2",
                     help="frame scene: c2 (the torus, default) or c4:<i> / c5:<i>, the seeded union scene i of "
                          "the batching / serving workloads with its camera (profiling cases)")
@@ -619,6 +622,31 @@ def main():
         td.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+
+    if args.only:
+        prec = rt.FP32_POLISH64 if args.precision == "polish64" else rt.FP32
+        if args.engine:
+            rt.set_engine_config(**{k.strip(): int(v) for k, v in (kv.split("=") for kv in args.engine.split(","))})
+        flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+        if args.only == "batch-render":
+            scs = [scenes.scene_c4(i) for i in range(64)]
+            store = rt.GpuScene(scs, device=local)
+            reqs = [rt.Request.alloc(i, c, side, side, 1, DEPTH, device=local)
+                    for i, (c, side) in enumerate(scenes.camera_c4(i) for i in range(64))]
+            tr = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=prec, schedule=rt.WAVEFRONT))
+            for _ in range(max(1, args.warmup)):
+                tr.render_batch(reqs, store)
+                torch.cuda.synchronize()
+            ms = timed(torch, torch.cuda.current_stream(), flush, lambda: tr.render_batch(reqs, store), args.steps)
+            c = store.counters()
+            out = {"Mrays_s": c["rays"] * len(ms) / (sum(ms) * 1e-3) / 1e6, "ms": ms, "counters": c,
+                   "engine_settings": rt.engine_config()}
+        elif args.only == "batching":
+            out = batching_leg(rt, scenes, torch, dev, torch.cuda.current_stream(), prec, flush, steps=args.steps)
+        else:
+            out = serving_leg(rt, scenes, torch, dev, prec)
+        print(json.dumps({args.only: out}), flush=True)
+        return
 
     scene, cam = frame_scene(scenes, args.scene)
     split = rt.SPLIT_LONGEST if args.split == "longest" else rt.SPLIT_REFERENCE

@@ -683,12 +683,16 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
     return true;
 }
 
-static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, float grazeSin, LocalCounters& lc)
+// anyHit: stop at the first root found.  An any-hit query only asks whether
+// the patch has a root before sink.dist, which the first one answers; the
+// reference's search runs on to the closest root and returns the same flag.
+static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, float grazeSin, LocalCounters& lc,
+                                               bool anyHit = false)
 {
     float4 st[kClipStack];
     ClipState c;
     clip_begin(c, sink, tol, grazeSin);
-    while (clip_step(c, st, sink, lc)) {}
+    while (clip_step(c, st, sink, lc) && !(anyHit && c.found)) {}
     return c.found;
 }
 
@@ -770,16 +774,23 @@ __device__ __forceinline__ void dbasis_d(double t, double* w)
 // mixed-precision iterative refinement: the residual S(u,v) - (o + t d) is
 // evaluated in FP64 (Bernstein weights and the tensor sum in double), the 3x3
 // Jacobian [dS/du dS/dv -d] and its solve stay in FP32, and (u,v,t)
-// accumulate in FP64.  An FP32 Jacobian is accurate to ~1e-7 relative, so each
-// step cuts the error by about that factor times the Jacobian's condition
-// number; the iteration stops once the update is below 1e-9 of t (the
-// remaining error is then far below FP32 resolution).  Hits
-// where kPolishSteps such steps do not converge (ill-conditioned, e.g.
-// grazing) continue with up to kPolishSteps64 full-FP64 Newton steps (FP64
-// Jacobian, as the oracle's polish).  The result is kept if it is finite and
-// lies inside the patch domain (1e-6 slack) in front of the origin.
+// accumulate in FP64.  An FP32 Jacobian is accurate to ~1e-7 relative, so a
+// step from an error e leaves about 1e-7 x cond x e + c e^2 (Newton's
+// quadratic term).  The iteration stops once the update is below 1e-9 of t,
+// or after a step whose update was at most kPolishAccept (relative in t,
+// absolute in u + v) on a well-conditioned system (|det| at least
+// kPolishMinSin of |dS/du| |dS/dv|, the ray's direction being a unit vector):
+// the error left is then ~1e-10 relative, far below FP32 resolution, and the
+// step that would only confirm it (a second FP64 residual, the dominant cost
+// on a GPU whose FP64 rate is 1/64 of its FP32 rate) is skipped.  Hits where
+// kPolishSteps such steps do not converge (ill-conditioned, e.g. grazing)
+// continue with up to kPolishSteps64 full-FP64 Newton steps (FP64 Jacobian,
+// as the oracle's polish).  The result is kept if it is finite and lies
+// inside the patch domain (1e-6 slack) in front of the origin.
 constexpr int kPolishSteps = 3;
 constexpr int kPolishSteps64 = 10;
+constexpr double kPolishAccept = 1e-5;
+constexpr float kPolishMinSin = 1e-3f;
 
 // Projected surface point and partials at (U, V) in FP64.
 __device__ __forceinline__ void surface_d(const float4* __restrict__ P, double U, double V, double3& Sp, double3& Su,
@@ -857,6 +868,13 @@ static __device__ __noinline__ bool newton_polish64(const float4* __restrict__ P
         // the last step bounds the error of the previous iterate and contracts
         // by ~1e-7 x the Jacobian's condition: below 1e-9 the result is FP32-exact
         if (fabs(dT) <= 1e-9 * fabs(T) && fabs(dU) + fabs(dV) <= 1e-9) { converged = true; break; }
+        // a small step on a well-conditioned system: the next would only confirm it
+        if (fabs(dT) <= kPolishAccept * fabs(T) && fabs(dU) + fabs(dV) <= kPolishAccept &&
+            fabsf(det) >= kPolishMinSin * len(Su) * len(Sv))
+        {
+            converged = true;
+            break;
+        }
     }
     if (!converged)
     {
@@ -1050,10 +1068,11 @@ __device__ __forceinline__ void to_local(const DevObject& ob, float3 o, float3 d
     scale_inv = s;
 }
 
-__device__ __forceinline__ bool search_patch(HitSink& sink, const Query& q, LocalCounters& lc)
+__device__ __forceinline__ bool search_patch(HitSink& sink, const Query& q, LocalCounters& lc, bool anyHit = false)
 {
     lc.candidates++;
-    return q.method == 0 ? clip_patch(sink, q.tol, graze_sin(q.precision), lc) : subdiv_patch(sink, q.tol, lc);
+    return q.method == 0 ? clip_patch(sink, q.tol, graze_sin(q.precision), lc, anyHit)
+                         : subdiv_patch(sink, q.tol, lc);
 }
 
 // FP64 Newton polish of a world-space hit, done in the object's space.
@@ -1063,16 +1082,20 @@ __device__ __forceinline__ void polish_hit(const DevScene& S, float3 o, float3 d
     const float4* P = S.patches + 16ull * (__ldg(S.patchBase + ob.surface) + uint32_t(hit.patch));
     const float* m = ob.w2l;
     double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
-    double lw = ox * m[3] + oy * m[7] + oz * m[11] + m[15];
-    double3 lo = make_double3((ox * m[0] + oy * m[4] + oz * m[8] + m[12]) / lw,
-                              (ox * m[1] + oy * m[5] + oz * m[9] + m[13]) / lw,
-                              (ox * m[2] + oy * m[6] + oz * m[10] + m[14]) / lw);
+    double3 lo = make_double3(ox * m[0] + oy * m[4] + oz * m[8] + m[12], ox * m[1] + oy * m[5] + oz * m[9] + m[13],
+                              ox * m[2] + oy * m[6] + oz * m[10] + m[14]);
+    // an affine world-to-object matrix (the usual case) has w = 1: no division
+    if (!(m[3] == 0.0f && m[7] == 0.0f && m[11] == 0.0f && m[15] == 1.0f))
+    {
+        const double lw = ox * m[3] + oy * m[7] + oz * m[11] + m[15];
+        lo = make_double3(lo.x / lw, lo.y / lw, lo.z / lw);
+    }
     double3 ld = make_double3(dx * m[0] + dy * m[4] + dz * m[8], dx * m[1] + dy * m[5] + dz * m[9],
                               dx * m[2] + dy * m[6] + dz * m[10]);
-    double sc = sqrt(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z);
-    ld = make_double3(ld.x / sc, ld.y / sc, ld.z / sc);
+    const double sc = sqrt(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z), isc = 1.0 / sc;
+    ld = make_double3(ld.x * isc, ld.y * isc, ld.z * isc);
     double t = double(hit.t) * sc, u = hit.u, v = hit.v;
-    if (newton_polish64(P, lo, ld, t, u, v)) { hit.t = float(t / sc); hit.u = float(u); hit.v = float(v); }
+    if (newton_polish64(P, lo, ld, t, u, v)) { hit.t = float(t * isc); hit.u = float(u); hit.v = float(v); }
 }
 
 // Closest hit over the object-level BVH and each object's patch BVH
@@ -1132,7 +1155,7 @@ __device__ __forceinline__ bool scene_any(const DevScene& S, uint32_t group, flo
         float llimit = lmax;
         auto leaf = [&](uint32_t p) -> bool {
             HitSink sink {patches + 16ull * p, lo, ld, lmax, make_float2(0.0f, 0.0f)};
-            return search_patch(sink, q, lc);
+            return search_patch(sink, q, lc, true);
         };
         return hash_traverse<true>(S, S.bvhs[ob.surface], lo, linv, llimit, leaf, lc);
     };

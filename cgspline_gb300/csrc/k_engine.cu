@@ -521,7 +521,12 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
         if (clipping)
         {
             bool found = false, more = false;
-            if (q.method == 0) { more = clip_step<kG64>(c, stack, sink, lc); found = c.found; }
+            if (q.method == 0)
+            {
+                more = clip_step<kG64>(c, stack, sink, lc);
+                found = c.found;
+                if (kAny && found) more = false;  // an any-hit search ends at its first root
+            }
             else found = subdiv_patch(sink, q.tol, lc);
             if (!more)
             {
