@@ -569,12 +569,6 @@ struct ClipState
     float tol;
     bool found, b64;  // b64: FP64 projection and fat-line bounds (near-grazing)
     bool fresh;       // the net is still to be projected (the search's first step)
-    // Where the projected net is kept for the pops: point i at net[i * netStride]
-    // (a lane's column of a shared-memory array), or null to project it again
-    // from the patch at each pop.  The kept net is the one the first step
-    // projected, so both give the same sub-nets bit for bit.
-    float2* net;
-    uint32_t netStride;
 };
 
 // grazeSin > 0: the precision form (candidates within asin(grazeSin) of
@@ -593,8 +587,6 @@ __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, fl
     c.sl = 0;
     c.it = 0;
     c.found = false;
-    c.net = nullptr;
-    c.netStride = 0;
 }
 
 // Transposes the 4x4 net in registers where t holds.  A cut along v
@@ -675,18 +667,10 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
             a = c.emin.x; b = c.emax.x;
         }
     }
-    if (pop && c.net)
-    {
-#pragma unroll
-        for (int i = 0; i < 16; i++) c.buf[i] = c.net[i * c.netStride];
-    }
-    else if (fresh || pop)
+    if (fresh || pop)
     {
         if (b64) project_net64(c.buf, sink.P, sink.o, sink.d);
         else project_net(c.buf, sink.P, sink.o, sink.d);
-        if (c.net)
-#pragma unroll
-            for (int i = 0; i < 16; i++) c.net[i * c.netStride] = c.buf[i];
     }
     if (fresh)
     {

@@ -424,9 +424,6 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
     const uint32_t n = nDev ? *nDev : n0;
     LocalCounters lc;
     float4 stack[kClipStack];
-    // each lane's projected net, kept for the pops of its search (16 points,
-    // lane-minor: a warp's access is two conflict-free wavefronts)
-    __shared__ float2 nets[16 * kResolveThreads];
     ClipState c;
     HitSink sink {nullptr, f3(0, 0, 0), f3(0, 0, 1), 0.0f, make_float2(0, 0)};
     bool active = false, exhausted = false, clipping = false;
@@ -516,12 +513,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                     sink.dist = kAny ? lmax : lt;
                     sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
                     lc.candidates++;
-                    if (q.method == 0)
-                    {
-                        clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision));
-                        c.net = nets + threadIdx.x;
-                        c.netStride = blockDim.x;
-                    }
+                    if (q.method == 0) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision));
                     clipping = true;
                 }
             }
