@@ -432,7 +432,9 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
     """64 resident scenes (seeded unions of displaced cube-spheres and tori,
     256..65,536 patches each), one request per scene with 64^2..1024^2 primary
     rays + 1 bounce + shadow rays.  Batched: every request in one
-    cgs_render_batch wavefront (replayed from a captured CUDA graph).  Plain:
+    cgs_render_batch wavefront (replayed from a captured CUDA graph), at the
+    engine settings the autotuner picks on this batch for each BVH build (the
+    reference build's pick stays in force afterwards).  Plain:
     one k_render_plain launch per request (the reference's per-frame launch
     shape), back to back; both on the reference's BVH topology, and the
     batched path again on the longest-axis build, with the FP32 + FP64-polish
@@ -451,6 +453,10 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
         out["footprint_mb"] = store.footprint() / 2 ** 20
         reqs = [rt.Request.alloc(i, c, side, side, 1, DEPTH, device=dev.index or 0)
                 for i, (c, side) in enumerate(cams)]
+        # the autotuner picks the engine settings on this batch (outside the timed region)
+        t0 = time.perf_counter()
+        cfg, tms = rt.autotune(store, reqs, rt.Options(recursion_depth=DEPTH, precision=prec), repeats=2)
+        out[f"autotune_{split_name}"] = {"settings": cfg, "ms": tms, "seconds": time.perf_counter() - t0}
         legs = (("batched", rt.WAVEFRONT, prec), ("plain", rt.PLAIN, prec)) if split == rt.SPLIT_REFERENCE else \
             (("batched_split_longest", rt.WAVEFRONT, prec),
              ("batched_split_longest_graze64", rt.WAVEFRONT, rt.FP32_GRAZE64))
@@ -478,6 +484,7 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
             out["accuracy_split_longest"] = accuracy_vs_fp64(rt, store, rays, prec, grp)
             out["accuracy_split_longest_graze64"] = accuracy_vs_fp64(rt, store, rays, rt.FP32_GRAZE64, grp)
         store.close()
+    rt.set_engine_config(**out["autotune_reference"]["settings"])
     out["speedup_vs_plain"] = out["batched"]["value"] / out["plain"]["value"]
     out["speedup_vs_plain_split_longest"] = out["batched_split_longest"]["value"] / out["plain"]["value"]
     out["speedup_vs_plain_split_longest_graze64"] = \
@@ -792,9 +799,9 @@ def main():
             extra["precision"] = precision_leg(rt, scenes, torch, dev, g, scene, flush)
         if args.scene == "c2":
             extra["subdivision"] = subdivision_leg(rt, torch, g, cam, flush, scene, subset)
-        # the traversal occupancy cap leaves room for the wavefront's overlapping
-        # shadow query; the batched and served queries have no such overlap and
-        # run the traversal at full occupancy
+        # the batching leg tunes the engine on its own batch and leaves the
+        # reference build's pick in force for the serving leg; without it the
+        # served requests run the frame's pick with the traversal uncapped
         rt.set_engine_config(collect_occupancy=0)
         if not args.no_batching:
             extra["batching"] = batching_leg(rt, scenes, torch, dev, stream, prec, flush)

@@ -670,9 +670,9 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
                saved.compressedNodes, saved.queueChunk, saved.packetWidth, saved.rayOrder};
     double curMs = score(cur);
     const std::vector<std::pair<int Point::*, std::vector<int>>> knobs {
-        {&Point::passes, {1, 2, 4}}, {&Point::ct, {128, 256}},   {&Point::rt, {64, 128}},
-        {&Point::capped, {0, 1}},    {&Point::cq, {0, 1}},       {&Point::chunk, {32, 48, 64}},
-        {&Point::width, {1, 8, 16}}, {&Point::order, {0, 1}}};
+        {&Point::passes, {1, 2, 4, 8}}, {&Point::ct, {128, 256}},   {&Point::rt, {64, 128}},
+        {&Point::capped, {0, 1}},       {&Point::cq, {0, 1}},       {&Point::chunk, {8, 16, 32, 64}},
+        {&Point::width, {1, 8, 16}},    {&Point::order, {0, 1}}};
     for (int round = 0; round < 2 && status == CGS_OK; round++)
         for (const auto& [field, values] : knobs)
             for (int v : values)

@@ -44,7 +44,7 @@ namespace {
 
 constexpr int kCollectThreads = 256;   // launch bound; runtime block size 128 or 256
 constexpr int kResolveThreads = 128;   // launch bound; runtime block size 64 or 128
-constexpr uint32_t kChunk = 64;        // list entries per ray and pass (the most; EngineConfig::queueChunk)
+constexpr uint32_t kChunk = 64;        // list entries per ray and pass (the most; EngineConfig::queueChunk is the first pass's)
 // One collect step appends at most two entries: a leaf's first patch and,
 // when that patch ends the leaf and nothing is postponed inside the object,
 // the marker that leaves the object.
@@ -67,7 +67,7 @@ struct Eng  // per-ray engine state, SoA over the query's capacity
     int32_t *obj, *lpatch;
     float *leafEntry, *limit, *lt, *lu, *lv;
     uint32_t* ctl;  // per pass: collect fetch, resolve fetch
-    uint32_t chunk;        // list entries a ray may fill per pass (<= kChunk)
+    uint32_t chunk;        // list entries a ray may fill in the first pass; each later pass doubles it (<= kChunk)
     uint32_t packetWidth;  // idle lanes a warp gathers before the traversal refills it
 };
 
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         if (__ballot_sync(0xFFFFFFFFu, active || !exhausted) == 0) break;
         if (!active) continue;
 
-        if (ncand + kMaxAppendsPerStep > E.chunk)
+        if (ncand + kMaxAppendsPerStep > min(kChunk, E.chunk << pass))
         {
             // no room for what one step may append: park before this step
             E.node[rid] = node; E.key[rid] = key; E.post[rid] = post; E.leaf[rid] = leaf;
@@ -695,7 +695,7 @@ bool valid_engine_config(const EngineConfig& c)
     return c.passes >= 1 && c.passes <= kMaxPasses && (c.collectThreads == 128 || c.collectThreads == 256) &&
            (c.resolveThreads == 64 || c.resolveThreads == 128) && c.collectOccupancy >= 0 && c.collectOccupancy <= 32 &&
            c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
-           (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 16 &&
+           (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 8 &&
            c.queueChunk <= int(kChunk) && c.queueChunk % 8 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32 &&
            (c.rayOrder == 0 || c.rayOrder == 1);
 }

@@ -325,9 +325,11 @@ typedef struct cgs_engine_config {
      * both settings give the same hits; the exported BVH is the exact one.
      * The autotuner tries both. */
     int compressed_nodes;
-    /* Candidate-list entries a ray may fill in one collect pass before it
-     * parks (16..64, a multiple of 8; default 64).  Smaller lists park rays
-     * sooner and hand the resolve kernel shorter, more even rows. */
+    /* Candidate-list entries a ray may fill in the first collect pass before
+     * it parks (8..64, a multiple of 8; default 64); each later pass doubles
+     * it, up to 64.  A small first chunk parks a ray after its nearest few
+     * candidates, so that the next pass walks the rest of the tree culled by
+     * the hit the clip found among them. */
     int queue_chunk;
     /* Packet refill (1..32; default 1): the traversal kernel gives a warp's
      * idle lanes new rays only once at least this many are idle, or none of
@@ -347,9 +349,9 @@ int cgs_engine_config_set(const cgs_engine_config* config);
  * renders of it with CUDA events per candidate setting, keeping the fastest
  * (median) as the process-wide setting.  The search is a coordinate descent
  * from the current setting, two rounds over the knobs in turn (passes 1, 2,
- * 4; collect 128, 256 and resolve 64, 128 threads; traversal blocks per SM
+ * 4, 8; collect 128, 256 and resolve 64, 128 threads; traversal blocks per SM
  * as many as fit or 768 threads' worth; exact or compressed nodes; queue
- * chunk 32, 48, 64; packet width 1, 8, 16; scanline or tiled ray order),
+ * chunk 8, 16, 32, 64; packet width 1, 8, 16; scanline or tiled ray order),
  * each knob set to its fastest
  * value with the others held; a setting already timed is not timed again.
  * Synchronises `stream`. */

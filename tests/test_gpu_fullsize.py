@@ -57,6 +57,7 @@ def test_engine_settings_agree_at_full_size(setup):
                     {"passes": 2, "backtrack_cache": 1, "packet_width": 8},
                     {"passes": 2, "backtrack_cache": 1, "queue_chunk": 16, "packet_width": 8},
                     {"passes": 1, "backtrack_cache": 1, "queue_chunk": 40, "packet_width": 32},
+                    {"passes": 8, "backtrack_cache": 1, "queue_chunk": 8, "packet_width": 8, "ray_order": 1},
                     {"passes": 4, "backtrack_cache": 0, "queue_chunk": 32, "packet_width": 16,
                      "compressed_nodes": 1}):
             rt.set_engine_config(**{**base, **cfg})
