@@ -637,7 +637,8 @@ def main():
         flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
         if args.only == "batch-render":
             scs = [scenes.scene_c4(i) for i in range(64)]
-            store = rt.GpuScene(scs, device=local)
+            store = rt.GpuScene(scs, device=local,
+                                split=rt.SPLIT_LONGEST if args.split == "longest" else rt.SPLIT_REFERENCE)
             reqs = [rt.Request.alloc(i, c, side, side, 1, DEPTH, device=local)
                     for i, (c, side) in enumerate(scenes.camera_c4(i) for i in range(64))]
             tr = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=prec, schedule=rt.WAVEFRONT))
