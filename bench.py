@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--engine", default=None,
                     help="fixed engine settings for the frame instead of the autotuner's pick, e.g. "
                          "passes=2,collect_threads=256,resolve_threads=128,collect_occupancy=3 (profiling runs)")
-    ap.add_argument("--only", default=None, choices=["batching", "serving", "batch-render"],
+    ap.add_argument("--only", default=None, choices=["batching", "serving", "batch-render", "precision"],
                     help="run only this leg and print its JSON object (profiling runs; no bench line); "
                          "batch-render: the batching workload's batched render alone, --warmup + --steps times")
     ap.add_argument("--scene", default="c2",
@@ -649,6 +649,9 @@ def main():
             c = store.counters()
             out = {"Mrays_s": c["rays"] * len(ms) / (sum(ms) * 1e-3) / 1e6, "ms": ms, "counters": c,
                    "engine_settings": rt.engine_config()}
+        elif args.only == "precision":
+            sc = scenes.scene_c2()
+            out = precision_leg(rt, scenes, torch, dev, rt.GpuScene(sc, device=local), sc, flush)
         elif args.only == "batching":
             out = batching_leg(rt, scenes, torch, dev, torch.cuda.current_stream(), prec, flush, steps=args.steps)
         else:

@@ -503,10 +503,10 @@ __device__ __forceinline__ double3 unit3d(double3 a)
     return l != 0.0 ? make_double3(a.x / l, a.y / l, a.z / l) : a;
 }
 
-// project_net with the axes and dot products in double, rounded to float.
-__device__ __forceinline__ void project_net64(float2* net, const float4* __restrict__ P, float3 o, float3 d)
+// project_net with the axes and dot products in double, rounded to float, on
+// a ray given in double.
+__device__ __forceinline__ void project_net64(float2* net, const float4* __restrict__ P, double3 o, double3 dd)
 {
-    const double3 dd = make_double3(d.x, d.y, d.z);
     const double3 a0 = unit3d(cross_d(dd, make_double3(dd.x, dd.y, dd.z + 8.0)));
     const double3 a1 = unit3d(cross_d(dd, a0));
 #pragma unroll
@@ -516,6 +516,32 @@ __device__ __forceinline__ void project_net64(float2* net, const float4* __restr
         const double3 Q = make_double3(double(q.x) - o.x, double(q.y) - o.y, double(q.z) - o.z);
         net[i] = make_float2(float(dot_d(a0, Q)), float(dot_d(a1, Q)));
     }
+}
+
+// A ray in an object's space computed in double from the FP32 world ray: the
+// origin through the world-to-object matrix, the direction through its 3x3
+// part, normalised.  The FP32 object-space ray rounds each of these, and on a
+// near-grazing ray that one-ulp turn of the direction moves the line across a
+// tangent root; the precision form projects near-grazing candidates from
+// this ray instead.
+struct Ray64 { double3 o, d; };
+__device__ __forceinline__ Ray64 to_local64(const DevObject& ob, float3 o, float3 d)
+{
+    const float* m = ob.w2l;
+    const double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+    Ray64 r;
+    r.o = make_double3(ox * m[0] + oy * m[4] + oz * m[8] + m[12], ox * m[1] + oy * m[5] + oz * m[9] + m[13],
+                       ox * m[2] + oy * m[6] + oz * m[10] + m[14]);
+    if (!(m[3] == 0.0f && m[7] == 0.0f && m[11] == 0.0f && m[15] == 1.0f))
+    {
+        const double lw = ox * m[3] + oy * m[7] + oz * m[11] + m[15];
+        r.o = make_double3(r.o.x / lw, r.o.y / lw, r.o.z / lw);
+    }
+    const double3 ld = make_double3(dx * m[0] + dy * m[4] + dz * m[8], dx * m[1] + dy * m[5] + dz * m[9],
+                                    dx * m[2] + dy * m[6] + dz * m[10]);
+    const double il = 1.0 / sqrt(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z);
+    r.d = make_double3(ld.x * il, ld.y * il, ld.z * il);
+    return r;
 }
 
 // The precision form's near-grazing test of a candidate: the ray within
@@ -569,17 +595,33 @@ struct ClipState
     float tol;
     bool found, b64;  // b64: FP64 projection and fat-line bounds (near-grazing)
     bool fresh;       // the net is still to be projected (the search's first step)
+    // b64: the ray the net is projected from (origin, direction), kept in
+    // local memory: read only where a projection starts, it would otherwise
+    // hold twelve registers through the whole search
+    volatile double ray64[6];
 };
 
 // grazeSin > 0: the precision form (candidates within asin(grazeSin) of
 // grazing get the FP64 bounds).  kG64 = false compiles the FP64 path out
 // (searches that never take it: a smaller loop body for the instruction
 // cache).
+// ob, wo, wd: the candidate's object and the world ray, from which a
+// near-grazing candidate's ray is recomputed in double (to_local64); a null
+// ob projects it from the FP32 ray in the sink.
 template<bool kG64 = true>
-__device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, float tol, float grazeSin)
+__device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, float tol, float grazeSin,
+                                           const DevObject* ob = nullptr, float3 wo = {}, float3 wd = {})
 {
     c.b64 = kG64 && grazeSin > 0.0f && near_grazing(sink.P, sink.d, grazeSin);
     c.tol = c.b64 ? kGrazeTol : tol;
+    if (kG64 && c.b64)
+    {
+        Ray64 r;
+        if (ob) r = to_local64(*ob, wo, wd);
+        else r = Ray64 {make_double3(sink.o.x, sink.o.y, sink.o.z), make_double3(sink.d.x, sink.d.y, sink.d.z)};
+        c.ray64[0] = r.o.x; c.ray64[1] = r.o.y; c.ray64[2] = r.o.z;
+        c.ray64[3] = r.d.x; c.ray64[4] = r.d.y; c.ray64[5] = r.d.z;
+    }
     c.fresh = true;  // the first clip_step projects the net
     c.emin = make_float2(0.0f, 0.0f);
     c.emax = make_float2(1.0f, 1.0f);
@@ -669,7 +711,9 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
     }
     if (fresh || pop)
     {
-        if (b64) project_net64(c.buf, sink.P, sink.o, sink.d);
+        if (b64)
+            project_net64(c.buf, sink.P, make_double3(c.ray64[0], c.ray64[1], c.ray64[2]),
+                          make_double3(c.ray64[3], c.ray64[4], c.ray64[5]));
         else project_net(c.buf, sink.P, sink.o, sink.d);
     }
     if (fresh)
@@ -687,11 +731,12 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
 // the patch has a root before sink.dist, which the first one answers; the
 // reference's search runs on to the closest root and returns the same flag.
 static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, float grazeSin, LocalCounters& lc,
-                                               bool anyHit = false)
+                                               bool anyHit = false, const DevObject* ob = nullptr, float3 wo = {},
+                                               float3 wd = {})
 {
     float4 st[kClipStack];
     ClipState c;
-    clip_begin(c, sink, tol, grazeSin);
+    clip_begin(c, sink, tol, grazeSin, ob, wo, wd);
     while (clip_step(c, st, sink, lc) && !(anyHit && c.found)) {}
     return c.found;
 }
@@ -1068,10 +1113,11 @@ __device__ __forceinline__ void to_local(const DevObject& ob, float3 o, float3 d
     scale_inv = s;
 }
 
-__device__ __forceinline__ bool search_patch(HitSink& sink, const Query& q, LocalCounters& lc, bool anyHit = false)
+__device__ __forceinline__ bool search_patch(HitSink& sink, const Query& q, LocalCounters& lc, bool anyHit = false,
+                                             const DevObject* ob = nullptr, float3 wo = {}, float3 wd = {})
 {
     lc.candidates++;
-    return q.method == 0 ? clip_patch(sink, q.tol, graze_sin(q.precision), lc, anyHit)
+    return q.method == 0 ? clip_patch(sink, q.tol, graze_sin(q.precision), lc, anyHit, ob, wo, wd)
                          : subdiv_patch(sink, q.tol, lc);
 }
 
@@ -1117,7 +1163,11 @@ __device__ __forceinline__ int scene_closest(const DevScene& S, uint32_t group, 
         const float3 linv = f3(1.0f / ld.x, 1.0f / ld.y, 1.0f / ld.z);
         auto leaf = [&](uint32_t p) -> bool {
             HitSink sink {patches + 16ull * p, lo, ld, lt, make_float2(lu, lv)};
-            if (search_patch(sink, q, lc)) { lt = sink.dist; lu = sink.uv.x; lv = sink.uv.y; lp = p; return true; }
+            if (search_patch(sink, q, lc, false, &ob, o, d))
+            {
+                lt = sink.dist; lu = sink.uv.x; lv = sink.uv.y; lp = p;
+                return true;
+            }
             return false;
         };
         bool b = hash_traverse<false>(S, S.bvhs[ob.surface], lo, linv, lt, leaf, lc);

@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                     sink.dist = kAny ? lmax : lt;
                     sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
                     lc.candidates++;
-                    if (q.method == 0) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision));
+                    if (q.method == 0) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision), &S.objects[obj], o, d);
                     clipping = true;
                 }
             }

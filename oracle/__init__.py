@@ -40,6 +40,13 @@ def set_graze_mode(mode: int):
     the nine control-net cells' normals, with silhouettes; 0 the diagonals'
     plane alone."""
     lib().ora_set_graze_mode(int(mode))
+
+
+def set_graze64_ray(on: int):
+    """CLIP_GRAZE64: project a near-grazing candidate from the object-space
+    ray computed in double from the world ray (1, the default), or from the
+    FP32 one (0)."""
+    lib().ora_set_graze64_ray(int(on))
 GRAZE_5, GRAZE_30 = 0.0871557427, 0.5
 FP32, FP32_POLISH64, FP64 = 0, 1, 2
 
@@ -93,6 +100,7 @@ def lib():
         L.ora_patch_intersect.argtypes = [fp, u32, fp, C.c_float, C.c_int, P, P, P]
         L.ora_patch_subdiv_host.argtypes = [fp, u32, fp, C.c_float, P, P]
         L.ora_set_graze_mode.argtypes = [C.c_int]
+        L.ora_set_graze64_ray.argtypes = [C.c_int]
         L.ora_patch_eval.argtypes = [fp, C.c_float, C.c_float, fp, fp]
         _lib = L
     return _lib

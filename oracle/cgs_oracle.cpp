@@ -709,8 +709,15 @@ template<class R> inline bool grazing(const V4<R> P[16], V3<R> d)
 // src/Spline_BezierClipping.cu:46-114 and src/Spline_Subdivision.cu:111-165:
 // project the 16 points onto two planes that contain the ray, then run the
 // 2-D search with an onHit that keeps the closest point in front.
+// ray64 (optional): the same ray in object space computed in double from the
+// world ray; a near-grazing candidate's FP64 projection then starts from it
+// instead of from the FP32 object-space ray (restates to_local64 and its use
+// in the CUDA path's precision form; 0 gives the projection from the FP32
+// ray, for comparison).
+static int g_graze64Ray = 1;
 template<class R>
-bool intersect_patch(R& distance, V2<R>& uv, const Ray<R>& ray, const V4<R> P[16], R tol, int method, ClipStats* st)
+bool intersect_patch(R& distance, V2<R>& uv, const Ray<R>& ray, const V4<R> P[16], R tol, int method, ClipStats* st,
+                     const Ray<double>* ray64 = nullptr)
 {
     const V3<R> d = ray.d;
     const V3<R> axis0 = versor(cross(d, d + V3<R>{0, 0, 8}));
@@ -723,7 +730,7 @@ bool intersect_patch(R& distance, V2<R>& uv, const Ray<R>& ray, const V4<R> P[16
     }
     if (method == kClipDeviceB64P)
     {
-        const V3<double> dd = cast3<double>(d), oo = cast3<double>(ray.o);
+        const V3<double> dd = ray64 ? ray64->d : cast3<double>(d), oo = ray64 ? ray64->o : cast3<double>(ray.o);
         const V3<double> a0 = versor(cross(dd, dd + V3<double>{0, 0, 8}));
         const V3<double> a1 = versor(cross(dd, a0));
         for (int i = 0; i < 16; i++)
@@ -1323,13 +1330,24 @@ inline int scene_intersect(const Scene& sc, Hit& hit0, const Ray<float>& ray0, c
         d = 1 / d;
         lr.d = lr.d * d;
         float lt = lr.max;
+        Ray<double> lr64;
+        const bool use64 = g_graze64Ray && q.method == kClipGraze;
+        if (use64)
+        {
+            M4<double> M64 = load_m4<double>(ob.w2l);
+            V4<double> o64 {double(ray0.o.x), double(ray0.o.y), double(ray0.o.z), 1.0};
+            lr64.o = project(mul(M64, o64));
+            lr64.d = mul(upper3(M64), cast3<double>(ray0.d));
+            lr64.d = lr64.d * (1.0 / length(lr64.d));
+        }
         uint32_t lpatch = 0; V2<float> luv {0, 0};
         auto leaf = [&](uint32_t p) -> bool {
             if (cn) cn->candidates++;
             V4<float> P[16];
             s.patch(p, P);
             float dist = lt; V2<float> uv = luv;
-            if (intersect_patch<float>(dist, uv, lr, P, q.tol, q.method, cn ? &cn->cs : nullptr))
+            if (intersect_patch<float>(dist, uv, lr, P, q.tol, q.method, cn ? &cn->cs : nullptr,
+                                       use64 ? &lr64 : nullptr))
             {
                 lpatch = p; lt = dist; luv = uv;
                 return true;
@@ -1758,6 +1776,9 @@ void ora_philox(uint32_t* ctr4, uint32_t k0, uint32_t k1) { philox(ctr4, k0, k1)
 void ora_set_graze_sin(float s) { g_grazeSin = s; }
 // the near-grazing test of CLIP_GRAZE64 (process-wide; see grazing())
 void ora_set_graze_mode(int m) { g_grazeMode = m; }
+// CLIP_GRAZE64: project a near-grazing candidate from the object-space ray
+// computed in double (1, the default) or from the FP32 one (0)
+void ora_set_graze64_ray(int m) { g_graze64Ray = m; }
 
 static const BVH* pick_bvh(const Scene* s, int which)
 {
