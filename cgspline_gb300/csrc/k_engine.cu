@@ -69,6 +69,7 @@ struct Eng  // per-ray engine state, SoA over the query's capacity
     uint32_t* ctl;  // per pass: collect fetch, resolve fetch
     uint32_t chunk;        // list entries a ray may fill in the first pass; each later pass doubles it (<= kChunk)
     uint32_t packetWidth;  // idle lanes a warp gathers before the traversal refills it
+    uint32_t originLast;   // any hit: search candidates whose leaf box holds the ray's origin last
 };
 
 constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 16;
@@ -427,6 +428,9 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
     ClipState c;
     HitSink sink {nullptr, f3(0, 0, 0), f3(0, 0, 1), 0.0f, make_float2(0, 0)};
     bool active = false, exhausted = false, clipping = false;
+    // any hit with E.originLast: sweep 0 searches the candidates whose leaf box
+    // holds the ray's origin (entry <= 0) not, sweep 1 only those
+    bool sweep = false;
     uint32_t rid = 0, k = 0, count = 0, patch = 0;
     int32_t obj = -1, lpatch = -1;
     float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
@@ -451,6 +455,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                     k = 0;
                     obj = -1;
                     clipping = false;
+                    sweep = false;
                     load_ray(rays, rid, o, d, tmax);
                     limit = kAny ? tmax : (pass == 0 ? tmax : E.limit[rid]);
                     list = E.list + size_t(rid) * kChunk;
@@ -467,6 +472,13 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
         // as many lanes as possible.
         while (!clipping && !finished)
         {
+            if (kAny && k >= count && E.originLast && !sweep)
+            {
+                sweep = true;  // the candidates whose leaf box holds the origin, last
+                k = 0;
+                obj = -1;
+                continue;
+            }
             if (k >= count)
             {
                 // end of this pass's chunk: keep what the next pass needs
@@ -506,7 +518,8 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
             {
                 patch = e.x;
                 const float entry = __uint_as_float(e.y);
-                if (entry < (kAny ? lmax : lt))
+                const bool turn = !kAny || !E.originLast || ((entry <= 0.0f) == sweep);
+                if (turn && entry < (kAny ? lmax : lt))
                 {
                     const uint32_t surface = S.objects[obj].surface;
                     sink.P = S.patches + 16ull * (__ldg(S.patchBase + surface) + patch);
@@ -697,7 +710,7 @@ bool valid_engine_config(const EngineConfig& c)
            c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
            (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 8 &&
            c.queueChunk <= int(kChunk) && c.queueChunk % 8 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32 &&
-           (c.rayOrder == 0 || c.rayOrder == 1);
+           (c.rayOrder == 0 || c.rayOrder == 1) && (c.originLast == 0 || c.originLast == 1);
 }
 
 bool set_engine_config(const EngineConfig& c)
@@ -733,6 +746,7 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
         const EngineConfig ec = engine_config();
         E.chunk = uint32_t(ec.queueChunk);
         E.packetWidth = uint32_t(ec.packetWidth);
+        E.originLast = uint32_t(ec.originLast);
     }
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const int flat = sms() * 4;
@@ -760,6 +774,7 @@ cudaError_t run_traverse(const DevScene& S, RaysSoA rays, uint32_t n, bool any, 
         const EngineConfig ec = engine_config();
         E.chunk = uint32_t(ec.queueChunk);
         E.packetWidth = uint32_t(ec.packetWidth);
+        E.originLast = uint32_t(ec.originLast);
     }
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const EngineConfig c = engine_config();

@@ -341,6 +341,13 @@ typedef struct cgs_engine_config {
      * directions).  Every ray keeps its sample index, so frames are the
      * same under both. */
     int ray_order;
+    /* Any-hit queries (shadow rays): 1 searches a ray's candidates whose leaf
+     * box holds its origin after the others (0 default: in traversal order).
+     * A shadow ray starts on the surface it leaves, and the search of that
+     * patch converges on the root just behind the origin before rejecting
+     * it; an occluder found first ends the ray without it.  The order does
+     * not change an any-hit answer. */
+    int origin_last;
 } cgs_engine_config;
 int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
@@ -351,7 +358,8 @@ int cgs_engine_config_set(const cgs_engine_config* config);
  * from the current setting, two rounds over the knobs in turn (passes 1, 2,
  * 4, 8; collect 128, 256 and resolve 64, 128 threads; traversal blocks per SM
  * as many as fit or 768 threads' worth; exact or compressed nodes; queue
- * chunk 8, 16, 32, 64; packet width 1, 8, 16; scanline or tiled ray order),
+ * chunk 8, 16, 32, 64; packet width 1, 8, 16; scanline or tiled ray order;
+ * any-hit candidates in traversal order or origin boxes last),
  * each knob set to its fastest
  * value with the others held; a setting already timed is not timed again.
  * Synchronises `stream`. */

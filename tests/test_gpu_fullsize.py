@@ -180,3 +180,33 @@ def test_render_host_into_caller_buffers(setup):
     fb1, lin1 = tr.render_host(S.camera_c2(), g, 640, 360, out=(fb, lin))
     assert fb1 is fb and lin1 is lin
     assert np.array_equal(fb0, fb) and np.array_equal(lin0, lin)
+
+
+def test_origin_last_keeps_any_hit_answers(setup):
+    """Shadow rays from every primary hit of the frame toward the first light
+    (origin offset 1e-4 along the light direction, bounded by the light's
+    distance): searching the candidates whose leaf box holds the origin last
+    gives the same any-hit answer for every ray, with no more clip
+    iterations."""
+    rt, torch, g, rays = setup
+    h = g.intersect(rays)
+    hit = h["patch"] >= 0
+    P = rays[:3, hit] + rays[3:6, hit] * h["t"][hit]
+    light = torch.tensor(S.scene_c2().lights[0].position, dtype=torch.float32, device=P.device)[:, None]
+    L = light - P
+    dist = L.norm(dim=0)
+    L = L / dist
+    shadow = torch.cat([P + 1e-4 * L, L, dist[None]], 0).contiguous()
+    base = rt.engine_config()
+    out = {}
+    try:
+        for ol in (0, 1):
+            rt.set_engine_config(origin_last=ol)
+            a = host(g.intersect(shadow, any_hit=True))
+            out[ol] = (a["patch"] >= 0, g.counters())
+    finally:
+        rt.set_engine_config(**base)
+    assert np.array_equal(out[0][0], out[1][0])
+    assert 0.01 < out[0][0].mean() < 0.99
+    assert out[1][1]["iterations"] <= out[0][1]["iterations"]
+    assert out[0][1]["device_errors"] == 0 and out[1][1]["device_errors"] == 0
