@@ -719,22 +719,7 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
     if (fresh)
     {
         c.fresh = false;
-        // A projected net whose bounding box lies clear of the origin on one
-        // side of an axis, by more than 2^-20 of its largest coordinate, has
-        // no root, and the search would find none: every sub-net it derives
-        // is a convex combination of these points (the slicing weights are
-        // non-negative), so it stays on that side, where no corner triangle
-        // can hold the origin.  The search ends here instead of clipping its
-        // way to that answer.
-        float x0 = c.buf[0].x, x1 = x0, y0 = c.buf[0].y, y1 = y0;
-#pragma unroll
-        for (int i = 1; i < 16; i++)
-        {
-            x0 = fminf(x0, c.buf[i].x); x1 = fmaxf(x1, c.buf[i].x);
-            y0 = fminf(y0, c.buf[i].y); y1 = fmaxf(y1, c.buf[i].y);
-        }
-        const float m = 0x1p-20f * fmaxf(fmaxf(-x0, x1), fmaxf(-y0, y1));
-        return !(x0 > m || x1 < -m || y0 > m || y1 < -m);
+        return true;
     }
     subpatchU(c.buf, a, b);  // every lane: the cut, or the u range of the popped sub-net
     if (pop) subpatchV(c.buf, c.emin.y, c.emax.y);
