@@ -356,14 +356,20 @@ struct HitSink
     }
 };
 
-// approximateIntersection, src/Spline.h:739-765
-__device__ __forceinline__ bool approximateIntersection(HitSink& sink, const float2* p, float2 pmin, float2 pmax)
+// approximateIntersection, src/Spline.h:739-765, on the net's corner points
+// p0 = p[0], p3 = p[3], p12 = p[12], p15 = p[15]
+__device__ __forceinline__ bool approximateIntersection(HitSink& sink, float2 p0, float2 p3, float2 p12, float2 p15,
+                                                        float2 pmin, float2 pmax)
 {
     bool found = false;
     float2 coord, psize = pmax - pmin;
-    if (triangleOriginIntersection(coord, p[0], p[3], p[12])) found |= sink(pmin + coord * psize);
-    if (triangleOriginIntersection(coord, p[15], p[12], p[3])) found |= sink(pmax - coord * psize);
+    if (triangleOriginIntersection(coord, p0, p3, p12)) found |= sink(pmin + coord * psize);
+    if (triangleOriginIntersection(coord, p15, p12, p3)) found |= sink(pmax - coord * psize);
     return found;
+}
+__device__ __forceinline__ bool approximateIntersection(HitSink& sink, const float2* p, float2 pmin, float2 pmax)
+{
+    return approximateIntersection(sink, p[0], p[3], p[12], p[15], pmin, pmax);
 }
 
 // Project the 16 control points onto two planes containing the ray
@@ -595,6 +601,7 @@ struct ClipState
     float tol;
     bool found, b64;  // b64: FP64 projection and fat-line bounds (near-grazing)
     bool fresh;       // the net is still to be projected (the search's first step)
+    bool tposed;      // buf holds the transposed net (left so by a cut along v)
     // b64: the ray the net is projected from (origin, direction), kept in
     // local memory: read only where a projection starts, it would otherwise
     // hold twelve registers through the whole search
@@ -623,6 +630,7 @@ __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, fl
         c.ray64[3] = r.d.x; c.ray64[4] = r.d.y; c.ray64[5] = r.d.z;
     }
     c.fresh = true;  // the first clip_step projects the net
+    c.tposed = false;
     c.emin = make_float2(0.0f, 0.0f);
     c.emax = make_float2(1.0f, 1.0f);
     c.cutsideStack = 0;
@@ -652,6 +660,11 @@ __device__ __forceinline__ void transpose_if(float2* p, bool t)
 // (clip_begin leaves that to it), at the same place in the code as the
 // re-projection after a pop, so lanes starting a search and lanes popping a
 // sub-net share those instructions; it is not counted as an iteration.
+// A cut along v leaves the net transposed (c.tposed); the next step
+// transposes it only if its own cut needs the other orientation, so a step
+// moves the net at most once, and the sub-net of a pop is derived in the
+// natural orientation.  A loop iteration costs the union of the paths its
+// lanes take, so the transposes are kept off the paths that differ.
 template<bool kG64 = true>
 __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, LocalCounters& lc)
 {
@@ -666,11 +679,14 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
         lc.iterations++;
         tr = (c.cutsideStack & 1) != 0;  // this step cuts along v
         pop = true;
-        if (len2(c.buf[3] - c.buf[12]) < c.tol && len2(c.buf[15] - c.buf[0]) < c.tol)
-            c.found |= approximateIntersection(sink, c.buf, c.emin, c.emax);
+        // the corners in the natural orientation (a transpose swaps p3 and p12)
+        const float2 p3 = c.tposed ? c.buf[12] : c.buf[3], p12 = c.tposed ? c.buf[3] : c.buf[12];
+        if (len2(p3 - p12) < c.tol && len2(c.buf[15] - c.buf[0]) < c.tol)
+            c.found |= approximateIntersection(sink, c.buf[0], p3, p12, c.buf[15], c.emin, c.emax);
         else
         {
-            transpose_if(c.buf, tr);
+            transpose_if(c.buf, tr != c.tposed);
+            c.tposed = tr;
             float lower, upper;
             if (b64) clip_range64(c.buf, 0, lower, upper);
             else clip_range(c.buf, 0, lower, upper);
@@ -715,6 +731,7 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
             project_net64(c.buf, sink.P, make_double3(c.ray64[0], c.ray64[1], c.ray64[2]),
                           make_double3(c.ray64[3], c.ray64[4], c.ray64[5]));
         else project_net(c.buf, sink.P, sink.o, sink.d);
+        c.tposed = false;
     }
     if (fresh)
     {
@@ -723,7 +740,6 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
     }
     subpatchU(c.buf, a, b);  // every lane: the cut, or the u range of the popped sub-net
     if (pop) subpatchV(c.buf, c.emin.y, c.emax.y);
-    else transpose_if(c.buf, tr);
     return true;
 }
 
