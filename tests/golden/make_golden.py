@@ -21,13 +21,19 @@ committed files).
   teaset_golden.npz  the reference's own teaset scene (assets/scenes/
                      Teaset01.dl with the .be surfaces it names): the scene's
                      surfaces, objects, light and camera, closest hits of
-                     160x90 camera rays and a 96x54 frame.
+                     160x90 camera rays and a 96x54 frame;
+  test32_golden.npz, test152_golden.npz
+                     the reference's test scenes assets/scenes/Test32.dl and
+                     Test152.dl (32 and 152 teaset pieces on the long-wave
+                     floor, 11 and 51 lights), stored the same way: closest
+                     and any hits of 160x90 camera rays and a 96x54 frame.
 
 The seeded scenes are regenerated by the tests from cgspline_gb300.scenes;
 each file stores a SHA-256 of the scene arrays so that a changed generator is
 caught.  The teaset's geometry is stored in the file itself.
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [name ...]   (default: every file; names:
+      c1 torus32 union teaset test32 test152)
 """
 import os
 import sys
@@ -47,9 +53,25 @@ from cgspline_gb300 import scenes as S  # noqa: E402
 REFERENCE_ROOT = os.environ.get("CGS_REFERENCE_ROOT", "/root/reference")
 
 
-def teaset():
+def dl_scene(file):
     from cgspline_gb300 import dl
-    return dl.load_dl(os.path.join(REFERENCE_ROOT, "assets", "scenes", "Teaset01.dl"))
+    return dl.load_dl(os.path.join(REFERENCE_ROOT, "assets", "scenes", file))
+
+
+def write_stored(name, sc, cam, size=(160, 90), frame=(96, 54)):
+    """A fixture that stores its scene (surfaces, objects, lights, environment)."""
+    print(f"{name}_golden.npz: {sc.patch_count} patches, {len(sc.objects)} objects, {len(sc.lights)} lights")
+    out = reference_outputs(sc, cam, *size, *frame)
+    geo = {}
+    for k, s in enumerate(sc.surfaces):
+        geo[f"surface{k}_points"] = s.points
+        geo[f"surface{k}_indices"] = s.indices
+    objs = np.array([[o.surface, *o.local2world, *o.world2local, *o.material.packed()] for o in sc.objects],
+                    np.float32)
+    lights = np.array([l.packed() for l in sc.lights], np.float32)
+    np.savez_compressed(os.path.join(HERE, f"{name}_golden.npz"), surfaces=np.int32(len(sc.surfaces)), objects=objs,
+                        lights=lights, background=np.asarray(sc.background, np.float32),
+                        ambient=np.asarray(sc.ambient, np.float32), scene_sha=np.bytes_(scene_sha(sc)), **geo, **out)
 
 
 def same_hits(a, b, keys=("t", "u", "v", "patch", "object")):
@@ -84,11 +106,8 @@ def reference_outputs(sc, cam, w, h, fw, fh, depth=1):
                 pinned_by_reference=np.int32(1))
 
 
-def main():
-    if not R.available():
-        raise SystemExit(f"the reference build is needed: {R.unavailable_reason()}")
-
-    # C1: the inputs, BVH and hash in the file (as before), checked against the reference
+def write_c1():
+    """C1: the inputs, BVH and hash in the file, checked against the reference."""
     sc = S.scene_c1()
     o = oracle.OracleScene(sc)
     r = R.RefScene(sc)
@@ -107,26 +126,29 @@ def main():
                         t=hr["t"], u=hr["u"], v=hr["v"], patch=hr["patch"], pinned_by_reference=np.int32(1))
     print("c1_golden.npz: hits", int((hr["patch"] >= 0).sum()), "of", rays.shape[1], "(reference == oracle)")
 
+
+def main():
+    if not R.available():
+        raise SystemExit(f"the reference build is needed: {R.unavailable_reason()}")
+    # optional arguments: the fixture names to write (default: all)
+    only = set(sys.argv[1:])
+
+    if not only or "c1" in only:
+        write_c1()
+
     for name, make, size, frame in (("torus32", torus32, (160, 90), (64, 36)),
                                     ("union", union5, (96, 96), (64, 64))):
+        if only and name not in only:
+            continue
         sc, cam = make()
         print(f"{name}_golden.npz: {sc.patch_count} patches, {len(sc.objects)} objects")
         out = reference_outputs(sc, cam, *size, *frame)
         np.savez_compressed(os.path.join(HERE, f"{name}_golden.npz"), scene_sha=np.bytes_(scene_sha(sc)), **out)
 
-    sc, cam = teaset()
-    print(f"teaset_golden.npz: {sc.patch_count} patches, {len(sc.objects)} objects")
-    out = reference_outputs(sc, cam, 160, 90, 96, 54)
-    geo = {}
-    for k, s in enumerate(sc.surfaces):
-        geo[f"surface{k}_points"] = s.points
-        geo[f"surface{k}_indices"] = s.indices
-    objs = np.array([[o.surface, *o.local2world, *o.world2local, *o.material.packed()] for o in sc.objects],
-                    np.float32)
-    lights = np.array([l.packed() for l in sc.lights], np.float32)
-    np.savez_compressed(os.path.join(HERE, "teaset_golden.npz"), surfaces=np.int32(len(sc.surfaces)), objects=objs,
-                        lights=lights, background=np.asarray(sc.background, np.float32),
-                        ambient=np.asarray(sc.ambient, np.float32), scene_sha=np.bytes_(scene_sha(sc)), **geo, **out)
+    for name, file in (("teaset", "Teaset01.dl"), ("test32", "Test32.dl"), ("test152", "Test152.dl")):
+        if only and name not in only:
+            continue
+        write_stored(name, *dl_scene(file))
 
 
 if __name__ == "__main__":

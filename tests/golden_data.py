@@ -10,7 +10,9 @@ import numpy as np
 from cgspline_gb300 import scenes as S
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-NAMES = ("torus32", "union", "teaset")
+NAMES = ("torus32", "union", "teaset", "test32", "test152")
+# fixtures that store their scene (the reference's own .dl scenes)
+STORED = ("teaset", "test32", "test152")
 
 
 def load(name: str):
@@ -52,8 +54,8 @@ def camera(packed):
     return S.Camera(tuple(p[0:4]), tuple(p[4:7]), tuple(p[7:10]), p[10])
 
 
-def teaset_scene(g):
-    """The teaset scene stored in teaset_golden.npz."""
+def stored_scene(g, name="teaset"):
+    """The scene stored in a fixture of STORED."""
     surfaces = [S.Surface(g[f"surface{k}_points"], g[f"surface{k}_indices"]) for k in range(int(g["surfaces"]))]
     objects = []
     for row in g["objects"]:
@@ -63,7 +65,7 @@ def teaset_scene(g):
     lights = [S.Light(tuple(l[0:3]), float(l[3]), tuple(l[4:7]), float(l[7]), tuple(l[8:11]), float(l[11]))
               for l in g["lights"]]
     return S.Scene(surfaces, objects, lights, tuple(float(x) for x in g["background"]),
-                   tuple(float(x) for x in g["ambient"]), name="teaset")
+                   tuple(float(x) for x in g["ambient"]), name=name)
 
 
 def scene(name: str, g):
@@ -73,7 +75,7 @@ def scene(name: str, g):
     elif name == "union":
         sc, _ = union5()
     else:
-        sc = teaset_scene(g)
+        sc = stored_scene(g, name)
     if scene_sha(sc) != bytes(g["scene_sha"]).decode():
         raise AssertionError(f"{name}: the scene generator no longer gives the fixture's scene")
     return sc, camera(g["camera"])

@@ -86,6 +86,18 @@ def test_oracle_matches_reference_union_scene(oracle_mod, index):
 
 
 @needs_ref
+@pytest.mark.parametrize("file", ["Test56.dl", "Test104.dl", "Teaset02.dl"])
+def test_oracle_matches_reference_dl_scenes(oracle_mod, file):
+    """The reference's own scene files beyond the stored fixtures: BVHs of
+    every surface and of the object level, closest and any hits, a frame."""
+    import os
+    from cgspline_gb300 import dl
+    root = os.environ.get("CGS_REFERENCE_ROOT", "/root/reference")
+    sc, cam = dl.load_dl(os.path.join(root, "assets", "scenes", file))
+    assert _compare_scene(oracle_mod, sc, cam, 160, 90, 64, 36) > 5000
+
+
+@needs_ref
 def test_oracle_matches_reference_full_c2_frame_rays(oracle_mod):
     """All 1920x1080 primary rays of the 16,384-patch torus."""
     sc = G.one_material(S.scene_c2())
