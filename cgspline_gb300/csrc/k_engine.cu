@@ -242,7 +242,10 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
             E.tnode[rid] = tnode; E.tkey[rid] = tkey; E.tpost[rid] = tpost; E.tleaf[rid] = tleaf;
             E.count[rid] = ncand;
             E.status[rid] = kPending;
-            if (ncand >= kHeavyList) E.heavy[atomicAdd(E.ctl + 4 * pass + 2, 1u)] = rid;
+            {
+                const uint32_t h = warp_push(E.ctl + 4 * pass + 2, ncand >= kHeavyList);
+                if (h != EMPTY) E.heavy[h] = rid;
+            }
             active = false;
             continue;
         }
@@ -416,7 +419,10 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         {
             E.count[rid] = ncand;
             E.status[rid] = kTraversed;
-            if (ncand >= kHeavyList) E.heavy[atomicAdd(E.ctl + 4 * pass + 2, 1u)] = rid;
+            {
+                const uint32_t h = warp_push(E.ctl + 4 * pass + 2, ncand >= kHeavyList);
+                if (h != EMPTY) E.heavy[h] = rid;
+            }
             active = false;
         }
     }
@@ -721,8 +727,8 @@ bool valid_engine_config(const EngineConfig& c)
     return c.passes >= 1 && c.passes <= kMaxPasses && (c.collectThreads == 128 || c.collectThreads == 256) &&
            (c.resolveThreads == 64 || c.resolveThreads == 128) && c.collectOccupancy >= 0 && c.collectOccupancy <= 32 &&
            c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
-           (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 8 &&
-           c.queueChunk <= int(kChunk) && c.queueChunk % 8 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32 &&
+           (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 4 &&
+           c.queueChunk <= int(kChunk) && c.queueChunk % 4 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32 &&
            (c.rayOrder == 0 || c.rayOrder == 1) && (c.originLast == 0 || c.originLast == 1);
 }
 

@@ -326,7 +326,7 @@ typedef struct cgs_engine_config {
      * The autotuner tries both. */
     int compressed_nodes;
     /* Candidate-list entries a ray may fill in the first collect pass before
-     * it parks (8..64, a multiple of 8; default 64); each later pass doubles
+     * it parks (4..64, a multiple of 4; default 64); each later pass doubles
      * it, up to 64.  A small first chunk parks a ray after its nearest few
      * candidates, so that the next pass walks the rest of the tree culled by
      * the hit the clip found among them. */

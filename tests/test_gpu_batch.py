@@ -212,7 +212,7 @@ def test_engine_settings_and_autotune(rt, store, torch):
             hit = ref["patch"] >= 0
             assert np.abs(got["t"][hit] - ref["t"][hit]).max(initial=0) <= 1e-6 * ref["t"][hit].max(initial=1)
         from cgspline_gb300._capi import CgsError
-        for bad in ({"passes": 9}, {"queue_chunk": 12}, {"queue_chunk": 72}, {"queue_chunk": 20}, {"queue_chunk": 0},
+        for bad in ({"passes": 9}, {"queue_chunk": 10}, {"queue_chunk": 72}, {"queue_chunk": 2}, {"queue_chunk": 0},
                     {"origin_last": 2},
                     {"packet_width": 0}, {"packet_width": 33}, {"ray_order": 2}):
             with pytest.raises(CgsError):
