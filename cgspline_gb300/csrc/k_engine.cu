@@ -66,19 +66,13 @@ struct Eng  // per-ray engine state, SoA over the query's capacity
     uint32_t *node, *key, *post, *leaf, *tnode, *tkey, *tpost, *tleaf, *jumped;
     int32_t *obj, *lpatch;
     float *leafEntry, *limit, *lt, *lu, *lv;
-    uint32_t* heavy;  // the current pass's rays with at least kHeavyList list entries
-    uint32_t* ctl;  // per pass: collect fetch, resolve fetch, heavy-list length
+    uint32_t* ctl;  // per pass: collect fetch, resolve fetch
     uint32_t chunk;        // list entries a ray may fill in the first pass; each later pass doubles it (<= kChunk)
     uint32_t packetWidth;  // idle lanes a warp gathers before the traversal refills it
     uint32_t originLast;   // any hit: search candidates whose leaf box holds the ray's origin last
 };
 
-constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 17;
-// A ray whose list holds at least this many entries after a collect pass is
-// also entered in the pass's heavy list, and the resolve pass takes the heavy
-// list first: the longest searches start at once instead of ending the launch
-// on a few lanes (longest-first order; each ray is still resolved once).
-constexpr uint32_t kHeavyList = 16;
+constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 16;
 
 Eng carve(uint32_t* base, uint32_t cap)
 {
@@ -93,7 +87,6 @@ Eng carve(uint32_t* base, uint32_t cap)
     e.leafEntry = reinterpret_cast<float*>(take(cap)); e.limit = reinterpret_cast<float*>(take(cap));
     e.lt = reinterpret_cast<float*>(take(cap)); e.lu = reinterpret_cast<float*>(take(cap));
     e.lv = reinterpret_cast<float*>(take(cap));
-    e.heavy = take(cap);
     e.ctl = take(4 * (kMaxPasses + 1));
     return e;
 }
@@ -242,10 +235,6 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
             E.tnode[rid] = tnode; E.tkey[rid] = tkey; E.tpost[rid] = tpost; E.tleaf[rid] = tleaf;
             E.count[rid] = ncand;
             E.status[rid] = kPending;
-            {
-                const uint32_t h = warp_push(E.ctl + 4 * pass + 2, ncand >= kHeavyList);
-                if (h != EMPTY) E.heavy[h] = rid;
-            }
             active = false;
             continue;
         }
@@ -419,10 +408,6 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         {
             E.count[rid] = ncand;
             E.status[rid] = kTraversed;
-            {
-                const uint32_t h = warp_push(E.ctl + 4 * pass + 2, ncand >= kHeavyList);
-                if (h != EMPTY) E.heavy[h] = rid;
-            }
             active = false;
         }
     }
@@ -451,25 +436,21 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
     float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
     float tmax = 0, lmax = 0, sinv = 1, lt = 0, lu = 0, lv = 0, limit = 0;
     const uint2* list = nullptr;
-    // the pass's heavy list, then every ray in order (skipping the heavy ones)
-    const uint32_t nh = E.ctl[4 * pass + 2];
     for (;;)
     {
         const bool need = !active && !exhausted;
         const uint32_t idx = warp_fetch(E.ctl + 4 * pass + 1, need);
         if (need)
         {
-            if (idx >= n + nh)
+            if (idx >= n)
                 exhausted = true;
             else
             {
-                const uint32_t r = idx < nh ? E.heavy[idx] : idx - nh;
-                const uint32_t st = E.status[r];
-                count = E.count[r];
-                // a heavy ray met in order is taken (or already done) from the list
-                if (count > 0 && st != kFinished && (idx < nh || count < kHeavyList))
+                const uint32_t st = E.status[idx];
+                count = E.count[idx];
+                if (count > 0 && st != kFinished)
                 {
-                    rid = r;
+                    rid = idx;
                     active = true;
                     k = 0;
                     obj = -1;
