@@ -66,13 +66,17 @@ struct Eng  // per-ray engine state, SoA over the query's capacity
     uint32_t *node, *key, *post, *leaf, *tnode, *tkey, *tpost, *tleaf, *jumped;
     int32_t *obj, *lpatch;
     float *leafEntry, *limit, *lt, *lu, *lv;
-    uint32_t* ctl;  // per pass: collect fetch, resolve fetch
+    // the rays to walk in pass p >= 1 (those that parked in pass p - 1) are
+    // queue[p & 1][0 .. ctl[4p + 2]); the rays still parked after the last
+    // pass P, for the inline fallback, are queue[P & 1][0 .. ctl[4P + 2])
+    uint32_t* queue[2];
+    uint32_t* ctl;  // per pass: collect fetch, resolve fetch, length of the pass's queue
     uint32_t chunk;        // list entries a ray may fill in the first pass; each later pass doubles it (<= kChunk)
     uint32_t packetWidth;  // idle lanes a warp gathers before the traversal refills it
     uint32_t originLast;   // any hit: search candidates whose leaf box holds the ray's origin last
 };
 
-constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 16;
+constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 18;
 
 Eng carve(uint32_t* base, uint32_t cap)
 {
@@ -87,6 +91,7 @@ Eng carve(uint32_t* base, uint32_t cap)
     e.leafEntry = reinterpret_cast<float*>(take(cap)); e.limit = reinterpret_cast<float*>(take(cap));
     e.lt = reinterpret_cast<float*>(take(cap)); e.lu = reinterpret_cast<float*>(take(cap));
     e.lv = reinterpret_cast<float*>(take(cap));
+    e.queue[0] = take(cap); e.queue[1] = take(cap);
     e.ctl = take(4 * (kMaxPasses + 1));
     return e;
 }
@@ -167,6 +172,9 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
     BvhRef B {};  // the BVH walked now; its hash parameters are read at a table lookup
     uint32_t nrays = 0;
     uint2* list = nullptr;
+    // pass 0 walks every ray; a later pass only the queue of rays that parked
+    const uint32_t m = pass == 0 ? n : E.ctl[4 * pass + 2];
+    const uint32_t* queue = E.queue[pass & 1];
     for (;;)
     {
         const bool need = !active && !exhausted;
@@ -174,18 +182,19 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
         const uint32_t idx = warp_fetch(E.ctl + 4 * pass, need, E.packetWidth, active);
         if (need && idx != EMPTY)
         {
-            if (idx >= n)
+            const uint32_t r = idx < m ? (pass == 0 ? idx : queue[idx]) : 0u;
+            if (idx >= m)
                 exhausted = true;
-            else if (pass == 0 && rays.group && __ldg(rays.group + idx) >= S.ngroups)
+            else if (pass == 0 && rays.group && __ldg(rays.group + r) >= S.ngroups)
             {
                 // a group outside the store: the ray stays a miss and raises an error bit
                 lc.errors |= kErrGroup;
-                E.count[idx] = 0;
-                E.status[idx] = kTraversed;
+                E.count[r] = 0;
+                E.status[r] = kTraversed;
             }
-            else if (pass == 0 || E.status[idx] == kPending)
+            else if (pass == 0 || E.status[r] == kPending)
             {
-                rid = idx;
+                rid = r;
                 const uint32_t g = rays.group ? __ldg(rays.group + rid) : 0u;
                 active = true;
                 float3 d;
@@ -235,6 +244,7 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
             E.tnode[rid] = tnode; E.tkey[rid] = tkey; E.tpost[rid] = tpost; E.tleaf[rid] = tleaf;
             E.count[rid] = ncand;
             E.status[rid] = kPending;
+            E.queue[(pass + 1) & 1][warp_push(E.ctl + 4 * (pass + 1) + 2, true)] = rid;
             active = false;
             continue;
         }
@@ -436,21 +446,25 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
     float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
     float tmax = 0, lmax = 0, sinv = 1, lt = 0, lu = 0, lv = 0, limit = 0;
     const uint2* list = nullptr;
+    // pass 0 resolves every ray; a later pass the rays its traversal walked
+    const uint32_t m = pass == 0 ? n : E.ctl[4 * pass + 2];
+    const uint32_t* queue = E.queue[pass & 1];
     for (;;)
     {
         const bool need = !active && !exhausted;
         const uint32_t idx = warp_fetch(E.ctl + 4 * pass + 1, need);
         if (need)
         {
-            if (idx >= n)
+            if (idx >= m)
                 exhausted = true;
             else
             {
-                const uint32_t st = E.status[idx];
-                count = E.count[idx];
+                const uint32_t r = pass == 0 ? idx : queue[idx];
+                const uint32_t st = E.status[r];
+                count = E.count[r];
                 if (count > 0 && st != kFinished)
                 {
-                    rid = idx;
+                    rid = r;
                     active = true;
                     k = 0;
                     obj = -1;
@@ -565,14 +579,17 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
 
 // Rays unfinished after the last pass: the inline search from the start.
 template<bool kAny>
-__global__ void __launch_bounds__(128) k_rest(DevScene S, RaysSoA rays, uint32_t n0, const uint32_t* nDev, Eng E,
-                                              Query q, HitsSoA hits, int32_t* occluded, Counters* cnt)
+__global__ void __launch_bounds__(128) k_rest(DevScene S, RaysSoA rays, Eng E, int passes, Query q, HitsSoA hits,
+                                              int32_t* occluded, Counters* cnt)
 {
-    const uint32_t n = nDev ? *nDev : n0;
+    // the rays still parked after the last pass
+    const uint32_t m = E.ctl[4 * passes + 2];
+    const uint32_t* queue = E.queue[passes & 1];
     LocalCounters lc;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
-    for (uint32_t rid = tid; rid < n; rid += nt)
+    for (uint32_t i = tid; i < m; i += nt)
     {
+        const uint32_t rid = queue[i];
         if (E.status[rid] != kPending) continue;
         float3 o, d; float tmax;
         load_ray(rays, rid, o, d, tmax);
@@ -679,7 +696,7 @@ void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Q
         k_resolve<kAny, kG64><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
         nl += 2;
     }
-    k_rest<kAny><<<sms() * 4, 128, 0, stream>>>(S, rays, n, nDev, E, q, hits, occluded, cnt);
+    k_rest<kAny><<<sms() * 4, 128, 0, stream>>>(S, rays, E, c.passes, q, hits, occluded, cnt);
     nl++;
 }
 
