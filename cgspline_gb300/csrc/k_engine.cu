@@ -68,7 +68,8 @@ struct Eng  // per-ray engine state, SoA over the query's capacity
     float *leafEntry, *limit, *lt, *lu, *lv;
     // the rays to walk in pass p >= 1 (those that parked in pass p - 1) are
     // queue[p & 1][0 .. ctl[4p + 2]); the rays still parked after the last
-    // pass P, for the inline fallback, are queue[P & 1][0 .. ctl[4P + 2])
+    // pass P, for the inline fallback, are queue[P & 1][0 .. ctl[4P + 2]).
+    // k_pending builds each in ray order, 256 rays at a time.
     uint32_t* queue[2];
     uint32_t* ctl;  // per pass: collect fetch, resolve fetch, length of the pass's queue
     uint32_t chunk;        // list entries a ray may fill in the first pass; each later pass doubles it (<= kChunk)
@@ -244,7 +245,6 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
             E.tnode[rid] = tnode; E.tkey[rid] = tkey; E.tpost[rid] = tpost; E.tleaf[rid] = tleaf;
             E.count[rid] = ncand;
             E.status[rid] = kPending;
-            E.queue[(pass + 1) & 1][warp_push(E.ctl + 4 * (pass + 1) + 2, true)] = rid;
             active = false;
             continue;
         }
@@ -610,6 +610,41 @@ __global__ void __launch_bounds__(128) k_rest(DevScene S, RaysSoA rays, Eng E, i
     flush_counters(cnt, lc, 0);
 }
 
+// The queue of parked rays for the next pass, in ray order within each tile
+// of 256 rays (the tiles' slices land in the order their blocks claim them),
+// so that a packet of consecutive queue positions holds neighbouring rays.
+constexpr int kPendingThreads = 256;
+__global__ void __launch_bounds__(kPendingThreads) k_pending(const uint32_t* __restrict__ status, uint32_t n0,
+                                                             const uint32_t* nDev, uint32_t* queue, uint32_t* len)
+{
+    const uint32_t n = nDev ? *nDev : n0;
+    __shared__ uint32_t offset[kPendingThreads / 32];
+    __shared__ uint32_t base;
+    const uint32_t w = threadIdx.x / 32, lane = threadIdx.x % 32;
+    for (uint32_t t0 = blockIdx.x * kPendingThreads; t0 < n; t0 += gridDim.x * kPendingThreads)
+    {
+        const uint32_t i = t0 + threadIdx.x;
+        const bool p = i < n && status[i] == kPending;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, p);
+        if (lane == 0) offset[w] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            uint32_t sum = 0;
+            for (uint32_t k = 0; k < kPendingThreads / 32; k++)
+            {
+                const uint32_t c = offset[k];
+                offset[k] = sum;
+                sum += c;
+            }
+            base = sum ? atomicAdd(len, sum) : 0u;
+        }
+        __syncthreads();
+        if (p) queue[base + offset[w] + __popc(m & ((1u << lane) - 1u))] = i;
+        __syncthreads();
+    }
+}
+
 __global__ void k_init(RaysSoA rays, uint32_t n0, const uint32_t* nDev, HitsSoA hits, int32_t* occluded, Eng E)
 {
     const uint32_t n = nDev ? *nDev : n0;
@@ -690,14 +725,21 @@ void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Q
     const uint32_t warps = (n + 31) / 32;
     const int gc = int(std::min<uint32_t>(uint32_t(cb), warps / (ct / 32) + 1));
     const int gr = int(std::min<uint32_t>(uint32_t(rb), warps / (rt / 32) + 1));
+    const int gp = int(std::min<uint32_t>(uint32_t(sms() * 8), (n + kPendingThreads - 1) / kPendingThreads));
     for (int p = 0; p < c.passes; p++)
     {
+        if (p > 0)
+        {
+            k_pending<<<gp, kPendingThreads, 0, stream>>>(E.status, n, nDev, E.queue[p & 1], E.ctl + 4 * p + 2);
+            nl++;
+        }
         launch_collect<kAny>(gc, ct, stream, S, rays, n, nDev, E, p, c, cnt);
         k_resolve<kAny, kG64><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
         nl += 2;
     }
+    k_pending<<<gp, kPendingThreads, 0, stream>>>(E.status, n, nDev, E.queue[c.passes & 1], E.ctl + 4 * c.passes + 2);
     k_rest<kAny><<<sms() * 4, 128, 0, stream>>>(S, rays, E, c.passes, q, hits, occluded, cnt);
-    nl++;
+    nl += 2;
 }
 
 }  // namespace
