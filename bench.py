@@ -258,6 +258,21 @@ def run_reference(args, rank, world):
 
 
 # ----------------------------------------------------------- GPU legs --
+def tile_order(w, h):
+    """Pixel index of each queue position when a w x h image's primary rays
+    are queued in 8 x 4 tiles (bands of 4 rows cut into 8-column chunks, the
+    order of the render's tiled ray queue)."""
+    import numpy as np
+    p = np.arange(w * h, dtype=np.int64)
+    band = p // (4 * w)
+    m = p - band * 4 * w
+    hb = np.minimum(4, h - 4 * band)
+    c = m // (8 * hb)
+    q = m - c * 8 * hb
+    cw = np.minimum(8, w - 8 * c)
+    return (4 * band + q // cw) * w + 8 * c + q % cw
+
+
 def timed(torch, stream, flush, fn, reps):
     """Device ms of each of `reps` calls of fn(), L2 flushed before each."""
     e0 = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
@@ -730,6 +745,9 @@ def main():
         # frame's first traversal pass.  Algorithmic bytes per ray: 28 in,
         # 64 per inner-node visit, 8 per backtrack (table + displacement).
         prim = rt.camera_rays(cam, W, H, device=local)
+        if rt.engine_config()["ray_order"] == 1:
+            # the frame queues its primary rays in 8 x 4 pixel tiles: the same order here
+            prim = prim[:, torch.from_numpy(tile_order(W, H)).to(prim.device)].contiguous()
         for _ in range(3):
             g.traverse(prim, stream=stream, copy_lengths=False)
         torch.cuda.synchronize()

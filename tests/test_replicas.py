@@ -66,3 +66,17 @@ def test_reference_arm_runs_on_rank_zero_only(capsys):
         steps, warmup = 1, 0
     assert bench.run_reference(Args(), 1, 2) is None
     assert capsys.readouterr().out == ""
+
+
+def test_bench_tile_order_is_a_permutation():
+    """The roofline launch queues the frame's primary rays in the render's
+    8 x 4 tile order: a permutation of the pixels, tile by tile."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    for w, h in ((1920, 1080), (33, 17), (8, 4), (5, 3)):
+        t = bench.tile_order(w, h)
+        assert np.array_equal(np.sort(t), np.arange(w * h))
+    t = bench.tile_order(16, 8)
+    assert list(t[:8]) == list(range(8)) and list(t[8:16]) == list(range(16, 24))
+    assert list(t[32:40]) == list(range(8, 16))
