@@ -531,8 +531,8 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
     per rate through the continuous-batching server (reference and
     longest-axis BVH builds) and through the plain server (one request per
     launch, one at a time, reference build); p50 / p99 latency from submit to
-    completion, and rays/s over the stream.  The engine settings are the
-    autotuner's pick on the stream's renders of 512x512 and below."""
+    completion, and rays/s over the stream.  The engine settings are the ones
+    in force (bench.py's batching leg leaves its autotuned pick)."""
     import numpy as np
     t0 = time.perf_counter()
     scs = [scenes.scene_c5(i) for i in range(32)]
@@ -586,14 +586,6 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
                 "Mrays_s": rays / span / 1e6, "rays": int(rays), "span_s": span}
 
     opts = rt.Options(recursion_depth=3, precision=prec)
-    # the autotuner picks the engine settings on the stream's smaller renders
-    # (512x512 and below, with their spp and depths), outside the timed region
-    small = [r for r in reqs if not isinstance(r, tuple) and r.width * r.height <= 512 * 512]
-    if small:
-        t0 = time.perf_counter()
-        cfg, tms = rt.autotune(stores["reference"], small, opts, repeats=2)
-        out["autotune"] = {"settings": cfg, "ms": tms, "requests": len(small),
-                           "seconds": time.perf_counter() - t0}
     servers = {"served": rt.Server(stores["reference"], slots=slots, memory_budget=budget_gb << 30, options=opts),
                "served_split_longest": rt.Server(stores["longest"], slots=slots, memory_budget=budget_gb << 30,
                                                  options=opts),
