@@ -470,7 +470,7 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
                 for i, (c, side) in enumerate(cams)]
         # the autotuner picks the engine settings on this batch (outside the timed region)
         t0 = time.perf_counter()
-        cfg, tms = rt.autotune(store, reqs, rt.Options(recursion_depth=DEPTH, precision=prec), repeats=2)
+        cfg, tms = rt.autotune(store, reqs, rt.Options(recursion_depth=DEPTH, precision=prec), repeats=3)
         out[f"autotune_{split_name}"] = {"settings": cfg, "ms": tms, "seconds": time.perf_counter() - t0}
         legs = (("batched", rt.WAVEFRONT, prec), ("plain", rt.PLAIN, prec)) if split == rt.SPLIT_REFERENCE else \
             (("batched_split_longest", rt.WAVEFRONT, prec),

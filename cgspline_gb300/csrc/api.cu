@@ -684,6 +684,18 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
                 const double ms = score(p);
                 if (ms < curMs) { curMs = ms; cur = p; }
             }
+    // the pass count and the first chunk act together (a small chunk needs the
+    // passes to resume its rays), so a last stage tries them as pairs
+    for (int passes : {2, 4, 8})
+        for (int chunk : {8, 16, 32, 64})
+        {
+            if (status != CGS_OK) break;
+            Point p = cur;
+            p.passes = passes;
+            p.chunk = chunk;
+            const double ms = score(p);
+            if (ms < curMs) { curMs = ms; cur = p; }
+        }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     const EngineConfig winner = config(cur);

@@ -360,7 +360,7 @@ int cgs_engine_config_set(const cgs_engine_config* config);
  * as many as fit or 768 threads' worth; exact or compressed nodes; queue
  * chunk 8, 16, 32, 64; packet width 1, 8, 16; scanline or tiled ray order;
  * any-hit candidates in traversal order or origin boxes last),
- * each knob set to its fastest
+ * then passes 2, 4, 8 x first chunk 8, 16, 32, 64 as pairs, each knob set to its fastest
  * value with the others held; a setting already timed is not timed again.
  * Synchronises `stream`. */
 int cgs_autotune_render(cgs_scene* scene, const cgs_render_request* requests, uint32_t n,
