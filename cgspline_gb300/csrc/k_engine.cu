@@ -657,18 +657,45 @@ __global__ void k_init(RaysSoA rays, uint32_t n0, const uint32_t* nDev, HitsSoA 
     }
 }
 
-__global__ void __launch_bounds__(128) k_polish(DevScene S, RaysSoA rays, uint32_t n0, const uint32_t* nDev,
-                                                HitsSoA hits)
+// One polish per hit.  A warp gathers the hits of the rays it sweeps into a
+// shared-memory list and polishes them 32 at a time, so that its FP64
+// instructions run with full lanes where misses are scattered among hits
+// (the FP64 pipe takes a warp instruction whatever its active lanes).
+constexpr int kPolishThreads = 128;
+__device__ __forceinline__ void polish_ray(const DevScene& S, const RaysSoA& rays, HitsSoA& hits, uint32_t i)
+{
+    HitRecord h {hits.t[i], hits.u[i], hits.v[i], hits.patch[i], hits.object[i]};
+    polish_hit(S, f3(rays.ox[i], rays.oy[i], rays.oz[i]), f3(rays.dx[i], rays.dy[i], rays.dz[i]), h);
+    hits.t[i] = h.t; hits.u[i] = h.u; hits.v[i] = h.v;
+}
+__global__ void __launch_bounds__(kPolishThreads) k_polish(DevScene S, RaysSoA rays, uint32_t n0,
+                                                           const uint32_t* nDev, HitsSoA hits)
 {
     const uint32_t n = nDev ? *nDev : n0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    __shared__ uint32_t pend[kPolishThreads / 32][64];
+    uint32_t* my = pend[threadIdx.x / 32];
+    const uint32_t lane = threadIdx.x % 32;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, nwarps = gridDim.x * blockDim.x / 32;
+    uint32_t cnt = 0;  // warp-uniform
+    for (uint32_t base = warp * 32; base < n; base += nwarps * 32)
     {
-        const int32_t ob = hits.object[i];
-        if (ob < 0) continue;
-        HitRecord h {hits.t[i], hits.u[i], hits.v[i], hits.patch[i], ob};
-        polish_hit(S, f3(rays.ox[i], rays.oy[i], rays.oz[i]), f3(rays.dx[i], rays.dy[i], rays.dz[i]), h);
-        hits.t[i] = h.t; hits.u[i] = h.u; hits.v[i] = h.v;
+        const uint32_t i = base + lane;
+        const bool hit = i < n && hits.object[i] >= 0;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
+        if (hit) my[cnt + __popc(m & ((1u << lane) - 1u))] = i;
+        cnt += __popc(m);
+        __syncwarp();
+        if (cnt >= 32)
+        {
+            polish_ray(S, rays, hits, my[lane]);
+            cnt -= 32;
+            const uint32_t rest = lane < cnt ? my[32 + lane] : 0u;
+            __syncwarp();
+            if (lane < cnt) my[lane] = rest;
+            __syncwarp();
+        }
     }
+    if (lane < cnt) polish_ray(S, rays, hits, my[lane]);
 }
 
 int sms()
@@ -816,7 +843,7 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     else launch<false, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     if (!any && polishes(q.precision))
     {
-        k_polish<<<flat * 2, 128, 0, stream>>>(S, rays, n, nDev, hits);
+        k_polish<<<flat * 2, kPolishThreads, 0, stream>>>(S, rays, n, nDev, hits);
         nl++;
     }
     if (launches) *launches += nl;
