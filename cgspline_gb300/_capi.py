@@ -62,8 +62,7 @@ class Hits(C.Structure):
 class EngineConfig(C.Structure):
     _fields_ = [(k, C.c_int) for k in ("passes", "collect_threads", "resolve_threads", "collect_occupancy",
                                        "resolve_occupancy", "backtrack_cache", "compressed_nodes",
-                                       "queue_chunk", "packet_width", "ray_order", "origin_last",
-                                       "any_chunk")]
+                                       "queue_chunk", "packet_width", "ray_order", "origin_last")]
 
 
 class ServerOptions(C.Structure):

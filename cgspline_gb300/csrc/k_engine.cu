@@ -796,8 +796,7 @@ bool valid_engine_config(const EngineConfig& c)
            c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
            (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 4 &&
            c.queueChunk <= int(kChunk) && c.queueChunk % 4 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32 &&
-           (c.rayOrder == 0 || c.rayOrder == 1) && (c.originLast == 0 || c.originLast == 1) &&
-           (c.anyChunk == 0 || (c.anyChunk >= 4 && c.anyChunk <= int(kChunk) && c.anyChunk % 4 == 0));
+           (c.rayOrder == 0 || c.rayOrder == 1) && (c.originLast == 0 || c.originLast == 1);
 }
 
 bool set_engine_config(const EngineConfig& c)
@@ -831,7 +830,7 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     Eng E = carve(scratch, capacity);
     {
         const EngineConfig ec = engine_config();
-        E.chunk = uint32_t(any && ec.anyChunk ? ec.anyChunk : ec.queueChunk);
+        E.chunk = uint32_t(ec.queueChunk);
         E.packetWidth = uint32_t(ec.packetWidth);
         E.originLast = uint32_t(ec.originLast);
     }

@@ -87,7 +87,6 @@ struct EngineConfig
     int packetWidth = 1;     // the traversal refills a warp once this many lanes are idle (1..32)
     int rayOrder = 0;        // primary rays of a render: 0 in scanline order, 1 in 8 x 4 pixel tiles
     int originLast = 0;      // any hit: 1 searches the candidates whose leaf box holds the origin last
-    int anyChunk = 0;        // any hit: the first pass's chunk (0: queueChunk; else 4..64, multiple of 4)
 };
 EngineConfig engine_config();
 bool set_engine_config(const EngineConfig& c);

@@ -348,10 +348,6 @@ typedef struct cgs_engine_config {
      * it; an occluder found first ends the ray without it.  The order does
      * not change an any-hit answer. */
     int origin_last;
-    /* Any-hit queries: the first pass's candidate-list chunk (0, the default:
-     * queue_chunk; else 4..64, a multiple of 4).  An occluded shadow ray ends
-     * at its first root, so a small chunk ends it after a short walk. */
-    int any_chunk;
 } cgs_engine_config;
 int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
@@ -363,8 +359,7 @@ int cgs_engine_config_set(const cgs_engine_config* config);
  * 4, 8; collect 128, 256 and resolve 64, 128 threads; traversal blocks per SM
  * as many as fit or 768 threads' worth; exact or compressed nodes; queue
  * chunk 8, 16, 32, 64; packet width 1, 8, 16; scanline or tiled ray order;
- * any-hit candidates in traversal order or origin boxes last; any-hit first
- * chunk as queue_chunk, 4, 8 or 16),
+ * any-hit candidates in traversal order or origin boxes last),
  * then passes 2, 4, 8 x first chunk 8, 16, 32, 64 as pairs, each knob set to its fastest
  * value with the others held; a setting already timed is not timed again.
  * Synchronises `stream`. */

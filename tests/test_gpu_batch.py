@@ -213,7 +213,7 @@ def test_engine_settings_and_autotune(rt, store, torch):
             assert np.abs(got["t"][hit] - ref["t"][hit]).max(initial=0) <= 1e-6 * ref["t"][hit].max(initial=1)
         from cgspline_gb300._capi import CgsError
         for bad in ({"passes": 9}, {"queue_chunk": 10}, {"queue_chunk": 72}, {"queue_chunk": 2}, {"queue_chunk": 0},
-                    {"origin_last": 2}, {"any_chunk": 2}, {"any_chunk": 70}, {"any_chunk": 6},
+                    {"origin_last": 2},
                     {"packet_width": 0}, {"packet_width": 33}, {"ray_order": 2}):
             with pytest.raises(CgsError):
                 rt.set_engine_config(**bad)
@@ -222,7 +222,6 @@ def test_engine_settings_and_autotune(rt, store, torch):
         assert cfg == rt.engine_config() and ms > 0
         assert cfg["passes"] in (1, 2, 4, 8) and cfg["collect_threads"] in (128, 256)
         assert cfg["queue_chunk"] in (8, 16, 32, 64) and cfg["packet_width"] in (1, 8, 16)
-        assert cfg["any_chunk"] in (0, 4, 8, 16)
     finally:
         rt.set_engine_config(**base)
 
