@@ -84,8 +84,8 @@ struct EngineConfig
     int compressedNodes = 0; // 1: the traversal reads the 32-byte compressed node mirror
     int queueChunk = 64;     // candidate-list entries a ray may fill in the first pass (4..64, multiple of 4);
                              // each later pass doubles it, up to 64
-    int packetWidth = 1;     // the traversal refills a warp once this many lanes are idle (1..32)
-    int rayOrder = 0;        // primary rays of a render: 0 in scanline order, 1 in 8 x 4 pixel tiles
+    int packetWidth = 8;     // the traversal refills a warp once this many lanes are idle (1..32)
+    int rayOrder = 1;        // primary rays of a render: 0 in scanline order, 1 in 8 x 4 pixel tiles
     int originLast = 0;      // any hit: 1 searches the candidates whose leaf box holds the origin last
 };
 EngineConfig engine_config();

@@ -331,13 +331,13 @@ typedef struct cgs_engine_config {
      * candidates, so that the next pass walks the rest of the tree culled by
      * the hit the clip found among them. */
     int queue_chunk;
-    /* Packet refill (1..32; default 1): the traversal kernel gives a warp's
+    /* Packet refill (1..32; default 8): the traversal kernel gives a warp's
      * idle lanes new rays only once at least this many are idle, or none of
      * its lanes is busy, so that rays enter a warp in packets of adjacent
      * pixels; 1 refills every idle lane at once. */
     int packet_width;
-    /* Order of a render's primary rays in the ray queue (0 default: scanline;
-     * 1: 8 x 4 pixel tiles, so that a warp's rays are neighbours in both
+    /* Order of a render's primary rays in the ray queue (0: scanline; 1, the
+     * default: 8 x 4 pixel tiles, so that a warp's rays are neighbours in both
      * directions).  Every ray keeps its sample index, so frames are the
      * same under both. */
     int ray_order;

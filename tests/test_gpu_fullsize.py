@@ -51,9 +51,10 @@ def test_engine_settings_agree_at_full_size(setup):
     base = rt.engine_config()
     got = {}
     try:
-        for cfg in ({"passes": 2, "backtrack_cache": 1}, {"passes": 1, "backtrack_cache": 0},
+        for cfg in ({"passes": 2, "backtrack_cache": 1, "packet_width": 1},
+                    {"passes": 1, "backtrack_cache": 0},
                     {"passes": 8, "collect_threads": 128, "resolve_threads": 128, "backtrack_cache": 1},
-                    {"passes": 2, "backtrack_cache": 0},
+                    {"passes": 2, "backtrack_cache": 0, "packet_width": 1},
                     {"passes": 2, "backtrack_cache": 1, "packet_width": 8},
                     {"passes": 2, "backtrack_cache": 1, "queue_chunk": 16, "packet_width": 8},
                     {"passes": 1, "backtrack_cache": 1, "queue_chunk": 40, "packet_width": 32},
@@ -70,7 +71,8 @@ def test_engine_settings_agree_at_full_size(setup):
     runs = list(got.values())
     for h, _ in runs[1:]:
         same_hits(runs[0][0], h)
-    (h1, c1), (h0, c0) = got[(("backtrack_cache", 1), ("passes", 2))], got[(("backtrack_cache", 0), ("passes", 2))]
+    (h1, c1) = got[(("backtrack_cache", 1), ("packet_width", 1), ("passes", 2))]
+    (h0, c0) = got[(("backtrack_cache", 0), ("packet_width", 1), ("passes", 2))]
     for k in h1:
         assert np.array_equal(h1[k], h0[k]), k
     # the packet refill changes when a warp takes its rays, not which rays
