@@ -62,7 +62,8 @@ class Hits(C.Structure):
 class EngineConfig(C.Structure):
     _fields_ = [(k, C.c_int) for k in ("passes", "collect_threads", "resolve_threads", "collect_occupancy",
                                        "resolve_occupancy", "backtrack_cache", "compressed_nodes",
-                                       "queue_chunk", "packet_width", "ray_order", "origin_last")]
+                                       "queue_chunk", "packet_width", "ray_order", "origin_last",
+                                       "subdiv_levels")]
 
 
 class ServerOptions(C.Structure):

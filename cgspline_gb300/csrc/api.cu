@@ -578,7 +578,7 @@ static cgs_engine_config to_c(const EngineConfig& c)
 {
     return cgs_engine_config {c.passes,         c.collectThreads,  c.resolveThreads, c.collectOccupancy,
                               c.resolveOccupancy, c.backtrackCache, c.compressedNodes, c.queueChunk,
-                              c.packetWidth,      c.rayOrder,       c.originLast};
+                              c.packetWidth,      c.rayOrder,       c.originLast,      c.subdivLevels};
 }
 
 int cgs_engine_config_get(cgs_engine_config* out)
@@ -595,7 +595,7 @@ int cgs_engine_config_set(const cgs_engine_config* in)
     const EngineConfig c {in->passes,          in->collect_threads, in->resolve_threads,
                           in->collect_occupancy, in->resolve_occupancy, in->backtrack_cache,
                           in->compressed_nodes,  in->queue_chunk,     in->packet_width,
-                          in->ray_order,         in->origin_last};
+                          in->ray_order,         in->origin_last,     in->subdiv_levels};
     return set_engine_config(c) ? CGS_OK : CGS_ERR_INVALID_ARGUMENT;
 }
 
@@ -626,18 +626,18 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
     // the knobs; `capped` stands for the traversal's blocks per SM: as many as
     // fit (0), or three quarters of that (768 threads per SM), which leaves
     // room for the overlapping queries
-    struct Point { int passes, ct, rt, capped, cq, chunk, width, order, olast; };
+    struct Point { int passes, ct, rt, capped, cq, chunk, width, order, olast, levels; };
     auto config = [&](const Point& p) {
         EngineConfig c = saved;
         c.passes = p.passes; c.collectThreads = p.ct; c.resolveThreads = p.rt;
         c.collectOccupancy = p.capped ? 768 / p.ct : 0; c.resolveOccupancy = 0;
         c.compressedNodes = p.cq; c.queueChunk = p.chunk; c.packetWidth = p.width; c.rayOrder = p.order;
-        c.originLast = p.olast;
+        c.originLast = p.olast; c.subdivLevels = p.levels;
         return c;
     };
     auto key = [](const Point& p) {
-        return (((((((int64_t(p.passes) * 512 + p.ct) * 256 + p.rt) * 2 + p.capped) * 2 + p.cq) * 128 + p.chunk) * 64 +
-                 p.width) * 2 + p.order) * 2 + p.olast;
+        return ((((((((int64_t(p.passes) * 512 + p.ct) * 256 + p.rt) * 2 + p.capped) * 2 + p.cq) * 128 + p.chunk) * 64 +
+                  p.width) * 2 + p.order) * 2 + p.olast) * 128 + p.levels;
     };
     std::map<int64_t, double> scores;
     auto score = [&](const Point& p) -> double {
@@ -668,12 +668,15 @@ int cgs_autotune_render(cgs_scene* s, const cgs_render_request* reqs, uint32_t n
 
     // start from the current setting, rounded onto the search grid
     Point cur {saved.passes, saved.collectThreads, saved.resolveThreads, saved.collectOccupancy != 0 ? 1 : 0,
-               saved.compressedNodes, saved.queueChunk, saved.packetWidth, saved.rayOrder, saved.originLast};
+               saved.compressedNodes, saved.queueChunk, saved.packetWidth, saved.rayOrder, saved.originLast,
+               saved.subdivLevels};
     double curMs = score(cur);
-    const std::vector<std::pair<int Point::*, std::vector<int>>> knobs {
+    std::vector<std::pair<int Point::*, std::vector<int>>> knobs {
         {&Point::passes, {1, 2, 4, 8}}, {&Point::ct, {128, 256}},   {&Point::rt, {64, 128}},
         {&Point::capped, {0, 1}},       {&Point::cq, {0, 1}},       {&Point::chunk, {8, 16, 32, 64}},
         {&Point::width, {1, 8, 16}},    {&Point::order, {0, 1}},    {&Point::olast, {0, 1}}};
+    // the subdivision levels per round matter only to a subdivision batch
+    if (opt->method == CGS_METHOD_SUBDIV) knobs.push_back({&Point::levels, {1, 4, 16, 64}});
     for (int round = 0; round < 2 && status == CGS_OK; round++)
         for (const auto& [field, values] : knobs)
             for (int v : values)

@@ -602,6 +602,10 @@ struct ClipState
     bool found, b64;  // b64: FP64 projection and fat-line bounds (near-grazing)
     bool fresh;       // the net is still to be projected (the search's first step)
     bool tposed;      // buf holds the transposed net (left so by a cut along v)
+    // the resumable subdivision search (subdiv_step) keeps its walk in the same
+    // state: the bit trail in cutsideStack, the level in sl, the sub-domain's
+    // integer coordinates in tu / tv, and `fresh` as its reload flag
+    uint32_t tu, tv;
     // b64: the ray the net is projected from (origin, direction), kept in
     // local memory: read only where a projection starts, it would otherwise
     // hold twelve registers through the whole search
@@ -763,6 +767,73 @@ static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, float g
 // backtrack, accept a leaf whose bounding box strictly contains the origin
 // once both diagonals are below tol (or after 31 halvings).  The sub-domain
 // follows the buffer: after k halvings su = 2^-ceil(k/2), sv = 2^-floor(k/2).
+// subdiv_patch as a resumable search for the query engine: subdiv_begin
+// projects the net; each subdiv_step runs up to `levels` iterations of the
+// same loop and returns false when the search is over (c.found: a root was
+// kept), so lanes of a warp interleave their searches and refill from the
+// queue one search at a time.  The iterations are subdiv_patch's, in the same
+// order, so the results are the same bit for bit.
+__device__ __forceinline__ void subdiv_begin(ClipState& c, const HitSink& sink, float tol)
+{
+    project_net(c.buf, sink.P, sink.o, sink.d);
+    c.cutsideStack = 0; c.tu = 0; c.tv = 0; c.sl = 0; c.it = 0;
+    c.fresh = false; c.found = false; c.tol = tol;
+}
+static __device__ __noinline__ bool subdiv_step(ClipState& c, HitSink& sink, LocalCounters& lc, int levels)
+{
+    uint32_t trail = uint32_t(c.cutsideStack), tu = c.tu, tv = c.tv;
+    int k = c.sl;
+    bool more = true;
+    for (int s = 0; s < levels; s++)
+    {
+        if (c.it >= 4 * kMaxClipIterations) { lc.errors |= kErrClipIterations; more = false; break; }
+        c.it++;
+        lc.iterations++;
+        const float su = ldexpf(1.0f, -((k + 1) >> 1)), sv = ldexpf(1.0f, -(k >> 1));
+        const float2 emin = make_float2(float(tu) * su, float(tv) * sv);
+        const float2 emax = make_float2(emin.x + su, emin.y + sv);
+        if (c.fresh)
+        {
+            project_net(c.buf, sink.P, sink.o, sink.d);
+            subpatchU(c.buf, emin.x, emax.x);
+            subpatchV(c.buf, emin.y, emax.y);
+        }
+        float2 bmin = c.buf[0], bmax = c.buf[0];
+#pragma unroll
+        for (int i = 1; i < 16; i++)
+        {
+            bmin = make_float2(fminf(bmin.x, c.buf[i].x), fminf(bmin.y, c.buf[i].y));
+            bmax = make_float2(fmaxf(bmax.x, c.buf[i].x), fmaxf(bmax.y, c.buf[i].y));
+        }
+        if (bmin.x < 0.0f && bmin.y < 0.0f && bmax.x > 0.0f && bmax.y > 0.0f)
+        {
+            if ((len2(c.buf[3] - c.buf[12]) < c.tol && len2(c.buf[15] - c.buf[0]) < c.tol) || k >= 31)
+                c.found |= approximateIntersection(sink, c.buf, emin, emax);
+            else
+            {
+                c.fresh = false;
+                if ((k & 1) == 0) { subpatchU(c.buf, 0.0f, 0.5f); tu <<= 1; }
+                else { subpatchV(c.buf, 0.0f, 0.5f); tv <<= 1; }
+                trail <<= 1;
+                ++k;
+                continue;
+            }
+        }
+        const int ones = __clz(__brev(~trail));
+        if (ones >= k) { more = false; break; }
+        const int hi = k - 1, lo = k - ones;
+        const int evens = (hi / 2) - ((lo + 1) / 2) + 1;
+        tu >>= evens;
+        tv >>= (ones - evens);
+        k -= ones;
+        trail = (trail >> ones) | 1u;
+        if (((k - 1) & 1) == 0) tu |= 1u; else tv |= 1u;
+        c.fresh = true;
+    }
+    c.cutsideStack = int(trail); c.tu = tu; c.tv = tv; c.sl = k;
+    return more;
+}
+
 static __device__ __noinline__ bool subdiv_patch(HitSink& sink, float tol, LocalCounters& lc)
 {
     float2 buf[16];

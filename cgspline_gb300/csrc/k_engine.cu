@@ -75,6 +75,7 @@ struct Eng  // per-ray engine state, SoA over the query's capacity
     uint32_t chunk;        // list entries a ray may fill in the first pass; each later pass doubles it (<= kChunk)
     uint32_t packetWidth;  // idle lanes a warp gathers before the traversal refills it
     uint32_t originLast;   // any hit: search candidates whose leaf box holds the ray's origin last
+    uint32_t subdivLevels; // subdivision searches: bisection levels a lane runs per resolve round
 };
 
 constexpr size_t kWordsPerRay = 2 + 2 * kChunk + 18;
@@ -541,6 +542,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                     sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
                     lc.candidates++;
                     if (q.method == 0) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision), &S.objects[obj], o, d);
+                    else subdiv_begin(c, sink, q.tol);
                     clipping = true;
                 }
             }
@@ -554,7 +556,12 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                 found = c.found;
                 if (kAny && found) more = false;  // an any-hit search ends at its first root
             }
-            else found = subdiv_patch(sink, q.tol, lc);
+            else
+            {
+                more = subdiv_step(c, sink, lc, int(E.subdivLevels));
+                found = c.found;
+                if (kAny && found) more = false;
+            }
             if (!more)
             {
                 clipping = false;
@@ -796,7 +803,8 @@ bool valid_engine_config(const EngineConfig& c)
            c.resolveOccupancy >= 0 && c.resolveOccupancy <= 32 && (c.backtrackCache == 0 || c.backtrackCache == 1) &&
            (c.compressedNodes == 0 || c.compressedNodes == 1) && c.queueChunk >= 4 &&
            c.queueChunk <= int(kChunk) && c.queueChunk % 4 == 0 && c.packetWidth >= 1 && c.packetWidth <= 32 &&
-           (c.rayOrder == 0 || c.rayOrder == 1) && (c.originLast == 0 || c.originLast == 1);
+           (c.rayOrder == 0 || c.rayOrder == 1) && (c.originLast == 0 || c.originLast == 1) &&
+           c.subdivLevels >= 1 && c.subdivLevels <= 64;
 }
 
 bool set_engine_config(const EngineConfig& c)
@@ -833,6 +841,7 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
         E.chunk = uint32_t(ec.queueChunk);
         E.packetWidth = uint32_t(ec.packetWidth);
         E.originLast = uint32_t(ec.originLast);
+        E.subdivLevels = uint32_t(ec.subdivLevels);
     }
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const int flat = sms() * 4;
@@ -861,6 +870,7 @@ cudaError_t run_traverse(const DevScene& S, RaysSoA rays, uint32_t n, bool any, 
         E.chunk = uint32_t(ec.queueChunk);
         E.packetWidth = uint32_t(ec.packetWidth);
         E.originLast = uint32_t(ec.originLast);
+        E.subdivLevels = uint32_t(ec.subdivLevels);
     }
     cudaMemsetAsync(E.ctl, 0, sizeof(uint32_t) * 4 * (kMaxPasses + 1), stream);
     const EngineConfig c = engine_config();

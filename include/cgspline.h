@@ -348,6 +348,12 @@ typedef struct cgs_engine_config {
      * it; an occluder found first ends the ray without it.  The order does
      * not change an any-hit answer. */
     int origin_last;
+    /* Subdivision searches (CGS_METHOD_SUBDIV): bisection levels a lane
+     * runs before the clip kernel's next round (1..64; default 8).  The
+     * search is resumable, so a lane that ends its search takes the next
+     * candidate or ray while its warp's other lanes go on; the levels only
+     * set how often the warp meets to refill.  Hits do not change. */
+    int subdiv_levels;
 } cgs_engine_config;
 int cgs_engine_config_get(cgs_engine_config* config);
 int cgs_engine_config_set(const cgs_engine_config* config);
@@ -359,7 +365,8 @@ int cgs_engine_config_set(const cgs_engine_config* config);
  * 4, 8; collect 128, 256 and resolve 64, 128 threads; traversal blocks per SM
  * as many as fit or 768 threads' worth; exact or compressed nodes; queue
  * chunk 8, 16, 32, 64; packet width 1, 8, 16; scanline or tiled ray order;
- * any-hit candidates in traversal order or origin boxes last),
+ * any-hit candidates in traversal order or origin boxes last; for a
+ * subdivision batch, 1, 4, 16 or 64 subdivision levels per round),
  * then passes 2, 4, 8 x first chunk 8, 16, 32, 64 as pairs, each knob set to its fastest
  * value with the others held; a setting already timed is not timed again.
  * Synchronises `stream`. */
