@@ -182,6 +182,34 @@ def test_subdivision_agrees_with_clipping(rt, c1_gpu, c1_oracle, oracle_mod, tor
     compare_hits(g, o, t_rtol=1e-5, uv_atol=2e-3)
 
 
+def test_subdivision_levels_per_round_give_identical_hits(rt, oracle_mod, torch):
+    """The query engine runs subdivision searches resumably, subdiv_levels
+    bisection levels per round of its clip kernel: every setting gives the
+    same hits, bit for bit, as the one-search-per-call inline path (one pass
+    of a one-entry list sends every ray to it)."""
+    g = rt.GpuScene(S.scene_c2(nu=32, nv=32))
+    rays = torch.from_numpy(oracle_mod.camera_rays(S.camera_c2(), 240, 135)).cuda()
+    base = rt.engine_config()
+    out = []
+    try:
+        for cfg in ({"subdiv_levels": 1}, {"subdiv_levels": 8}, {"subdiv_levels": 64},
+                    {"passes": 1, "queue_chunk": 4, "subdiv_levels": 3}):
+            rt.set_engine_config(**{**base, **cfg})
+            out.append(to_host(g.intersect(rays, method=rt.SUBDIV)))
+            assert g.counters()["device_errors"] == 0
+        from cgspline_gb300._capi import CgsError
+        for bad in (0, 65):
+            with pytest.raises(CgsError):
+                rt.set_engine_config(subdiv_levels=bad)
+    finally:
+        rt.set_engine_config(**base)
+    assert (out[0]["patch"] >= 0).sum() > 1000
+    for h in out[1:]:
+        for k in ("t", "u", "v", "patch", "object"):
+            assert np.array_equal(h[k], out[0][k]), k
+    g.close()
+
+
 def test_patch_pairs_entry_point(rt, c1_gpu, c1_scene, oracle_mod, torch):
     rays = oracle_mod.camera_rays(S.camera_c1(), 32, 32)
     n = rays.shape[1]
