@@ -779,7 +779,7 @@ __device__ __forceinline__ void subdiv_begin(ClipState& c, const HitSink& sink, 
     c.cutsideStack = 0; c.tu = 0; c.tv = 0; c.sl = 0; c.it = 0;
     c.fresh = false; c.found = false; c.tol = tol;
 }
-static __device__ __noinline__ bool subdiv_step(ClipState& c, HitSink& sink, LocalCounters& lc, int levels)
+__device__ __forceinline__ bool subdiv_step(ClipState& c, HitSink& sink, LocalCounters& lc, int levels)
 {
     uint32_t trail = uint32_t(c.cutsideStack), tu = c.tu, tv = c.tv;
     int k = c.sl;

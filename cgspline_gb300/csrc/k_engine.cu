@@ -427,8 +427,10 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
 
 // ------------------------------------------------------------ resolve --
 // kG64: the search may take the FP64 grazing path (precision levels 3 and 5);
-// the other levels run an instance without that code.
-template<bool kAny, bool kG64>
+// the other levels run an instance without that code.  kSub: the searches
+// are the subdivision method's (a separate instance, so that the clipping
+// instances' loop holds no subdivision code).
+template<bool kAny, bool kG64, bool kSub = false>
 __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA rays, uint32_t n0,
                                                              const uint32_t* nDev, Eng E, int pass, Query q,
                                                              HitsSoA hits, int32_t* occluded, Counters* cnt)
@@ -541,7 +543,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
                     sink.dist = kAny ? lmax : lt;
                     sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
                     lc.candidates++;
-                    if (q.method == 0) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision), &S.objects[obj], o, d);
+                    if (!kSub) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision), &S.objects[obj], o, d);
                     else subdiv_begin(c, sink, q.tol);
                     clipping = true;
                 }
@@ -550,7 +552,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA
         if (clipping)
         {
             bool found = false, more = false;
-            if (q.method == 0)
+            if (!kSub)
             {
                 more = clip_step<kG64>(c, stack, sink, lc);
                 found = c.found;
@@ -725,13 +727,13 @@ int resident(const void* fn, int threads)
 
 // Resident blocks per SM of kernel fn at `threads` per block (cached: the
 // values depend only on the kernel and the block size).
-template<bool kAny, bool kG64> int per_sm(bool collect, int threads, bool compressed = true)
+template<bool kAny, bool kG64, bool kSub = false> int per_sm(bool collect, int threads, bool compressed = true)
 {
     static const int v[3][2] = {
         {resident((const void*)k_collect<kAny, false>, 128) / sms(),
          resident((const void*)k_collect<kAny, false>, 256) / sms()},
-        {resident((const void*)k_resolve<kAny, kG64>, 64) / sms(),
-         resident((const void*)k_resolve<kAny, kG64>, 128) / sms()},
+        {resident((const void*)k_resolve<kAny, kG64, kSub>, 64) / sms(),
+         resident((const void*)k_resolve<kAny, kG64, kSub>, 128) / sms()},
         {resident((const void*)k_collect<kAny, true>, 128) / sms(),
          resident((const void*)k_collect<kAny, true>, 256) / sms()}};
     return collect ? v[compressed ? 2 : 0][threads == 256] : v[1][threads == 128];
@@ -747,13 +749,14 @@ void launch_collect(int grid, int threads, cudaStream_t stream, const DevScene& 
         k_collect<kAny, false><<<grid, threads, 0, stream>>>(S, rays, n, nDev, E, pass, c.backtrackCache, cnt);
 }
 
-template<bool kAny, bool kG64>
+template<bool kAny, bool kG64, bool kSub = false>
 void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Query q, HitsSoA hits,
             int32_t* occluded, Eng E, Counters* cnt, cudaStream_t stream, int& nl)
 {
     const EngineConfig c = engine_config();
     const int ct = c.collectThreads, rt = c.resolveThreads;
-    const int pc = per_sm<kAny, kG64>(true, ct, c.compressedNodes != 0), pr = per_sm<kAny, kG64>(false, rt);
+    const int pc = per_sm<kAny, kG64, kSub>(true, ct, c.compressedNodes != 0);
+    const int pr = per_sm<kAny, kG64, kSub>(false, rt);
     const int cb = sms() * std::max(1, c.collectOccupancy ? std::min(c.collectOccupancy, pc) : pc);
     const int rb = sms() * std::max(1, c.resolveOccupancy ? std::min(c.resolveOccupancy, pr) : pr);
     const uint32_t warps = (n + 31) / 32;
@@ -768,7 +771,7 @@ void launch(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_t* nDev, Q
             nl++;
         }
         launch_collect<kAny>(gc, ct, stream, S, rays, n, nDev, E, p, c, cnt);
-        k_resolve<kAny, kG64><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
+        k_resolve<kAny, kG64, kSub><<<gr, rt, 0, stream>>>(S, rays, n, nDev, E, p, q, hits, occluded, cnt);
         nl += 2;
     }
     k_pending<<<gp, kPendingThreads, 0, stream>>>(E.status, n, nDev, E.queue[c.passes & 1], E.ctl + 4 * c.passes + 2);
@@ -847,7 +850,12 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     const int flat = sms() * 4;
     k_init<<<flat, 256, 0, stream>>>(rays, n, nDev, hits, any ? occluded : nullptr, E);
     int nl = 1;
-    if (any) launch<true, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    if (q.method != 0)
+    {
+        if (any) launch<true, false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+        else launch<false, false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    }
+    else if (any) launch<true, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     else if (graze_sin(q.precision) > 0.0f) launch<false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     else launch<false, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     if (!any && polishes(q.precision))
