@@ -87,7 +87,7 @@ struct EngineConfig
     int packetWidth = 8;     // the traversal refills a warp once this many lanes are idle (1..32)
     int rayOrder = 1;        // primary rays of a render: 0 in scanline order, 1 in 8 x 4 pixel tiles
     int originLast = 0;      // any hit: 1 searches the candidates whose leaf box holds the origin last
-    int subdivLevels = 8;    // subdivision searches: bisection levels a lane runs per resolve round (1..64)
+    int subdivLevels = 4;    // subdivision searches: bisection levels a lane runs per resolve round (1..64)
 };
 EngineConfig engine_config();
 bool set_engine_config(const EngineConfig& c);

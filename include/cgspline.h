@@ -349,7 +349,7 @@ typedef struct cgs_engine_config {
      * not change an any-hit answer. */
     int origin_last;
     /* Subdivision searches (CGS_METHOD_SUBDIV): bisection levels a lane
-     * runs before the clip kernel's next round (1..64; default 8).  The
+     * runs before the clip kernel's next round (1..64; default 4).  The
      * search is resumable, so a lane that ends its search takes the next
      * candidate or ray while its warp's other lanes go on; the levels only
      * set how often the warp meets to refill.  Hits do not change. */
