@@ -429,9 +429,10 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
 // kG64: the search may take the FP64 grazing path (precision levels 3 and 5);
 // the other levels run an instance without that code.  kSub: the searches
 // are the subdivision method's (a separate instance, so that the clipping
-// instances' loop holds no subdivision code).
+// instances' loop holds no subdivision code).  The FP32 clipping instances
+// are held to 128 registers, four 128-thread blocks per SM.
 template<bool kAny, bool kG64, bool kSub = false>
-__global__ void __launch_bounds__(kResolveThreads) k_resolve(DevScene S, RaysSoA rays, uint32_t n0,
+__global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_resolve(DevScene S, RaysSoA rays, uint32_t n0,
                                                              const uint32_t* nDev, Eng E, int pass, Query q,
                                                              HitsSoA hits, int32_t* occluded, Counters* cnt)
 {
