@@ -602,14 +602,10 @@ struct ClipState
     bool found, b64;  // b64: FP64 projection and fat-line bounds (near-grazing)
     bool fresh;       // the net is still to be projected (the search's first step)
     bool tposed;      // buf holds the transposed net (left so by a cut along v)
-    // the resumable subdivision search (subdiv_step) keeps its walk in the same
-    // state: the bit trail in cutsideStack, the level in sl, the sub-domain's
-    // integer coordinates in tu / tv, and `fresh` as its reload flag
-    uint32_t tu, tv;
-    // b64: the ray the net is projected from (origin, direction), kept in
-    // local memory: read only where a projection starts, it would otherwise
-    // hold twelve registers through the whole search
-    volatile double ray64[6];
+    // The resumable subdivision search (subdiv_step) keeps its walk in the
+    // same state: the bit trail in cutsideStack, the level in sl, the
+    // sub-domain's integer coordinates in the bits of emin (which it does not
+    // use otherwise), and `fresh` as its reload flag.
 };
 
 // grazeSin > 0: the precision form (candidates within asin(grazeSin) of
@@ -618,10 +614,14 @@ struct ClipState
 // cache).
 // ob, wo, wd: the candidate's object and the world ray, from which a
 // near-grazing candidate's ray is recomputed in double (to_local64); a null
-// ob projects it from the FP32 ray in the sink.
+// ob projects it from the FP32 ray in the sink.  ray64: where that ray
+// (origin, direction) is kept for the search's projections, a six-double
+// array in local memory (read only where a projection starts, it would
+// otherwise hold twelve registers through the whole search).
 template<bool kG64 = true>
 __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, float tol, float grazeSin,
-                                           const DevObject* ob = nullptr, float3 wo = {}, float3 wd = {})
+                                           volatile double* ray64, const DevObject* ob = nullptr, float3 wo = {},
+                                           float3 wd = {})
 {
     c.b64 = kG64 && grazeSin > 0.0f && near_grazing(sink.P, sink.d, grazeSin);
     c.tol = c.b64 ? kGrazeTol : tol;
@@ -630,8 +630,8 @@ __device__ __forceinline__ void clip_begin(ClipState& c, const HitSink& sink, fl
         Ray64 r;
         if (ob) r = to_local64(*ob, wo, wd);
         else r = Ray64 {make_double3(sink.o.x, sink.o.y, sink.o.z), make_double3(sink.d.x, sink.d.y, sink.d.z)};
-        c.ray64[0] = r.o.x; c.ray64[1] = r.o.y; c.ray64[2] = r.o.z;
-        c.ray64[3] = r.d.x; c.ray64[4] = r.d.y; c.ray64[5] = r.d.z;
+        ray64[0] = r.o.x; ray64[1] = r.o.y; ray64[2] = r.o.z;
+        ray64[3] = r.d.x; ray64[4] = r.d.y; ray64[5] = r.d.z;
     }
     c.fresh = true;  // the first clip_step projects the net
     c.tposed = false;
@@ -670,7 +670,8 @@ __device__ __forceinline__ void transpose_if(float2* p, bool t)
 // natural orientation.  A loop iteration costs the union of the paths its
 // lanes take, so the transposes are kept off the paths that differ.
 template<bool kG64 = true>
-__device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, LocalCounters& lc)
+__device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sink, LocalCounters& lc,
+                                          const volatile double* ray64)
 {
     const bool b64 = kG64 && c.b64;
     const bool fresh = c.fresh;
@@ -732,8 +733,8 @@ __device__ __forceinline__ bool clip_step(ClipState& c, float4* st, HitSink& sin
     if (fresh || pop)
     {
         if (b64)
-            project_net64(c.buf, sink.P, make_double3(c.ray64[0], c.ray64[1], c.ray64[2]),
-                          make_double3(c.ray64[3], c.ray64[4], c.ray64[5]));
+            project_net64(c.buf, sink.P, make_double3(ray64[0], ray64[1], ray64[2]),
+                          make_double3(ray64[3], ray64[4], ray64[5]));
         else project_net(c.buf, sink.P, sink.o, sink.d);
         c.tposed = false;
     }
@@ -756,8 +757,9 @@ static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, float g
 {
     float4 st[kClipStack];
     ClipState c;
-    clip_begin(c, sink, tol, grazeSin, ob, wo, wd);
-    while (clip_step(c, st, sink, lc) && !(anyHit && c.found)) {}
+    volatile double ray64[6];
+    clip_begin(c, sink, tol, grazeSin, ray64, ob, wo, wd);
+    while (clip_step(c, st, sink, lc, ray64) && !(anyHit && c.found)) {}
     return c.found;
 }
 
@@ -776,12 +778,13 @@ static __device__ __noinline__ bool clip_patch(HitSink& sink, float tol, float g
 __device__ __forceinline__ void subdiv_begin(ClipState& c, const HitSink& sink, float tol)
 {
     project_net(c.buf, sink.P, sink.o, sink.d);
-    c.cutsideStack = 0; c.tu = 0; c.tv = 0; c.sl = 0; c.it = 0;
+    c.cutsideStack = 0; c.sl = 0; c.it = 0;
+    c.emin = make_float2(__uint_as_float(0u), __uint_as_float(0u));  // tu, tv
     c.fresh = false; c.found = false; c.tol = tol;
 }
 __device__ __forceinline__ bool subdiv_step(ClipState& c, HitSink& sink, LocalCounters& lc, int levels)
 {
-    uint32_t trail = uint32_t(c.cutsideStack), tu = c.tu, tv = c.tv;
+    uint32_t trail = uint32_t(c.cutsideStack), tu = __float_as_uint(c.emin.x), tv = __float_as_uint(c.emin.y);
     int k = c.sl;
     bool more = true;
     for (int s = 0; s < levels; s++)
@@ -830,7 +833,7 @@ __device__ __forceinline__ bool subdiv_step(ClipState& c, HitSink& sink, LocalCo
         if (((k - 1) & 1) == 0) tu |= 1u; else tv |= 1u;
         c.fresh = true;
     }
-    c.cutsideStack = int(trail); c.tu = tu; c.tv = tv; c.sl = k;
+    c.cutsideStack = int(trail); c.emin = make_float2(__uint_as_float(tu), __uint_as_float(tv)); c.sl = k;
     return more;
 }
 

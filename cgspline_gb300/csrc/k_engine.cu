@@ -429,8 +429,9 @@ __global__ void __launch_bounds__(kCollectThreads, 4) k_collect(DevScene S, Rays
 // kG64: the search may take the FP64 grazing path (precision levels 3 and 5);
 // the other levels run an instance without that code.  kSub: the searches
 // are the subdivision method's (a separate instance, so that the clipping
-// instances' loop holds no subdivision code).  The FP32 clipping instances
-// are held to 128 registers, four 128-thread blocks per SM.
+// instances' loop holds no subdivision code; at the grazing levels the kG64
+// instance runs subdivision searches whole instead).  The FP32 clipping
+// instances are held to 128 registers, four 128-thread blocks per SM.
 template<bool kAny, bool kG64, bool kSub = false>
 __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_resolve(DevScene S, RaysSoA rays, uint32_t n0,
                                                              const uint32_t* nDev, Eng E, int pass, Query q,
@@ -439,6 +440,7 @@ __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_r
     const uint32_t n = nDev ? *nDev : n0;
     LocalCounters lc;
     float4 stack[kClipStack];
+    volatile double ray64[6];  // kG64: a near-grazing search's ray in double
     ClipState c;
     HitSink sink {nullptr, f3(0, 0, 0), f3(0, 0, 1), 0.0f, make_float2(0, 0)};
     bool active = false, exhausted = false, clipping = false;
@@ -544,8 +546,9 @@ __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_r
                     sink.dist = kAny ? lmax : lt;
                     sink.uv = kAny ? make_float2(0.0f, 0.0f) : make_float2(lu, lv);
                     lc.candidates++;
-                    if (!kSub) clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision), &S.objects[obj], o, d);
-                    else subdiv_begin(c, sink, q.tol);
+                    if (kSub) subdiv_begin(c, sink, q.tol);
+                    else if (!(kG64 && q.method != 0))
+                        clip_begin<kG64>(c, sink, q.tol, graze_sin(q.precision), ray64, &S.objects[obj], o, d);
                     clipping = true;
                 }
             }
@@ -553,9 +556,14 @@ __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_r
         if (clipping)
         {
             bool found = false, more = false;
-            if (!kSub)
+            if (kG64 && q.method != 0)
             {
-                more = clip_step<kG64>(c, stack, sink, lc);
+                // the precision form's subdivision searches run whole, one call each
+                found = subdiv_patch(sink, q.tol, lc);
+            }
+            else if (!kSub)
+            {
+                more = clip_step<kG64>(c, stack, sink, lc, ray64);
                 found = c.found;
                 if (kAny && found) more = false;  // an any-hit search ends at its first root
             }
@@ -851,13 +859,14 @@ cudaError_t run_query(const DevScene& S, RaysSoA rays, uint32_t n, const uint32_
     const int flat = sms() * 4;
     k_init<<<flat, 256, 0, stream>>>(rays, n, nDev, hits, any ? occluded : nullptr, E);
     int nl = 1;
-    if (q.method != 0)
-    {
-        if (any) launch<true, false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
-        else launch<false, false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
-    }
-    else if (any) launch<true, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    // the FP64 grazing instance serves both methods at its level (its
+    // subdivision searches run whole); measured, it also runs the grazing
+    // clip 35% faster with that one-call search compiled in (6.35 against
+    // 4.72 Mrays/s on 2^20 grazing rays), a code-generation effect
+    if (any) q.method != 0 ? launch<true, false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl)
+                           : launch<true, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     else if (graze_sin(q.precision) > 0.0f) launch<false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
+    else if (q.method != 0) launch<false, false, true>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     else launch<false, false>(S, rays, n, nDev, q, hits, occluded, E, cnt, stream, nl);
     if (!any && polishes(q.precision))
     {

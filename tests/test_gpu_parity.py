@@ -207,6 +207,13 @@ def test_subdivision_levels_per_round_give_identical_hits(rt, oracle_mod, torch)
     for h in out[1:]:
         for k in ("t", "u", "v", "patch", "object"):
             assert np.array_equal(h[k], out[0][k]), k
+    # at the precision form's level the FP64 grazing instance runs the
+    # subdivision searches whole; the grazing test concerns clipping only, so
+    # the polished hits equal those of FP32 + FP64 polish
+    a = to_host(g.intersect(rays, method=rt.SUBDIV, precision=rt.FP32_GRAZE64))
+    b = to_host(g.intersect(rays, method=rt.SUBDIV, precision=rt.FP32_POLISH64))
+    for k in ("t", "u", "v", "patch", "object"):
+        assert np.array_equal(a[k], b[k]), k
     g.close()
 
 
