@@ -132,6 +132,7 @@ SIGNATURES = [
     ("cgs_autotune_render", C.c_int, [P, C.POINTER(RenderRequest), U32, C.POINTER(RenderOptions), C.c_int,
                                       C.POINTER(EngineConfig), C.POINTER(C.c_double), P]),
     ("cgs_scene_counters", C.c_int, [P, C.POINTER(Counters)]),
+    ("cgs_debug_fail_allocation", C.c_int, [U32]),
     ("cgs_perfect_hash_build", C.c_int, [P, U32, P, U32, P, U32, P, P]),
     ("cgs_server_create", C.c_int, [C.POINTER(P), P, C.POINTER(ServerOptions)]),
     ("cgs_server_destroy", C.c_int, [P]),

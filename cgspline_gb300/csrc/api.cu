@@ -9,6 +9,8 @@ using namespace cgs;
 
 namespace cgs {
 
+std::atomic<uint32_t> g_failAllocation {0};
+
 void camera_setup(const cgs_camera& c, uint32_t w, uint32_t h, int flip, CameraSetup& s)
 {
     // Transform::matrix() = T R S with the quaternion rotation of src/AlignedTypes.h:99-115
@@ -36,9 +38,12 @@ void camera_setup(const cgs_camera& c, uint32_t w, uint32_t h, int flip, CameraS
     if (flip) { s.tl[1] = -s.tl[1]; s.half_dy = -s.half_dy; }
 }
 
+// A failed reserve frees the old buffer: each capacity below is cleared
+// before its buffer grows, so that it never outlives the memory it describes.
 int ensure_engine(cgs_scene* sc, uint32_t capacity)
 {
-    if (sc->engineCapacity >= capacity) return CGS_OK;
+    if (sc->engineCapacity >= capacity && sc->engine.p) return CGS_OK;
+    sc->engineCapacity = 0;
     CGS_TRY(sc->engine.reserve(engine_words(capacity, kEnginePasses)));
     sc->engineCapacity = capacity;
     return CGS_OK;
@@ -149,6 +154,9 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
     if (wb.capacity >= samples && wb.lightCapacity >= nl && wb.engine) return CGS_OK;
     const size_t cap = std::max<uint32_t>(samples, wb.capacity);
     const uint32_t lc = std::max<uint32_t>(nl, wb.lightCapacity);
+    // the buffers below may be freed by a reserve that fails: the view is
+    // cleared first and set again only once all of them are in place
+    wb.capacity = 0; wb.lightCapacity = 0; wb.engine = nullptr; wb.engine2 = nullptr;
     const size_t sc = cap * lc;
     if (sc >= (1ull << 31)) return CGS_ERR_INVALID_ARGUMENT;
     CGS_TRY(ray0.reserve(9 * cap));
@@ -165,13 +173,15 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
     // the closest-hit queries hold `cap` rays, the shadow queries `sc`; with no
     // side stream both run on the first scratch
     const uint32_t ecap = uint32_t(side ? cap : std::max(cap, sc)), ecap2 = uint32_t(side ? sc : 0);
-    if (engineCapacity < ecap)
+    if (engineCapacity < ecap || !engine.p)
     {
+        engineCapacity = 0;
         CGS_TRY(engine.reserve(engine_words(ecap, kEnginePasses)));
         engineCapacity = ecap;
     }
-    if (ecap2 && engine2Capacity < ecap2)
+    if (ecap2 && (engine2Capacity < ecap2 || !engine2.p))
     {
+        engine2Capacity = 0;
         CGS_TRY(engine2.reserve(engine_words(ecap2, kEnginePasses)));
         engine2Capacity = ecap2;
     }
@@ -204,6 +214,9 @@ int RenderSlot::ensure(uint32_t samples, uint32_t lights, uint32_t nreq)
 int RenderSlot::ensure_engine(uint32_t rays)
 {
     if (engineCapacity >= rays && engine.p) return CGS_OK;
+    engineCapacity = 0;
+    wb.engine = nullptr;
+    wb.engineCapacity = 0;
     CGS_TRY(engine.reserve(engine_words(rays, kEnginePasses)));
     engineCapacity = rays;
     wb.engine = engine.p;
@@ -345,6 +358,12 @@ void query_end(cgs_scene* s, cudaStream_t st, bool captured)
 }  // namespace cgs
 
 extern "C" {
+
+int cgs_debug_fail_allocation(uint32_t nth)
+{
+    cgs::g_failAllocation.store(nth, std::memory_order_relaxed);
+    return CGS_OK;
+}
 
 int cgs_intersect(cgs_scene* s, const cgs_rays* rays, uint32_t n, int method, int precision, float tol, int any_hit,
                   const cgs_hits* hits, void* stream)

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -75,6 +76,16 @@ struct Group
     bool touched = false;  // objects, lights or environment were set
 };
 
+// Failure injection (cgs_debug_fail_allocation): growths left before the one
+// that reports out of memory, 0 when off.
+extern std::atomic<uint32_t> g_failAllocation;
+inline bool injected_allocation_failure()
+{
+    uint32_t k = g_failAllocation.load(std::memory_order_relaxed);
+    while (k != 0 && !g_failAllocation.compare_exchange_weak(k, k - 1, std::memory_order_relaxed)) {}
+    return k == 1;
+}
+
 template<class T> struct DBuf
 {
     T* p = nullptr;
@@ -84,6 +95,7 @@ template<class T> struct DBuf
         if (count <= n) return cudaSuccess;
         if (p) cudaFree(p);
         p = nullptr; n = 0;
+        if (injected_allocation_failure()) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
         if (e == cudaSuccess) n = count;
         return e;
@@ -236,7 +248,7 @@ void hash_coefficients(uint32_t n, uint32_t A[16], uint32_t B[16]);
 int ensure_engine(cgs_scene* sc, uint32_t capacity);
 inline bool valid_query(int method, int precision)
 {
-    return (method == 0 || method == 1) && precision >= 0 && precision <= 3;
+    return (method == 0 || method == 1) && precision >= 0 && precision <= 4;
 }
 // Fill `out` (device request table of `slot`) and the batch description for
 // n requests; validates them.  Returns a status.

@@ -144,6 +144,7 @@ int cgs_server::grow(Slot& s, int kind, uint32_t units, uint32_t nchunks)
     if (s.rs.bytes() - s.rs.engine.bytes() + query_bytes(cap) > share) s.rs.release();
     if (cap != s.qcap)
     {
+        s.qcap = 0;  // a reserve that fails frees its old buffer
         CGS_TRY(s.qrays.reserve(7ull * cap));
         CGS_TRY(s.qgroup.reserve(cap));
         CGS_TRY(s.qhitF.reserve(3ull * cap));

@@ -23,7 +23,7 @@ from . import _capi
 from ._capi import check
 
 CLIP, SUBDIV = 0, 1
-FP32, FP32_POLISH64, FP64, FP32_GRAZE64 = 0, 1, 2, 3
+FP32, FP32_POLISH64, FP64, FP32_GRAZE64, FP32_SILHOUETTE64 = 0, 1, 2, 3, 4
 PLAIN, WAVEFRONT = 0, 1
 SPLIT_REFERENCE, SPLIT_LONGEST = 0, 1
 MIRROR, MONTE_CARLO = 0, 1
@@ -531,6 +531,12 @@ def set_engine_config(**kw):
     cur.update(kw)
     c = _capi.EngineConfig(**cur)
     check(lib.cgs_engine_config_set(C.byref(c)), "cgs_engine_config_set")
+
+
+def debug_fail_allocation(nth: int):
+    """cgs_debug_fail_allocation: the nth growth of a working buffer from now
+    on (1 = the next) reports out of memory on the host; 0 cancels."""
+    check(_capi.load().cgs_debug_fail_allocation(int(nth)), "cgs_debug_fail_allocation")
 
 
 def autotune(scene: GpuScene, requests, options: Options | None = None, repeats: int = 3, stream=None):

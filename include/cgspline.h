@@ -43,12 +43,18 @@ enum cgs_method { CGS_METHOD_CLIP = 0, CGS_METHOD_SUBDIV = 1 };
  * FP32_POLISH64: FP32 search and traversal, then an FP64 Newton polish of
  * (u,v,t) of the winning hit.  FP32_GRAZE64 (the full precision form):
  * FP32_POLISH64, and candidates the ray meets within 30 degrees of grazing
- * (of the plane of the patch's diagonals) are searched on a net projected in
- * FP64 with FP64 fat-line bounds to tolerance 2^-20.  FP64: the whole search
- * in FP64 (traversal, clipping to 1e-9, every root polished), the comparison
- * run of the precision form.  Any-hit searches (shadow rays, any_hit
- * queries) always run in FP32. */
-enum cgs_precision { CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP64 = 2, CGS_PREC_FP32_GRAZE64 = 3 };
+ * (of the plane of the patch's diagonals or of a cell of its control net), or
+ * whose control net folds over the ray (a silhouette), are searched on a net
+ * projected in FP64 from the ray in double, with FP64 fat-line bounds to
+ * tolerance 2^-20.  FP32_SILHOUETTE64: the same with 5 degrees in place of
+ * 30, so that mostly silhouettes take the FP64 search.  FP64: the whole
+ * search in FP64 (traversal, clipping to 1e-9, every root polished), the
+ * comparison run of the precision form.  Any-hit searches (shadow rays,
+ * any_hit queries) always run in FP32. */
+enum cgs_precision {
+    CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP64 = 2, CGS_PREC_FP32_GRAZE64 = 3,
+    CGS_PREC_FP32_SILHOUETTE64 = 4
+};
 /* Split axis of the BVH build.  REFERENCE: BVH::split's axis, taken from a
  * box that is never inflated (src/rt/BVH.cpp:46-52) and so always y -- the
  * reference's topology, bit for bit.  LONGEST: the longest axis of the
@@ -379,6 +385,14 @@ int cgs_render_running(cgs_scene* scene);
 
 /* Counters of the scene's last query or render (synchronises the stream it ran on). */
 int cgs_scene_counters(cgs_scene* scene, cgs_counters* out);
+
+/* Failure injection on the host, for tests of the out-of-memory paths: the
+ * nth growth of a working buffer from now on (scratch, staging and slot
+ * buffers of queries, renders and servers; 1 = the next) frees the old
+ * buffer and reports CGS_ERR_OUT_OF_MEMORY without calling the allocator.
+ * 0 cancels.  No device work is involved; the calls that fail return the
+ * status, and the next call grows its buffers again. */
+int cgs_debug_fail_allocation(uint32_t nth);
 
 /* ------------------------------------------------------ perfect hash -- */
 /* PerfectHashFunction::build on n device keys (src/rt/PerfectHashFunction.cu:229-503).
