@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--schedule", default="wavefront", choices=["wavefront", "plain"])
-    ap.add_argument("--precision", default="polish64", choices=["fp32", "polish64", "silhouette64", "graze64"])
+    ap.add_argument("--precision", default="polish64", choices=["fp32", "polish64", "graze64"])
     ap.add_argument("--split", default="reference", choices=["reference", "longest"],
                     help="BVH split axis of the headline frame")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
@@ -330,17 +330,16 @@ def frame_leg(rt, torch, g, cam, tracer, frame, stream, flush, steps):
 
 def precision_leg(rt, scenes, torch, dev, g, scene, flush, n=1 << 20):
     """2^20 seeded grazing rays (within 0.5 degrees of the tangent plane at
-    random points of the torus): FP32, FP32 + FP64 polish, and the precision
-    forms (FP32 + FP64 polish + FP64 fat-line bounds for candidates within 5 or
-    30 degrees of grazing, and silhouettes) against the pure-FP64 GPU search,
-    with the throughput of each."""
+    random points of the torus): FP32, FP32 + FP64 polish, and the full
+    precision form (FP32 + FP64 polish + FP64 fat-line bounds for near-grazing
+    candidates) against the pure-FP64 GPU search, with the throughput of each."""
     import numpy as np
     rays = torch.from_numpy(scenes.grazing_rays(scene.surfaces[0], n, seed=3)).to(dev)
     stream = torch.cuda.current_stream()
     out = {"rays": n, "workload": "2^20 grazing rays, torus 16384 patches, closest hit"}
     res = {}
     for name, prec in (("fp64", rt.FP64), ("fp32", rt.FP32), ("fp32_polish64", rt.FP32_POLISH64),
-                       ("fp32_silhouette64", rt.FP32_SILHOUETTE64), ("fp32_graze64", rt.FP32_GRAZE64)):
+                       ("fp32_graze64", rt.FP32_GRAZE64)):
         g.intersect(rays, precision=prec)
         torch.cuda.synchronize()
         reps = 1 if prec == rt.FP64 else 3
@@ -349,7 +348,7 @@ def precision_leg(rt, scenes, torch, dev, g, scene, flush, n=1 << 20):
         res[name] = {k: v.cpu().numpy() for k, v in holder["r"].items()}
         out[name] = {"Mrays_s": n / (sum(ms) / reps * 1e-3) / 1e6, "ms": sum(ms) / reps}
     ref = res["fp64"]
-    for name in ("fp32", "fp32_polish64", "fp32_silhouette64", "fp32_graze64"):
+    for name in ("fp32", "fp32_polish64", "fp32_graze64"):
         a = res[name]
         both = (a["patch"] >= 0) & (ref["patch"] >= 0)
         rel = np.abs(a["t"][both] - ref["t"][both]) / ref["t"][both]
@@ -362,7 +361,7 @@ def precision_leg(rt, scenes, torch, dev, g, scene, flush, n=1 << 20):
     import oracle
     host_rays = rays.cpu().numpy()
     o64 = oracle.OracleScene(scene).intersect(host_rays, precision=oracle.FP64)
-    for name in ("fp64", "fp32", "fp32_polish64", "fp32_silhouette64", "fp32_graze64"):
+    for name in ("fp64", "fp32", "fp32_polish64", "fp32_graze64"):
         a = res[name]
         both = (a["patch"] >= 0) & (o64["patch"] >= 0)
         rel = np.abs(a["t"][both] - o64["t"][both]) / o64["t"][both]
@@ -454,8 +453,8 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
     one k_render_plain launch per request (the reference's per-frame launch
     shape), back to back; both on the reference's BVH topology, and the
     batched path again on the longest-axis build, with the FP32 + FP64-polish
-    form and with the two precision forms (FP64 fat-line bounds for
-    candidates within 5 or 30 degrees of grazing, and silhouettes, added)."""
+    form and with the full precision form (FP64 fat-line bounds for
+    near-grazing candidates added)."""
     t0 = time.perf_counter()
     scs = [scenes.scene_c4(i) for i in range(64)]
     cams = [scenes.camera_c4(i) for i in range(64)]
@@ -475,7 +474,6 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
         out[f"autotune_{split_name}"] = {"settings": cfg, "ms": tms, "seconds": time.perf_counter() - t0}
         legs = (("batched", rt.WAVEFRONT, prec), ("plain", rt.PLAIN, prec)) if split == rt.SPLIT_REFERENCE else \
             (("batched_split_longest", rt.WAVEFRONT, prec),
-             ("batched_split_longest_silhouette64", rt.WAVEFRONT, rt.FP32_SILHOUETTE64),
              ("batched_split_longest_graze64", rt.WAVEFRONT, rt.FP32_GRAZE64))
         for name, sched, p in legs:
             tr = rt.RayTracer(rt.Options(recursion_depth=DEPTH, precision=p, schedule=sched))
@@ -499,23 +497,20 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
             out["accuracy"] = accuracy_vs_fp64(rt, store, rays, prec, grp)
         else:
             out["accuracy_split_longest"] = accuracy_vs_fp64(rt, store, rays, prec, grp)
-            out["accuracy_split_longest_silhouette64"] = \
-                accuracy_vs_fp64(rt, store, rays, rt.FP32_SILHOUETTE64, grp)
             out["accuracy_split_longest_graze64"] = accuracy_vs_fp64(rt, store, rays, rt.FP32_GRAZE64, grp)
         store.close()
     rt.set_engine_config(**out["autotune_reference"]["settings"])
     out["speedup_vs_plain"] = out["batched"]["value"] / out["plain"]["value"]
     out["speedup_vs_plain_split_longest"] = out["batched_split_longest"]["value"] / out["plain"]["value"]
-    for lv in ("silhouette64", "graze64"):
-        out[f"speedup_vs_plain_split_longest_{lv}"] = \
-            out[f"batched_split_longest_{lv}"]["value"] / out["plain"]["value"]
+    out["speedup_vs_plain_split_longest_graze64"] = \
+        out["batched_split_longest_graze64"]["value"] / out["plain"]["value"]
     out["engine_settings"] = rt.engine_config()
     return out
 
 
 SERVE_RES = ((256, 256), (512, 512), (1920, 1080), (3840, 2160))
 PRECISIONS = {"fp32": lambda rt: rt.FP32, "polish64": lambda rt: rt.FP32_POLISH64,
-              "silhouette64": lambda rt: rt.FP32_SILHOUETTE64, "graze64": lambda rt: rt.FP32_GRAZE64}
+              "graze64": lambda rt: rt.FP32_GRAZE64}
 
 
 def serving_stream(n, seed=9):
@@ -608,17 +603,8 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
     out["served_stats"] = {k: st[k] for k in ("batches", "chunks", "peak_slot_bytes", "kernel_launches")}
     for sv in servers.values():
         sv.close()
-    # the 5-degree precision form at saturation only (longest-axis build), once
-    # the other servers have given back their slot buffers
-    sil = rt.Server(stores["longest"], slots=slots, memory_budget=budget_gb << 30,
-                    options=rt.Options(recursion_depth=3, precision=rt.FP32_SILHOUETTE64))
-    play(sil, 0, 1)
-    sat["served_split_longest_silhouette64"] = play(sil, 0, 7)
-    sil.close()
     sat["speedup"] = sat["served"]["Mrays_s"] / sat["plain"]["Mrays_s"]
     sat["speedup_split_longest"] = sat["served_split_longest"]["Mrays_s"] / sat["plain"]["Mrays_s"]
-    sat["speedup_split_longest_silhouette64"] = \
-        sat["served_split_longest_silhouette64"]["Mrays_s"] / sat["plain"]["Mrays_s"]
     out["saturation"] = sat
     # accuracy: 1% of 512x512 primary rays of every scene, against the FP64 GPU search
     rays, grp = [], []
@@ -629,8 +615,7 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
         grp.append(torch.full((sub.numel(),), i, dtype=torch.int32, device=dev))
     rays, grp = torch.cat(rays, 1).contiguous(), torch.cat(grp)
     out["accuracy_split_longest"] = accuracy_vs_fp64(rt, stores["longest"], rays, prec, grp)
-    out["accuracy_split_longest_silhouette64"] = \
-        accuracy_vs_fp64(rt, stores["longest"], rays, rt.FP32_SILHOUETTE64, grp)
+    out["accuracy_split_longest_graze64"] = accuracy_vs_fp64(rt, stores["longest"], rays, rt.FP32_GRAZE64, grp)
     for s in stores.values():
         s.close()
     out["engine_settings"] = rt.engine_config()

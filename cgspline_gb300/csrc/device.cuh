@@ -400,23 +400,17 @@ constexpr int kGrazeIterations = 1024;
 
 // Precision levels (enum cgs_precision) of closest-hit searches: 0 FP32;
 // 1 FP32 + FP64 polish; 2 pure FP64; 3 as 1, with the FP64 bounds for
-// candidates within 30 degrees of grazing or whose control net folds over the
-// ray (a silhouette); 4 the same with 5 degrees.  Internal levels 5 and 6:
-// the searches of 3 and 4 without the polish (closest-hit passes whose
-// polish runs separately).  Any-hit searches run at level 0.
-__host__ __device__ __forceinline__ bool polishes(int precision)
-{
-    return precision == 1 || precision == 3 || precision == 4;
-}
+// candidates within 30 degrees of grazing.  Internal level 5: the search of
+// 3 without the polish (closest-hit passes whose polish runs separately).
+// Any-hit searches run at level 0.
+__host__ __device__ __forceinline__ bool polishes(int precision) { return precision == 1 || precision == 3; }
 __host__ __device__ __forceinline__ float graze_sin(int precision)
 {
-    if (precision == 3 || precision == 5) return 0.5f;           // sin 30 degrees
-    if (precision == 4 || precision == 6) return 0.0871557427f;  // sin 5 degrees
-    return 0.0f;
+    return (precision == 3 || precision == 5) ? 0.5f : 0.0f;  // sin 30 degrees
 }
 __host__ __device__ __forceinline__ int search_only(int precision)
 {
-    return precision == 3 || precision == 5 ? 5 : precision == 4 || precision == 6 ? 6 : 0;
+    return precision == 3 ? 5 : precision == 5 ? 5 : 0;
 }
 
 __device__ __forceinline__ double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }

@@ -248,7 +248,7 @@ void hash_coefficients(uint32_t n, uint32_t A[16], uint32_t B[16]);
 int ensure_engine(cgs_scene* sc, uint32_t capacity);
 inline bool valid_query(int method, int precision)
 {
-    return (method == 0 || method == 1) && precision >= 0 && precision <= 4;
+    return (method == 0 || method == 1) && precision >= 0 && precision <= 3;
 }
 // Fill `out` (device request table of `slot`) and the batch description for
 // n requests; validates them.  Returns a status.

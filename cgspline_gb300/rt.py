@@ -23,7 +23,7 @@ from . import _capi
 from ._capi import check
 
 CLIP, SUBDIV = 0, 1
-FP32, FP32_POLISH64, FP64, FP32_GRAZE64, FP32_SILHOUETTE64 = 0, 1, 2, 3, 4
+FP32, FP32_POLISH64, FP64, FP32_GRAZE64 = 0, 1, 2, 3
 PLAIN, WAVEFRONT = 0, 1
 SPLIT_REFERENCE, SPLIT_LONGEST = 0, 1
 MIRROR, MONTE_CARLO = 0, 1

@@ -46,15 +46,10 @@ enum cgs_method { CGS_METHOD_CLIP = 0, CGS_METHOD_SUBDIV = 1 };
  * (of the plane of the patch's diagonals or of a cell of its control net), or
  * whose control net folds over the ray (a silhouette), are searched on a net
  * projected in FP64 from the ray in double, with FP64 fat-line bounds to
- * tolerance 2^-20.  FP32_SILHOUETTE64: the same with 5 degrees in place of
- * 30, so that mostly silhouettes take the FP64 search.  FP64: the whole
- * search in FP64 (traversal, clipping to 1e-9, every root polished), the
- * comparison run of the precision form.  Any-hit searches (shadow rays,
- * any_hit queries) always run in FP32. */
-enum cgs_precision {
-    CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP64 = 2, CGS_PREC_FP32_GRAZE64 = 3,
-    CGS_PREC_FP32_SILHOUETTE64 = 4
-};
+ * tolerance 2^-20.  FP64: the whole search in FP64 (traversal, clipping to
+ * 1e-9, every root polished), the comparison run of the precision form.
+ * Any-hit searches (shadow rays, any_hit queries) always run in FP32. */
+enum cgs_precision { CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP64 = 2, CGS_PREC_FP32_GRAZE64 = 3 };
 /* Split axis of the BVH build.  REFERENCE: BVH::split's axis, taken from a
  * box that is never inflated (src/rt/BVH.cpp:46-52) and so always y -- the
  * reference's topology, bit for bit.  LONGEST: the longest axis of the

@@ -172,8 +172,7 @@ class OracleScene:
     def intersect(self, rays, method=CLIP_HOST, precision=FP32, tol=2.0 ** -12, tol64=1e-9, any_hit=False,
                   nthreads=None, counters=False, graze_sin=GRAZE_30):
         """graze_sin: the grazing margin of CLIP_GRAZE64 (GRAZE_5 restates the
-        GPU's FP32_SILHOUETTE64 level, GRAZE_30 its FP32_GRAZE64 level; both
-        with precision FP32_POLISH64)."""
+        GPU's FP32_POLISH64 level, GRAZE_30 its FP32_GRAZE64 level)."""
         L = lib()
         L.ora_set_graze_sin(graze_sin)
         rays = np.ascontiguousarray(rays, np.float32)

@@ -42,18 +42,22 @@ def torus():
 
 
 def host(d):
-    return {k: v.cpu().numpy() for k, v in d.items()}
+    return {k: v if isinstance(v, np.ndarray) else v.cpu().numpy() for k, v in d.items()}
 
 
 def same_hits(a, b):
     return all(np.array_equal(a[k], b[k]) for k in a)
 
 
-@pytest.mark.parametrize("nth", [1, 2])
-def test_query_scratch_grows_again(rt, torus, torch, nth):
+# device rays grow the engine scratch only; host rays grow the ray staging,
+# the two hit stagings and then the engine scratch, in that order
+@pytest.mark.parametrize("where,nth", [("device", 1), ("host", 1), ("host", 3), ("host", 4)])
+def test_query_scratch_grows_again(rt, torus, torch, where, nth):
     from cgspline_gb300 import _capi
     small = rt.camera_rays(S.camera_c2(), 64, 36)
     big = rt.camera_rays(S.camera_c2(), 320, 180)
+    if where == "host":
+        small, big = small.cpu().numpy(), big.cpu().numpy()
     fresh = rt.GpuScene(torus)
     want_small, want_big = host(fresh.intersect(small)), host(fresh.intersect(big))
     fresh.close()

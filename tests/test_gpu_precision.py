@@ -66,16 +66,15 @@ def test_fp64_gpu_matches_fp64_oracle(rt, torus, torus_gpu, oracle_mod, torch, k
     assert torus_gpu.counters()["device_errors"] == 0
 
 
-@pytest.mark.parametrize("level", ["graze64", "silhouette64"])
-def test_precision_form_on_grazing_rays(rt, torus, torus_gpu, oracle_mod, torch, level):
+def test_precision_form_on_grazing_rays(rt, torus, torus_gpu, oracle_mod, torch):
     """FP32 + FP64 polish with the FP64 fat-line bounds of near-grazing
-    candidates (FP32_GRAZE64 at 30 degrees, FP32_SILHOUETTE64 at 5) against
-    the pure-FP64 GPU search on grazing rays: the plain FP32 search (the
-    reference's arithmetic) loses ~1% of these hits, the precision forms keep
-    hit/miss within 1e-3; the oracle's restatement of the same variant agrees
-    on hit/miss."""
-    prec = rt.FP32_GRAZE64 if level == "graze64" else rt.FP32_SILHOUETTE64
-    gs = oracle_mod.GRAZE_30 if level == "graze64" else oracle_mod.GRAZE_5
+    candidates (FP32_GRAZE64) against the pure-FP64 GPU search on grazing
+    rays: the plain FP32 search (the reference's arithmetic) loses ~1% of
+    these hits, the precision form keeps hit/miss within 1e-3; the oracle's
+    restatement of the same variant agrees on hit/miss."""
+    level = "graze64"
+    prec = rt.FP32_GRAZE64
+    gs = oracle_mod.GRAZE_30
     host_rays = S.grazing_rays(torus.surfaces[0], 1 << 14, seed=12)
     rays = torch.from_numpy(host_rays).cuda()
     ref = host(torus_gpu.intersect(rays, precision=rt.FP64))
@@ -91,7 +90,7 @@ def test_precision_form_on_grazing_rays(rt, torus, torus_gpu, oracle_mod, torch,
     assert torus_gpu.counters()["device_errors"] & 1 == 0
 
 
-@pytest.mark.parametrize("prec_name", ["FP32_POLISH64", "FP32_GRAZE64", "FP32_SILHOUETTE64"])
+@pytest.mark.parametrize("prec_name", ["FP32_POLISH64", "FP32_GRAZE64"])
 def test_precision_form_on_camera_rays(rt, torus_gpu, oracle_mod, torch, prec_name):
     """Camera rays: the precision levels keep every hit of the FP64 search and
     t within 1e-5 of it."""
