@@ -159,7 +159,7 @@ int cgs_scene_load(cgs_scene** out, const char* path, int device)
     const uint32_t magic = r.u32(), version = r.u32();
     const uint32_t ns = r.u32(), no = r.u32(), ng = r.u32(), split = r.u32();
     if (!r.ok || magic != kMagic || version != kVersion || ng == 0 || no == 0 ||
-        (split != CGS_SPLIT_REFERENCE && split != CGS_SPLIT_LONGEST) || uint64_t(ns + no + ng) * 8 > r.left)
+        (split != CGS_SPLIT_REFERENCE && split != CGS_SPLIT_LONGEST && split != CGS_SPLIT_MIRROR) || uint64_t(ns + no + ng) * 8 > r.left)
     {
         std::fclose(f);
         return CGS_ERR_INVALID_ARGUMENT;

@@ -119,8 +119,9 @@ DevMaterial to_dev(const cgs_material& m)
 }
 
 // BezierSurface::buildBVH (src/rt/Primitive.cu:199-220): per-patch bounds of
-// the 16 projected points and their mean as the centroid.
-void build_surface_bvh(Surface& s)
+// the 16 projected points and their mean as the centroid; `out` takes the
+// tree (its split_mode set by the caller).
+void build_surface_bvh(const Surface& s, HostBVH& out)
 {
     std::vector<Element> el(s.patchCount());
     for (uint32_t i = 0; i < el.size(); i++)
@@ -138,13 +139,13 @@ void build_surface_bvh(Surface& s)
             for (int k = 0; k < 3; k++) e.centroid[k] = e.centroid[k] + inv * p[k];
         }
     }
-    s.bvh.build(el);
+    out.build(el);
 }
 
 // Scene::buildBVH (src/rt/Scene.cu:218-232) for one group: object bounds of
 // the transformed points (BezierSurface::bounds(M), src/rt/Primitive.cu:172-179),
 // centroid = box centre, element index = the global object id.
-void build_group_bvh(cgs_scene* sc, Group& g)
+void build_group_bvh(const cgs_scene* sc, const Group& g, HostBVH& out)
 {
     std::vector<Element> el(g.objects.size());
     for (uint32_t i = 0; i < el.size(); i++)
@@ -167,7 +168,7 @@ void build_group_bvh(cgs_scene* sc, Group& g)
         el[i].bounds = b;
         for (int k = 0; k < 3; k++) el[i].centroid[k] = 0.5f * (b.lo[k] + b.hi[k]);
     }
-    g.top.build(el);
+    out.build(el);
 }
 
 void pack_nodes(const HostBVH& b, std::vector<float4>& out)
@@ -535,6 +536,45 @@ int hash_all(cgs_scene* sc, cudaStream_t stream)
 
 Group& current_group(cgs_scene* s) { return s->groups[s->current]; }
 
+// The exported form of BVH k of a mirrored store (CGS_SPLIT_MIRROR): the
+// reference-topology tree, built again on the host, and, once the store is
+// hashed, its perfect-hash table from the same device build as the store's
+// (cgs_perfect_hash_build) into temporary buffers.  params = A, B, N, mask.
+int mirror_export(const cgs_scene* s, uint32_t k, HostBVH& ref, std::vector<uint32_t>& table,
+                  std::vector<uint32_t>& disp, uint32_t params[4])
+{
+    const size_t ns = s->surfaces.size();
+    ref.split_mode = CGS_SPLIT_REFERENCE;
+    if (k < ns) build_surface_bvh(s->surfaces[k], ref);
+    else build_group_bvh(s, s->groups[k - ns], ref);
+    if (ref.emptyLeaf) return CGS_ERR_EMPTY_LEAF;
+    params[0] = params[1] = params[2] = params[3] = 0;
+    table.clear();
+    disp.clear();
+    if (!s->hashed) return CGS_OK;
+    CGS_TRY(cudaSetDevice(s->device));
+    const uint32_t n = uint32_t(ref.keys.size());
+    const uint32_t dcap = displ_size(n), tcap = table_capacity(n);
+    struct Temp
+    {
+        DBuf<uint32_t> keys, disp, table;
+        ~Temp() { keys.release(); disp.release(); table.release(); }
+    } d;
+    CGS_TRY(d.keys.reserve(n));
+    CGS_TRY(d.disp.reserve(dcap));
+    CGS_TRY(d.table.reserve(tcap));
+    uint32_t p5[5] = {};
+    CGS_TRY(cudaMemcpy(d.keys.p, ref.keys.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    if (int r = cgs_perfect_hash_build(d.keys.p, n, d.disp.p, dcap, d.table.p, tcap, p5, nullptr)) return r;
+    if (p5[2] > tcap || size_t(p5[3]) + 1 > dcap) return CGS_ERR_HASH_FAILED;
+    table.resize(p5[2]);
+    disp.resize(size_t(p5[3]) + 1);
+    CGS_TRY(cudaMemcpy(disp.data(), d.disp.p, disp.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CGS_TRY(cudaMemcpy(table.data(), d.table.p, table.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < 4; j++) params[j] = p5[j];
+    return CGS_OK;
+}
+
 bool bvh_index(const cgs_scene* s, int32_t which, uint32_t& k)
 {
     if (which >= 0)
@@ -718,7 +758,8 @@ int cgs_scene_set_environment(cgs_scene* s, const float bg[3], const float amb[3
 
 int cgs_scene_set_bvh_split(cgs_scene* s, int mode)
 {
-    if (!s || (mode != CGS_SPLIT_REFERENCE && mode != CGS_SPLIT_LONGEST)) return CGS_ERR_INVALID_ARGUMENT;
+    if (!s || (mode != CGS_SPLIT_REFERENCE && mode != CGS_SPLIT_LONGEST && mode != CGS_SPLIT_MIRROR))
+        return CGS_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(s->mu);
     if (s->splitMode != mode) s->bvhBuilt = s->uploaded = s->hashed = false;
     s->splitMode = mode;
@@ -749,15 +790,17 @@ int cgs_bvh_build(cgs_scene* s)
         for (size_t w; (w = next.fetch_add(1)) < work.size();)
         {
             const size_t i = work[w].second;
+            // a mirrored store traverses the longest-axis build
+            const int mode = s->splitMode == CGS_SPLIT_MIRROR ? CGS_SPLIT_LONGEST : s->splitMode;
             if (i < ns)
             {
-                s->surfaces[i].bvh.split_mode = s->splitMode;
-                build_surface_bvh(s->surfaces[i]);
+                s->surfaces[i].bvh.split_mode = mode;
+                build_surface_bvh(s->surfaces[i], s->surfaces[i].bvh);
             }
             else
             {
-                s->groups[i - ns].top.split_mode = s->splitMode;
-                build_group_bvh(s, s->groups[i - ns]);
+                s->groups[i - ns].top.split_mode = mode;
+                build_group_bvh(s, s->groups[i - ns], s->groups[i - ns].top);
             }
         }
     };
@@ -814,6 +857,19 @@ int cgs_bvh_sizes(const cgs_scene* s, int32_t which, uint32_t sizes[5])
     if (!s->bvhBuilt) return CGS_ERR_NOT_BUILT;
     uint32_t k;
     if (!bvh_index(s, which, k)) return CGS_ERR_INVALID_ARGUMENT;
+    if (s->splitMode == CGS_SPLIT_MIRROR)
+    {
+        HostBVH ref;
+        std::vector<uint32_t> table, disp;
+        uint32_t params[4];
+        if (int r = mirror_export(s, k, ref, table, disp, params)) return r;
+        sizes[0] = uint32_t(ref.nodes.size());
+        sizes[1] = uint32_t(ref.indices.size());
+        sizes[2] = params[2];
+        sizes[3] = displ_size(uint32_t(ref.keys.size()));
+        sizes[4] = uint32_t(ref.keys.size());
+        return CGS_OK;
+    }
     const HostBVH& b = s->bvh(k);
     sizes[0] = uint32_t(b.nodes.size());
     sizes[1] = uint32_t(b.indices.size());
@@ -830,7 +886,13 @@ int cgs_bvh_export(const cgs_scene* s, int32_t which, uint32_t* nodes, uint32_t*
     if (!s->bvhBuilt) return CGS_ERR_NOT_BUILT;
     uint32_t k;
     if (!bvh_index(s, which, k)) return CGS_ERR_INVALID_ARGUMENT;
-    const HostBVH& b = s->bvh(k);
+    HostBVH ref;
+    std::vector<uint32_t> mtable, mdisp;
+    uint32_t mparams[4] = {};
+    const bool mirror = s->splitMode == CGS_SPLIT_MIRROR;
+    if (mirror)
+        if (int r = mirror_export(s, k, ref, mtable, mdisp, mparams)) return r;
+    const HostBVH& b = mirror ? ref : s->bvh(k);
     if (nodes)
         for (size_t i = 0; i < b.nodes.size(); i++)
         {
@@ -844,7 +906,13 @@ int cgs_bvh_export(const cgs_scene* s, int32_t which, uint32_t* nodes, uint32_t*
         }
     if (keys) std::copy(b.keys.begin(), b.keys.end(), keys);
     if (indices) std::copy(b.indices.begin(), b.indices.end(), indices);
-    if (s->hashed)
+    if (mirror)
+    {
+        if (s->hashed && table) std::copy(mtable.begin(), mtable.end(), table);
+        if (s->hashed && disp) std::copy(mdisp.begin(), mdisp.end(), disp);
+        if (params) std::copy(mparams, mparams + 4, params);
+    }
+    else if (s->hashed)
     {
         CGS_TRY(cudaSetDevice(s->device));
         const DevBVH& d = s->hbvh[k];

@@ -25,7 +25,7 @@ from ._capi import check
 CLIP, SUBDIV = 0, 1
 FP32, FP32_POLISH64, FP64, FP32_GRAZE64 = 0, 1, 2, 3
 PLAIN, WAVEFRONT = 0, 1
-SPLIT_REFERENCE, SPLIT_LONGEST = 0, 1
+SPLIT_REFERENCE, SPLIT_LONGEST, SPLIT_MIRROR = 0, 1, 2
 MIRROR, MONTE_CARLO = 0, 1
 DEFAULT_TOL = 2.0 ** -12
 

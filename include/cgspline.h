@@ -54,8 +54,12 @@ enum cgs_precision { CGS_PREC_FP32 = 0, CGS_PREC_FP32_POLISH64 = 1, CGS_PREC_FP6
  * box that is never inflated (src/rt/BVH.cpp:46-52) and so always y -- the
  * reference's topology, bit for bit.  LONGEST: the longest axis of the
  * elements' centroid box, everything else unchanged: the same hits (up to
- * ties between equally distant candidates) with far fewer node visits. */
-enum cgs_bvh_split { CGS_SPLIT_REFERENCE = 0, CGS_SPLIT_LONGEST = 1 };
+ * ties between equally distant candidates) with far fewer node visits.
+ * MIRROR: queries and renders traverse the LONGEST build, while
+ * cgs_bvh_sizes / cgs_bvh_export give the REFERENCE topology and its hash
+ * table (built again on the host, and hashed by cgs_perfect_hash_build, at
+ * each call). */
+enum cgs_bvh_split { CGS_SPLIT_REFERENCE = 0, CGS_SPLIT_LONGEST = 1, CGS_SPLIT_MIRROR = 2 };
 /* PLAIN: one thread per pixel runs the whole bounce chain (the reference's
  * launch shape, src/rt/RayTracer.cu:171-178).  WAVEFRONT: persistent,
  * stage-separated kernels over compacted ray queues. */

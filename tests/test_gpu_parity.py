@@ -315,6 +315,38 @@ def test_longest_axis_split_bit_exact_and_same_hits(rt, c2_small, c2_small_gpu, 
     assert (r1["patch"] != r2["patch"])[hit].mean() < 1e-3
 
 
+@pytest.mark.parametrize("scene", ["torus", "union"])
+def test_mirror_split_exports_reference_and_traverses_longest(rt, c2_small, torch, scene):
+    """CGS_SPLIT_MIRROR: cgs_bvh_sizes / cgs_bvh_export give the reference
+    topology and its hash table bit for bit (those of a reference-split
+    store), while queries and renders run on the longest-axis build, so
+    their results equal a longest-split store's bit for bit."""
+    if scene == "torus":
+        sc, cam = c2_small, S.camera_c2()
+    else:
+        sc, cam = S.scene_c4(3, max_patches=4096), S.camera_c4(3)[0]
+    ref, lon, mir = (rt.GpuScene(sc, split=k) for k in (rt.SPLIT_REFERENCE, rt.SPLIT_LONGEST, rt.SPLIT_MIRROR))
+    for which in list(range(len(sc.surfaces))) + [-1]:
+        assert mir.bvh_sizes(which) == ref.bvh_sizes(which)
+        a, b = mir.bvh(which), ref.bvh(which)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (which, k)
+    rays = rt.camera_rays(cam, 160, 90)
+    for any_hit in (False, True):
+        a, b = to_host(mir.intersect(rays, any_hit=any_hit)), to_host(lon.intersect(rays, any_hit=any_hit))
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (any_hit, k)
+    frames = []
+    for g in (mir, lon):
+        f = rt.Frame(96, 54)
+        rt.RayTracer(rt.Options(recursion_depth=1)).render(f, cam, g)
+        torch.cuda.synchronize()
+        frames.append(f.rgba())
+    assert np.array_equal(frames[0], frames[1])
+    for g in (ref, lon, mir):
+        g.close()
+
+
 @pytest.mark.parametrize("split", [0, 1])
 def test_union_scene_hits_match_oracle_across_list_chunks(rt, oracle_mod, torch, split):
     """A seeded union of 52 displaced cube-spheres and tori (3,258 patches):
