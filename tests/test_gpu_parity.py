@@ -316,11 +316,12 @@ def test_longest_axis_split_bit_exact_and_same_hits(rt, c2_small, c2_small_gpu, 
 
 
 @pytest.mark.parametrize("scene", ["torus", "union"])
-def test_mirror_split_exports_reference_and_traverses_longest(rt, c2_small, torch, scene):
+def test_mirror_split_exports_reference_and_traverses_longest(rt, c2_small, torch, scene, tmp_path):
     """CGS_SPLIT_MIRROR: cgs_bvh_sizes / cgs_bvh_export give the reference
     topology and its hash table bit for bit (those of a reference-split
     store), while queries and renders run on the longest-axis build, so
-    their results equal a longest-split store's bit for bit."""
+    their results equal a longest-split store's bit for bit; a mirrored
+    store saved and loaded again keeps both."""
     if scene == "torus":
         sc, cam = c2_small, S.camera_c2()
     else:
@@ -343,7 +344,16 @@ def test_mirror_split_exports_reference_and_traverses_longest(rt, c2_small, torc
         torch.cuda.synchronize()
         frames.append(f.rgba())
     assert np.array_equal(frames[0], frames[1])
-    for g in (ref, lon, mir):
+    mir.save(str(tmp_path / "mirror.cgs"))
+    back = rt.GpuScene.load(str(tmp_path / "mirror.cgs"))
+    for which in list(range(len(sc.surfaces))) + [-1]:
+        a, b = back.bvh(which), ref.bvh(which)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), ("loaded", which, k)
+    a, b = to_host(back.intersect(rays)), to_host(lon.intersect(rays))
+    for k in a:
+        assert np.array_equal(a[k], b[k]), ("loaded", k)
+    for g in (ref, lon, mir, back):
         g.close()
 
 
