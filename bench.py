@@ -454,18 +454,31 @@ def batching_leg(rt, scenes, torch, dev, stream, prec, flush, steps=3):
     shape), back to back; both on the reference's BVH topology, and the
     batched path again on the longest-axis build, with the FP32 + FP64-polish
     form and with the full precision form (FP64 fat-line bounds for
-    near-grazing candidates added)."""
+    near-grazing candidates added).  The longest-axis legs run on a mirrored
+    store (CGS_SPLIT_MIRROR), which exports the reference topology."""
+    import numpy as np
     t0 = time.perf_counter()
     scs = [scenes.scene_c4(i) for i in range(64)]
     cams = [scenes.camera_c4(i) for i in range(64)]
     gen_s = time.perf_counter() - t0
     out = {"scenes": 64, "patches": int(sum(s.patch_count for s in scs)),
            "primary_rays": int(sum(side * side for _, side in cams)), "scene_gen_s": gen_s}
-    for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_LONGEST)):
+    # the longest-axis legs run on a mirrored store (CGS_SPLIT_MIRROR): it traverses the
+    # longest-axis build and exports the reference topology, checked here on two BVHs
+    out["split_longest_store"] = "CGS_SPLIT_MIRROR"
+    ref_export = {}
+    for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_MIRROR)):
         store, tm = store_build(rt, scs, dev, split)
         out[f"store_build_s_{split_name}"] = tm["total_s"]
         out[f"store_build_{split_name}"] = tm
         out["footprint_mb"] = store.footprint() / 2 ** 20
+        for w in (0, -1):
+            b = store.bvh(w)
+            if split == rt.SPLIT_REFERENCE:
+                ref_export[w] = b
+            else:
+                out["mirror_export_equals_reference"] = out.get("mirror_export_equals_reference", True) and all(
+                    np.array_equal(b[k], ref_export[w][k]) for k in b)
         reqs = [rt.Request.alloc(i, c, side, side, 1, DEPTH, device=dev.index or 0)
                 for i, (c, side) in enumerate(cams)]
         # the autotuner picks the engine settings on this batch (outside the timed region)
@@ -531,7 +544,8 @@ def serving_stream(n, seed=9):
 def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=40, slots=2, budget_gb=96):
     """32 resident scenes (1K..1M patches), a Poisson stream of nreq requests
     per rate through the continuous-batching server (reference and
-    longest-axis BVH builds) and through the plain server (one request per
+    longest-axis BVH builds, the latter a mirrored store that exports the
+    reference topology) and through the plain server (one request per
     launch, one at a time, reference build); p50 / p99 latency from submit to
     completion, and rays/s over the stream.  The engine settings are the ones
     in force (bench.py's batching leg leaves its autotuned pick)."""
@@ -544,7 +558,8 @@ def serving_leg(rt, scenes, torch, dev, prec, rates=(50, 200, 1000, 2000), nreq=
     out = {"scenes": 32, "patches": int(sum(s.patch_count for s in scs)), "requests_per_rate": nreq,
            "slots": slots, "memory_budget_gb": budget_gb, "scene_gen_s": gen_s, "rates": []}
     stores = {}
-    for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_LONGEST)):
+    out["split_longest_store"] = "CGS_SPLIT_MIRROR"
+    for split_name, split in (("reference", rt.SPLIT_REFERENCE), ("longest", rt.SPLIT_MIRROR)):
         stores[split_name], tm = store_build(rt, scs, dev, split)
         out[f"store_build_s_{split_name}"] = tm["total_s"]
         out[f"store_build_{split_name}"] = tm
