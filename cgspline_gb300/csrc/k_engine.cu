@@ -444,6 +444,7 @@ __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_r
     ClipState c;
     HitSink sink {nullptr, f3(0, 0, 0), f3(0, 0, 1), 0.0f, make_float2(0, 0)};
     bool active = false, exhausted = false, clipping = false;
+    bool thief = false;  // any hit: the lane searches an interval taken from another lane's search
     // any hit with E.originLast: sweep 0 searches the candidates whose leaf box
     // holds the ray's origin (entry <= 0) not, sweep 1 only those
     bool sweep = false;
@@ -483,6 +484,66 @@ __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_r
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, active || !exhausted) == 0) break;
+        if constexpr (kAny && !kSub && !kG64)
+        {
+            // The tail of an any-hit launch is a few long searches.  A lane
+            // left without rays takes the bottom (largest) pending interval of
+            // a search in its warp that holds two or more, and searches it as
+            // that search would after popping it: the same sub-net, derived
+            // from the projected net, and the same cut side.  The searched
+            // intervals are the same, so the roots found are; an any-hit
+            // answer needs one of them, and whichever lane finds it marks
+            // the ray occluded (writes of "occluded" never clear it).
+            const unsigned idleM = __ballot_sync(0xFFFFFFFFu, exhausted && !active);
+            const unsigned richM = __ballot_sync(0xFFFFFFFFu, clipping && !c.fresh && c.sl >= 2 && c.sl <= 30);
+            if (idleM && richM)
+            {
+                const unsigned lane = lane_id(), below = (1u << lane) - 1u;
+                const int pairs = min(__popc(idleM), __popc(richM));
+                const int idleRank = __popc(idleM & below), richRank = __popc(richM & below);
+                const bool isThief = ((idleM >> lane) & 1u) && idleRank < pairs;
+                const bool isVictim = ((richM >> lane) & 1u) && richRank < pairs;
+                const int src = isThief ? int(__fns(richM, 0, idleRank + 1)) : int(lane);
+                float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                int bit = 0;
+                if (isVictim)
+                {
+                    // entry i's cut side is bit (sl - i) of the bit stack; the
+                    // bits above the bottom entry's are clear
+                    e = stack[0];
+                    bit = (c.cutsideStack >> c.sl) & 1;
+                    c.cutsideStack &= ~(1 << c.sl);
+                    for (int i = 1; i < c.sl; i++) stack[i - 1] = stack[i];
+                    c.sl--;
+                }
+                const float4 se = make_float4(__shfl_sync(0xFFFFFFFFu, e.x, src), __shfl_sync(0xFFFFFFFFu, e.y, src),
+                                              __shfl_sync(0xFFFFFFFFu, e.z, src), __shfl_sync(0xFFFFFFFFu, e.w, src));
+                const int sbit = __shfl_sync(0xFFFFFFFFu, bit, src);
+                const uint32_t srid = __shfl_sync(0xFFFFFFFFu, rid, src);
+                const unsigned long long sp =
+                    __shfl_sync(0xFFFFFFFFu, (unsigned long long)reinterpret_cast<uintptr_t>(sink.P), src);
+                const float3 so = f3(__shfl_sync(0xFFFFFFFFu, sink.o.x, src), __shfl_sync(0xFFFFFFFFu, sink.o.y, src),
+                                     __shfl_sync(0xFFFFFFFFu, sink.o.z, src));
+                const float3 sd = f3(__shfl_sync(0xFFFFFFFFu, sink.d.x, src), __shfl_sync(0xFFFFFFFFu, sink.d.y, src),
+                                     __shfl_sync(0xFFFFFFFFu, sink.d.z, src));
+                const float sdist = __shfl_sync(0xFFFFFFFFu, sink.dist, src);
+                const float stol = __shfl_sync(0xFFFFFFFFu, c.tol, src);
+                if (isThief)
+                {
+                    rid = srid;
+                    sink.P = reinterpret_cast<const float4*>(uintptr_t(sp));
+                    sink.o = so; sink.d = sd; sink.dist = sdist; sink.uv = make_float2(0.0f, 0.0f);
+                    c.emin = make_float2(se.x, se.y);
+                    c.emax = make_float2(se.z, se.w);
+                    c.cutsideStack = sbit; c.sl = 0; c.it = 0; c.tol = stol;
+                    c.found = false; c.b64 = false; c.fresh = false; c.tposed = false;
+                    project_net(c.buf, sink.P, sink.o, sink.d);
+                    subpatchU(c.buf, se.x, se.z);
+                    subpatchV(c.buf, se.y, se.w);
+                    active = true; clipping = true; thief = true;
+                }
+            }
+        }
         if (!active) continue;
 
         bool finished = false;
@@ -590,6 +651,11 @@ __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_r
         {
             active = false;
             E.count[rid] = 0;
+        }
+        if (kAny && thief && !clipping)
+        {
+            thief = false;
+            active = false;
         }
     }
     flush_counters(cnt, lc, 0);

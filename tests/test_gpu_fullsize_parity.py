@@ -140,3 +140,44 @@ def test_fullsize_grazing_rays(rt, torch, oracle_mod):
     differ = (p["patch"] != od["patch"]) | ((od["patch"] >= 0) & (p["t"] != od["t"]))
     assert int(differ.sum()) <= 8, int(differ.sum())
     parity.close()
+
+
+def test_fullsize_shadow_rays(rt, torch, oracle_mod):
+    """Shadow rays of the C2 torus (16,384 patches) from the hit points of a
+    960x540 view toward two point lights: the any-hit engine, whose idle lanes
+    take pending intervals of long clip searches at the end of a launch, gives
+    the oracle's decisions on every ray -- the parity build against the
+    restatement of the reference's GPU clip (identical), the product build
+    (multiply-add contraction) on all but 1e-4 of the rays.  These rays leave
+    the surface, many at grazing angles, where contraction alone moves a few
+    near-tangent decisions."""
+    from cgspline_gb300 import _capi
+    sc = S.scene_c2()
+    o = oracle_mod.OracleScene(sc)
+    cam = oracle_mod.camera_rays(S.camera_c2(), 960, 540)
+    h = o.intersect(cam)
+    hit = h["patch"] >= 0
+    P = cam[0:3, hit] + h["t"][hit] * cam[3:6, hit]
+    shadow = []
+    for light in ((4.0, 8.0, 6.0), (-6.0, 3.0, -2.0)):
+        L = np.asarray(light, np.float32)[:, None] - P
+        dist = np.linalg.norm(L, axis=0, keepdims=True)
+        L = L / dist
+        shadow.append(np.concatenate([P + 1e-4 * L, L, dist], 0))
+    rays_h = np.ascontiguousarray(np.concatenate(shadow, 1), np.float32)
+    rays = torch.from_numpy(rays_h).cuda()
+    assert rays_h.shape[1] > 250_000
+    od = o.intersect(rays_h, method=oracle_mod.CLIP_DEVICE, any_hit=True)
+    oh = o.intersect(rays_h, any_hit=True)
+    assert 0.05 < float((oh["patch"] >= 0).mean()) < 0.95
+    parity = rt.GpuScene(sc, lib_path=_capi.LIB_NOFMA_PATH)
+    p = host(parity.intersect(rays, any_hit=True))
+    assert np.array_equal(p["patch"] >= 0, od["patch"] >= 0)
+    assert parity.counters()["device_errors"] == 0
+    parity.close()
+    g = rt.GpuScene(sc)
+    a = host(g.intersect(rays, any_hit=True))
+    differ = int(((a["patch"] >= 0) != (od["patch"] >= 0)).sum())
+    assert differ <= rays_h.shape[1] // 10_000, differ
+    assert g.counters()["device_errors"] == 0
+    g.close()
