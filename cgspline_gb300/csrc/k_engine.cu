@@ -24,7 +24,9 @@
 // beyond the best t of that moment, so none of its patches can give a
 // strictly closer hit; collecting it anyway changes nothing except for hits
 // within the search tolerance of the current best (near-ties).  Any-hit
-// queries stop at the first patch that reports a hit.
+// queries stop at the first patch that reports a hit; at the end of an
+// any-hit launch, lanes without rays share the pending intervals of the long
+// searches left in their warp.
 //
 // Both kernels refill lanes one ray (k_collect) or one clip iteration
 // (k_resolve) at a time, so heavy-tailed per-ray work does not idle the other
