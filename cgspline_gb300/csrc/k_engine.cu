@@ -490,14 +490,14 @@ __global__ void __launch_bounds__(kResolveThreads, (!kG64 && !kSub) ? 4 : 3) k_r
         {
             // The tail of an any-hit launch is a few long searches.  A lane
             // left without rays takes the bottom (largest) pending interval of
-            // a search in its warp that holds two or more, and searches it as
+            // a search in its warp that holds one or more, and searches it as
             // that search would after popping it: the same sub-net, derived
             // from the projected net, and the same cut side.  The searched
             // intervals are the same, so the roots found are; an any-hit
             // answer needs one of them, and whichever lane finds it marks
             // the ray occluded (writes of "occluded" never clear it).
             const unsigned idleM = __ballot_sync(0xFFFFFFFFu, exhausted && !active);
-            const unsigned richM = __ballot_sync(0xFFFFFFFFu, clipping && !c.fresh && c.sl >= 2 && c.sl <= 30);
+            const unsigned richM = __ballot_sync(0xFFFFFFFFu, clipping && !c.fresh && c.sl >= 1 && c.sl <= 30);
             if (idleM && richM)
             {
                 const unsigned lane = lane_id(), below = (1u << lane) - 1u;
